@@ -1,0 +1,213 @@
+"""gpufs_gb300: a GB300-native GPU file-system layer (GPUfs device API over an
+HBM buffer cache), driven from Python through its C ABI.
+
+The product is native: libgpufs_gb300.so (CUDA, sm_103a) built in-tree by
+gpufs_gb300.build.  This module only binds the C ABI declared in
+include/gpufs_gb300.h with ctypes; there is no Python or CPU fallback, and
+every entry point raises if the native library is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(_HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libgpufs_gb300.so")
+
+O_RDONLY = os.O_RDONLY
+O_WRONLY = os.O_WRONLY
+O_RDWR = os.O_RDWR
+O_CREAT = os.O_CREAT
+# reference flag names (libgpufs/fs_constants.h:86-90)
+O_GRDONLY = O_RDONLY
+O_GWRONLY = O_WRONLY
+O_GCREAT = O_CREAT
+O_GRDWR = O_RDWR
+O_GWRONCE = O_CREAT | O_WRONLY
+
+STAT_NAMES = ["hits", "misses", "evictions", "writebacks", "read_rpcs", "bytes_read_rpc", "opens", "closes",
+              "timeouts", "errors", "conflict_evictions", "host_requests", "host_reads", "host_read_bytes",
+              "host_writes", "host_write_bytes", "host_opens", "host_errors"]
+
+ERR_TIMEOUT, ERR_IO, ERR_NOMEM, ERR_TABLE, ERR_ARG = 1, 2, 4, 8, 16
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("log_page", ctypes.c_uint32), ("max_files", ctypes.c_uint32), ("pool_bytes", ctypes.c_uint64),
+                ("ring_slots", ctypes.c_uint32), ("host_workers", ctypes.c_uint32),
+                ("staging_depth", ctypes.c_uint32), ("pad0", ctypes.c_uint32), ("timeout_ns", ctypes.c_uint64),
+                ("device", ctypes.c_int32), ("pad1", ctypes.c_uint32)]
+
+
+_lib = None
+_c_p = ctypes.c_void_p
+_c_s = ctypes.c_char_p
+_u64 = ctypes.c_uint64
+_i64 = ctypes.c_longlong
+_int = ctypes.c_int
+
+_SIGS = {
+    "gfs_default_config": (None, [ctypes.POINTER(Config)]),
+    "gfs_create": (_int, [ctypes.POINTER(Config), ctypes.POINTER(_c_p)]),
+    "gfs_destroy": (_int, [_c_p]),
+    "gfs_run_handler": (_int, [_c_p, _int]),
+    "gfs_kernel_stream": (_c_p, [_c_p]),
+    "gfs_device_state": (_c_p, [_c_p]),
+    "gfs_page_size": (ctypes.c_uint32, [_c_p]),
+    "gfs_num_frames": (ctypes.c_uint32, [_c_p]),
+    "gfs_pool_base": (_c_p, [_c_p]),
+    "gfs_last_error": (ctypes.c_uint32, [_c_p, _int]),
+    "gfs_get_stats": (_int, [_c_p, ctypes.POINTER(ctypes.c_ulonglong), _int]),
+    "gfs_reset_stats": (_int, [_c_p]),
+    "gfs_set_paused": (_int, [_c_p, _int]),
+    "gfs_inject_read_errors": (_int, [_c_p, _int, _int]),
+    "gfs_pread": (_i64, [_c_p, _c_s, _u64, _u64, _c_p, _int, _int]),
+    "gfs_pread_dev": (_i64, [_c_p, _c_s, _u64, _u64, _c_p, _int, _int, ctypes.POINTER(ctypes.c_float)]),
+    "gfs_pwrite": (_i64, [_c_p, _c_s, _int, _u64, _u64, _c_p, _int, _int]),
+    "gfs_mmap_read": (_i64, [_c_p, _c_s, _u64, _u64, _c_p, _int, _int, _int]),
+    "gfs_fstat_path": (_i64, [_c_p, _c_s]),
+    "gfs_truncate_path": (_int, [_c_p, _c_s, _i64]),
+    "gfs_unlink_path": (_int, [_c_p, _c_s]),
+    "gfs_pwrite_fsync": (_i64, [_c_p, _c_s, _u64, _u64, _c_p]),
+    "gfs_memcopy": (_int, [_c_p, _c_s, _c_s, _int, _int, _int, ctypes.POINTER(ctypes.c_float)]),
+}
+
+
+def lib():
+    """Load libgpufs_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("gpufs_gb300: native library missing (%s); run gpufs_gb300.build.build()" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH, mode=ctypes.RTLD_GLOBAL)
+    for name, (res, args) in _SIGS.items():
+        if hasattr(L, name):
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+    _lib = L
+    return L
+
+
+def _p(path):
+    b = os.fsencode(path)
+    if len(b) >= 64:
+        raise ValueError("path longer than 63 bytes (FILENAME_SIZE): %r" % path)
+    return b
+
+
+class GfsError(OSError):
+    pass
+
+
+def _check(rc, what):
+    if rc < 0:
+        raise GfsError(-rc, "%s failed: %s" % (what, os.strerror(-rc) if -rc < 200 else str(rc)))
+    return rc
+
+
+class Session:
+    """One file-system session on one GPU (initializer() .. delete GPUGlobals)."""
+
+    def __init__(self, log_page=16, pool_bytes=2 << 30, max_files=1024, ring_slots=4096, host_workers=8,
+                 staging_depth=8, timeout_s=30.0, device=0):
+        L = lib()
+        c = Config()
+        L.gfs_default_config(ctypes.byref(c))
+        c.log_page = log_page
+        c.pool_bytes = pool_bytes
+        c.max_files = max_files
+        c.ring_slots = ring_slots
+        c.host_workers = host_workers
+        c.staging_depth = staging_depth
+        c.timeout_ns = int(timeout_s * 1e9)
+        c.device = device
+        h = ctypes.c_void_p()
+        _check(L.gfs_create(ctypes.byref(c), ctypes.byref(h)), "gfs_create")
+        self._h = h
+        self.L = L
+        self.page_size = L.gfs_page_size(h)
+        self.n_frames = L.gfs_num_frames(h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            self.L.gfs_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- device API driven from the host --
+    def pread(self, path, off=0, size=None, nblocks=8, nthreads=256):
+        if size is None:
+            size = max(0, os.path.getsize(path) - off)
+        out = np.empty(size, dtype=np.uint8)
+        n = _check(self.L.gfs_pread(self._h, _p(path), off, size, out.ctypes.data if size else None, nblocks,
+                                    nthreads), "gfs_pread")
+        return out[:n]
+
+    def pread_dev(self, path, off, size, dev_ptr, nblocks=8, nthreads=256):
+        ms = ctypes.c_float(0)
+        n = _check(self.L.gfs_pread_dev(self._h, _p(path), off, size, dev_ptr, nblocks, nthreads, ctypes.byref(ms)),
+                   "gfs_pread_dev")
+        return n, ms.value
+
+    def pwrite(self, path, data, off=0, oflags=O_GWRONCE, nblocks=8, nthreads=256):
+        a = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if not isinstance(data, np.ndarray) else
+                                 data.view(np.uint8).ravel())
+        return _check(self.L.gfs_pwrite(self._h, _p(path), oflags, off, a.size, a.ctypes.data if a.size else None,
+                                        nblocks, nthreads), "gfs_pwrite")
+
+    def pwrite_fsync(self, path, data, off=0):
+        a = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8))
+        return _check(self.L.gfs_pwrite_fsync(self._h, _p(path), off, a.size, a.ctypes.data), "gfs_pwrite_fsync")
+
+    def mmap_read(self, path, off=0, size=None, nblocks=8, nthreads=256, warp_api=False):
+        if size is None:
+            size = max(0, os.path.getsize(path) - off)
+        out = np.empty(size, dtype=np.uint8)
+        n = _check(self.L.gfs_mmap_read(self._h, _p(path), off, size, out.ctypes.data if size else None, nblocks,
+                                        nthreads, 1 if warp_api else 0), "gfs_mmap_read")
+        return out[:n]
+
+    def fstat(self, path):
+        return _check(self.L.gfs_fstat_path(self._h, _p(path)), "gfs_fstat_path")
+
+    def truncate(self, path, size):
+        return _check(self.L.gfs_truncate_path(self._h, _p(path), size), "gfs_truncate_path")
+
+    def unlink(self, path):
+        return _check(self.L.gfs_unlink_path(self._h, _p(path)), "gfs_unlink_path")
+
+    def memcopy(self, src, dst, nblocks=112, nthreads=256, mode=0):
+        ms = ctypes.c_float(0)
+        _check(self.L.gfs_memcopy(self._h, _p(src), _p(dst), nblocks, nthreads, mode, ctypes.byref(ms)),
+               "gfs_memcopy")
+        return ms.value
+
+    # -- introspection / fault injection --
+    def stats(self):
+        arr = (ctypes.c_ulonglong * len(STAT_NAMES))()
+        n = self.L.gfs_get_stats(self._h, arr, len(STAT_NAMES))
+        return {STAT_NAMES[i]: int(arr[i]) for i in range(n)}
+
+    def reset_stats(self):
+        self.L.gfs_reset_stats(self._h)
+
+    def last_error(self, clear=True):
+        return int(self.L.gfs_last_error(self._h, 1 if clear else 0))
+
+    def set_paused(self, paused):
+        self.L.gfs_set_paused(self._h, 1 if paused else 0)
+
+    def inject_read_errors(self, count, err=5):
+        self.L.gfs_inject_read_errors(self._h, count, err)

@@ -1,0 +1,502 @@
+/*
+ * Block- and warp-collective file operations (the bodies behind the
+ * reference-named device API).  Every thread of the calling block (warp for
+ * the _warp forms) must call with the same arguments, as in the reference
+ * (libgpufs/fs_calls.cu:685-687: "pread is expected to be issued by all
+ * threads in a thread block with the same parameters").
+ *
+ *   blk_read   <- gread        fs_calls.cu:689-737
+ *   blk_write  <- gwrite       fs_calls.cu:739-802
+ *   blk_mmap   <- gmmap        fs_calls.cu:422-481
+ *   blk_munmap <- gmunmap      fs_calls.cu:385-401
+ *   blk_flush  <- gfsync/flush fs_calls.cu:107-125, fs_structures.cu:263-298
+ *   blk_close  <- gclose       fs_calls.cu:35-105
+ *
+ * GB300 changes: up to 32 pages of one request are faulted in parallel, one
+ * lane per page (warp-cooperative lookup), so a block keeps up to 32 host
+ * reads in flight; then all warps copy, each warp a page segment with
+ * 16-byte cache-global vectors.  Reads clamp at end of file and return the
+ * byte count (the reference returns `size` whatever it read).
+ */
+#ifndef GFS_BLOCK_CUH
+#define GFS_BLOCK_CUH
+
+#include "gfs_device.cuh"
+
+namespace gfsd {
+namespace { /* internal linkage: every TU gets its own copy */
+
+__device__ __forceinline__ int blk_tid() {
+    return threadIdx.x + threadIdx.y * blockDim.x + threadIdx.z * blockDim.x * blockDim.y;
+}
+__device__ __forceinline__ int blk_nthr() { return blockDim.x * blockDim.y * blockDim.z; }
+
+/* group copy: threads [rank] of a group of `gsize` (<= 32, one warp) */
+__device__ __forceinline__ void grp_copy(uint8_t* dst, const uint8_t* src, size_t n, int rank, int gsize) {
+    if (gsize == 32) { warp_copy(dst, src, n, rank); return; }
+    for (size_t k = (size_t)rank; k < n; k += (size_t)gsize) dst[k] = src[k];
+}
+__device__ __forceinline__ void grp_zero(uint8_t* dst, size_t n, int rank, int gsize) {
+    if (gsize == 32) { warp_zero(dst, n, rank); return; }
+    for (size_t k = (size_t)rank; k < n; k += (size_t)gsize) dst[k] = 0;
+}
+
+/* Copy a round of `npages` page segments between frames and a linear user
+ * buffer.  Segment j covers file bytes [max(pos, page_j), min(end, page_j+1)).
+ * to_frame selects the direction. */
+__device__ __forceinline__ void blk_copy_round(gfs_state* S, const int* frames, uint32_t first, int npages,
+                                               uint64_t pos, uint64_t end, uint8_t* ubuf, uint64_t ubase,
+                                               bool to_frame) {
+    const int tid = blk_tid(), nthr = blk_nthr();
+    const int warp = tid >> 5, lane = tid & 31;
+    const int nwarps = (nthr + 31) >> 5;
+    const int gsize = (warp == nwarps - 1) ? (nthr - 32 * warp) : 32;
+    const uint32_t lp = S->log_page;
+    const uint64_t page = 1ull << lp;
+    int parts = nwarps / npages;
+    if (parts < 1) parts = 1;
+    const int items = npages * parts;
+    for (int k = warp; k < items; k += nwarps) {
+        int j = k / parts, p = k % parts;
+        uint64_t pstart = ((uint64_t)(first + (uint32_t)j)) << lp;
+        uint64_t s0 = pos > pstart ? pos : pstart;
+        uint64_t e0 = end < pstart + page ? end : pstart + page;
+        if (e0 <= s0) continue;
+        uint64_t len = e0 - s0;
+        uint64_t plen = ((len + (uint64_t)parts - 1) / (uint64_t)parts + 511u) & ~511ull;
+        uint64_t a = (uint64_t)p * plen;
+        if (a >= len) continue;
+        uint64_t b = a + plen < len ? a + plen : len;
+        uint8_t* fptr = frame_data(S, (uint32_t)frames[j]) + (s0 - pstart) + a;
+        uint8_t* uptr = ubuf + (s0 - ubase) + a;
+        if (to_frame) grp_copy(fptr, uptr, b - a, lane, gsize);
+        else grp_copy(uptr, fptr, b - a, lane, gsize);
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* read                                                                */
+/* ------------------------------------------------------------------ */
+__device__ __noinline__ long long blk_read(gfs_state* S, int fd, uint64_t off, uint64_t size, uint8_t* buf) {
+    __shared__ PinFile s_pf;
+    __shared__ uint64_t s_off, s_size;
+    __shared__ uint8_t* s_buf;
+    __shared__ int s_frames[32];
+    __shared__ int s_err, s_round, s_retry;
+    const int tid = blk_tid(), nthr = blk_nthr();
+    const unsigned m0 = nthr >= 32 ? 0xFFFFFFFFu : ((1u << nthr) - 1u); /* lanes of warp 0 */
+    __syncthreads();
+    if (tid == 0) {
+        s_err = 0;
+        s_round = nthr < 32 ? nthr : 32;
+        if (fd < 0 || (uint32_t)fd >= S->n_files || sstatus(ld_acq(&S->files[fd].st)) != GFS_SS_OPEN) {
+            s_err = -GFS_EBADF;
+        } else {
+            s_pf = pin_file(S, fd);
+            uint64_t fsz = s_pf.size;
+            s_size = off >= fsz ? 0 : (size < fsz - off ? size : fsz - off);
+        }
+        s_off = off;
+        s_buf = buf;
+    }
+    __syncthreads();
+    if (s_err) return s_err;
+    const uint64_t total = s_size, base = s_off;
+    const uint32_t lp = S->log_page;
+    uint64_t done = 0;
+    while (done < total) {
+        const uint64_t pos = base + done;
+        const uint32_t first = (uint32_t)(pos >> lp);
+        const uint32_t last = (uint32_t)((base + total - 1) >> lp);
+        int npages = (int)(last - first + 1u);
+        if (npages > s_round) npages = s_round;
+        if (tid < 32) {
+            int r = 0;
+            if (tid < npages) {
+                bool fresh;
+                r = pin_page(S, s_pf, first + (uint32_t)tid, GFS_PIN_READ | (npages > 1 ? GFS_PIN_NOALLOC : 0), &fresh);
+                if (r >= 0 && fresh) {
+                    /* no host bytes behind this page (cannot happen below the
+                     * clamped size of an open file): hand out zeros */
+                    uint32_t* d = (uint32_t*)frame_data(S, (uint32_t)r);
+                    for (uint32_t k = 0; k < (S->page_size >> 2); k++) d[k] = 0u;
+                    publish_valid(S, (uint32_t)r);
+                }
+                s_frames[tid] = r;
+            }
+            unsigned nomem = __ballot_sync(m0, tid < npages && r == -GFS_ENOMEM);
+            unsigned bad = __ballot_sync(m0, tid < npages && r < 0 && r != -GFS_ENOMEM);
+            if (bad || nomem) {
+                if (tid < npages && r >= 0) unpin(S, (uint32_t)r);
+                int e = bad ? __shfl_sync(m0, r, __ffs(bad) - 1) : 0;
+                if (tid == 0) {
+                    s_retry = 1;
+                    if (bad) s_err = e;
+                    else if (npages == 1) s_err = -GFS_ENOMEM;
+                    s_round = s_round > 1 ? s_round / 2 : 1;
+                }
+            } else if (tid == 0) {
+                s_retry = 0;
+            }
+        }
+        __syncthreads();
+        if (s_err) return s_err;
+        if (s_retry) continue;
+        uint64_t pend = ((uint64_t)(first + (uint32_t)npages)) << lp;
+        uint64_t end = base + total < pend ? base + total : pend;
+        blk_copy_round(S, s_frames, first, npages, pos, end, s_buf, base, false);
+        __syncthreads();
+        if (tid < npages) unpin(S, (uint32_t)s_frames[tid]);
+        if (tid == 0) count(S, &S->stats.hits, (unsigned long long)npages);
+        done = end - base;
+        __syncthreads();
+    }
+    return (long long)total;
+}
+
+/* ------------------------------------------------------------------ */
+/* write                                                               */
+/* ------------------------------------------------------------------ */
+__device__ __noinline__ long long blk_write(gfs_state* S, int fd, uint64_t off, uint64_t size, const uint8_t* buf) {
+    __shared__ PinFile s_pf;
+    __shared__ uint64_t s_off, s_size;
+    __shared__ const uint8_t* s_buf;
+    __shared__ int s_frames[32];
+    __shared__ unsigned s_fresh;
+    __shared__ int s_err, s_round, s_retry;
+    const int tid = blk_tid(), nthr = blk_nthr();
+    const unsigned m0 = nthr >= 32 ? 0xFFFFFFFFu : ((1u << nthr) - 1u); /* lanes of warp 0 */
+    __syncthreads();
+    if (tid == 0) {
+        s_err = 0;
+        s_round = nthr < 32 ? nthr : 32;
+        if (fd < 0 || (uint32_t)fd >= S->n_files || sstatus(ld_acq(&S->files[fd].st)) != GFS_SS_OPEN) {
+            s_err = -GFS_EBADF;
+        } else {
+            s_pf = pin_file(S, fd);
+            if (s_pf.oflags == O_GRDONLY) s_err = -GFS_EBADF;
+        }
+        s_off = off;
+        s_size = size;
+        s_buf = buf;
+    }
+    __syncthreads();
+    if (s_err) return s_err;
+    const uint64_t total = s_size, base = s_off;
+    const uint32_t lp = S->log_page;
+    const uint64_t page = 1ull << lp;
+    uint64_t done = 0;
+    while (done < total) {
+        const uint64_t pos = base + done;
+        const uint32_t first = (uint32_t)(pos >> lp);
+        const uint32_t last = (uint32_t)((base + total - 1) >> lp);
+        int npages = (int)(last - first + 1u);
+        if (npages > s_round) npages = s_round;
+        if (tid < 32) {
+            int r = 0;
+            bool fresh = false;
+            if (tid < npages) {
+                uint64_t pst = ((uint64_t)(first + (uint32_t)tid)) << lp;
+                bool full = pos <= pst && base + total >= pst + page;
+                int mode = full ? GFS_PIN_WFULL : (s_pf.oflags == O_GWRONCE ? GFS_PIN_WONCE : GFS_PIN_WPART);
+                r = pin_page(S, s_pf, first + (uint32_t)tid, mode | (npages > 1 ? GFS_PIN_NOALLOC : 0), &fresh);
+                s_frames[tid] = r;
+            }
+            unsigned fr_mask = __ballot_sync(m0, tid < npages && r >= 0 && fresh);
+            unsigned nomem = __ballot_sync(m0, tid < npages && r == -GFS_ENOMEM);
+            unsigned bad = __ballot_sync(m0, tid < npages && r < 0 && r != -GFS_ENOMEM);
+            if (bad || nomem) {
+                if (tid < npages && r >= 0) {
+                    if (fresh) { /* give back a page we never initialised */
+                        gfs_frame* F = &S->frames[r];
+                        uint64_t k = ld_rlx64(&F->key);
+                        index_remove(S, k, (uint32_t)r);
+                        release_owned(S, (uint32_t)r, GFS_FS_LOADING, 1u);
+                    } else {
+                        unpin(S, (uint32_t)r);
+                    }
+                }
+                int e = bad ? __shfl_sync(m0, r, __ffs(bad) - 1) : 0;
+                if (tid == 0) {
+                    s_retry = 1;
+                    if (bad) s_err = e;
+                    else if (npages == 1) s_err = -GFS_ENOMEM;
+                    s_round = s_round > 1 ? s_round / 2 : 1;
+                }
+            } else if (tid == 0) {
+                s_retry = 0;
+                s_fresh = fr_mask;
+            }
+        }
+        __syncthreads();
+        if (s_err) return s_err;
+        if (s_retry) continue;
+        uint64_t pend = ((uint64_t)(first + (uint32_t)npages)) << lp;
+        uint64_t end = base + total < pend ? base + total : pend;
+        /* zero the uncovered parts of fresh pages */
+        if (s_fresh) {
+            const int warp = tid >> 5, lane = tid & 31, nwarps = (nthr + 31) >> 5;
+            const int gsize = (warp == nwarps - 1) ? (nthr - 32 * warp) : 32;
+            for (int j = warp; j < npages; j += nwarps) {
+                if (!((s_fresh >> j) & 1u)) continue;
+                uint64_t pst = ((uint64_t)(first + (uint32_t)j)) << lp;
+                uint64_t a = pos > pst ? pos - pst : 0;
+                uint64_t b = end < pst + page ? end - pst : page;
+                uint8_t* d = frame_data(S, (uint32_t)s_frames[j]);
+                if (a) grp_zero(d, a, lane, gsize);
+                if (b < page) grp_zero(d + b, page - b, lane, gsize);
+            }
+        }
+        blk_copy_round(S, s_frames, first, npages, pos, end, (uint8_t*)s_buf, base, true);
+        __syncthreads();
+        if (tid < npages) {
+            uint32_t fr = (uint32_t)s_frames[tid];
+            uint64_t pst = ((uint64_t)(first + (uint32_t)tid)) << lp;
+            uint64_t b = end < pst + page ? end - pst : page;
+            atomicMax(&S->frames[fr].content, (uint32_t)b);
+            if ((s_fresh >> tid) & 1u) publish_valid(S, fr);
+            mark_dirty(S, fr);
+            unpin(S, fr);
+        }
+        if (tid == 0) atomicMax((unsigned long long*)&S->files[s_pf.slot].size, (unsigned long long)end);
+        done = end - base;
+        __syncthreads();
+    }
+    return (long long)total;
+}
+
+/* ------------------------------------------------------------------ */
+/* map / unmap                                                         */
+/* ------------------------------------------------------------------ */
+__device__ __forceinline__ int mmap_mode(int oflags) {
+    if (oflags == O_GRDONLY) return GFS_PIN_READ;
+    if (oflags == O_GWRONCE) return GFS_PIN_WONCE;
+    return GFS_PIN_WPART;
+}
+
+/* Single-thread part of a mapping: pin the page holding `off`.  Returns the
+ * frame or -error; *fresh when the caller must zero + publish it. */
+__device__ __forceinline__ int map_pin(gfs_state* S, int fd, uint64_t off, uint64_t size, bool* fresh, int ref) {
+    *fresh = false;
+    if (fd < 0 || (uint32_t)fd >= S->n_files || sstatus(ld_acq(&S->files[fd].st)) != GFS_SS_OPEN) return -GFS_EBADF;
+    PinFile pf = pin_file(S, fd);
+    const uint64_t page = (uint64_t)S->page_size;
+    uint64_t boff = off & (page - 1);
+    if (boff + size > page) { set_error(S, GFS_ERRB_ARG); return -GFS_EINVAL; }
+    if (pf.oflags == O_GRDONLY && off >= pf.size) return -GFS_EINVAL;
+    int r = pin_page(S, pf, (uint32_t)(off >> S->log_page), mmap_mode(pf.oflags), fresh);
+    if (r < 0) return r;
+    if (ref > 1) atomicAdd(&S->frames[r].st, (uint32_t)(ref - 1));
+    if (pf.oflags != O_GRDONLY) {
+        atomicMax(&S->frames[r].content, (uint32_t)(boff + size));
+        atomicMax((unsigned long long*)&S->files[fd].size, (unsigned long long)(off + size));
+    }
+    return r;
+}
+
+__device__ __noinline__ void* blk_mmap(gfs_state* S, int fd, uint64_t off, uint64_t size) {
+    __shared__ int s_r;
+    __shared__ bool s_fresh;
+    const int tid = blk_tid(), nthr = blk_nthr();
+    __syncthreads();
+    if (tid == 0) {
+        bool fr;
+        s_r = map_pin(S, fd, off, size, &fr, 1);
+        s_fresh = fr;
+    }
+    __syncthreads();
+    int r = s_r;
+    if (r < 0) return (void*)-1; /* GMAP_FAILED */
+    if (s_fresh) {
+        const int warp = tid >> 5, lane = tid & 31, nwarps = (nthr + 31) >> 5;
+        const int gsize = (warp == nwarps - 1) ? (nthr - 32 * warp) : 32;
+        uint64_t chunk = ((uint64_t)S->page_size / (uint64_t)nwarps + 15u) & ~15ull;
+        uint64_t a = (uint64_t)warp * chunk;
+        if (a < S->page_size) {
+            uint64_t b = a + chunk < S->page_size ? a + chunk : S->page_size;
+            grp_zero(frame_data(S, (uint32_t)r) + a, b - a, lane, gsize);
+        }
+        __syncthreads();
+        if (tid == 0) publish_valid(S, (uint32_t)r);
+        __syncthreads();
+    }
+    return frame_data(S, (uint32_t)r) + (off & ((uint64_t)S->page_size - 1));
+}
+
+__device__ __forceinline__ int addr_frame(gfs_state* S, const volatile void* addr) {
+    uintptr_t a = (uintptr_t)addr, p = (uintptr_t)S->pool;
+    if (a < p) return -1;
+    uint64_t fr = (uint64_t)(a - p) >> S->log_page;
+    if (fr >= S->n_frames) return -1;
+    return (int)fr;
+}
+
+__device__ __forceinline__ int unmap_one(gfs_state* S, const volatile void* addr, int ref) {
+    int fr = addr_frame(S, addr);
+    if (fr < 0) return -1;
+    uint64_t key = ld_rlx64(&S->frames[fr].key);
+    uint32_t f = key_file(key);
+    if (f < S->n_files && ld_rlx((const uint32_t*)&S->files[f].flags) != (uint32_t)O_GRDONLY) mark_dirty(S, (uint32_t)fr);
+    unpin(S, (uint32_t)fr, (uint32_t)ref);
+    return 0;
+}
+
+__device__ __noinline__ int blk_munmap(gfs_state* S, const volatile void* addr) {
+    __shared__ int s_r;
+    __threadfence();
+    __syncthreads();
+    if (blk_tid() == 0) s_r = unmap_one(S, addr, 1);
+    __syncthreads();
+    return s_r;
+}
+
+/* ------------------------------------------------------------------ */
+/* flush / close / open                                                */
+/* ------------------------------------------------------------------ */
+/* Write back every dirty frame of slot fd, spread over the block's threads
+ * (each thread one frame at a time, so the block keeps many write-backs in
+ * flight).  Returns 0 or the first error. */
+__device__ __noinline__ int blk_flush(gfs_state* S, int fd) {
+    __shared__ int s_err;
+    const int tid = blk_tid(), nthr = blk_nthr();
+    __syncthreads();
+    if (tid == 0) s_err = 0;
+    __syncthreads();
+    gfs_file* fe = &S->files[fd];
+    uint32_t gen = ld_rlx(&fe->gen);
+    int host_fd = (int)ld_rlx((const uint32_t*)&fe->host_fd);
+    int oflags = (int)ld_rlx((const uint32_t*)&fe->flags);
+    uint32_t nwords = (S->n_frames + 31u) >> 5;
+    for (uint32_t w = (uint32_t)tid; w < nwords; w += (uint32_t)nthr) {
+        uint32_t bits = ld_rlx(&S->dirty_bits[w]);
+        while (bits) {
+            uint32_t b = (uint32_t)(__ffs(bits) - 1);
+            bits &= bits - 1u;
+            uint32_t fr = (w << 5) | b;
+            if (key_file(ld_rlx64(&S->frames[fr].key)) != (uint32_t)fd) continue;
+            int rc = flush_frame(S, fr, (uint32_t)fd, gen, host_fd, oflags);
+            if (rc < 0) atomicCAS(&s_err, 0, rc);
+        }
+    }
+    __syncthreads();
+    return s_err;
+}
+
+__device__ __noinline__ int blk_close(gfs_state* S, int fd) {
+    __shared__ int s_r;
+    __syncthreads();
+    if (blk_tid() == 0) s_r = file_close_begin(S, fd);
+    __syncthreads();
+    int r = s_r;
+    if (r <= 0) return r;
+    int fl = blk_flush(S, fd);
+    __syncthreads();
+    if (blk_tid() == 0) {
+        int c = file_close_finish(S, fd);
+        s_r = fl < 0 ? fl : c;
+    }
+    __syncthreads();
+    return s_r;
+}
+
+__device__ __noinline__ int blk_open(gfs_state* S, const char* name, int oflags) {
+    __shared__ int s_r;
+    __syncthreads();
+    if (blk_tid() == 0) s_r = file_open(S, name, oflags);
+    __syncthreads();
+    return s_r;
+}
+
+/* single-thread truncate (reference single_thread_ftruncate, fs_calls.cu:127-140;
+ * the reference only supports size 0).  Dirty pages below a non-zero new size
+ * are written back first; then every cached page of the file is invalidated. */
+__device__ __noinline__ int st_truncate(gfs_state* S, int fd, uint64_t size) {
+    if (fd < 0 || (uint32_t)fd >= S->n_files) return -GFS_EBADF;
+    gfs_file* fe = &S->files[fd];
+    if (sstatus(ld_acq(&fe->st)) != GFS_SS_OPEN) return -GFS_EBADF;
+    if (size > 0) {
+        uint32_t gen = ld_rlx(&fe->gen);
+        int host_fd = (int)ld_rlx((const uint32_t*)&fe->host_fd);
+        int oflags = (int)ld_rlx((const uint32_t*)&fe->flags);
+        uint32_t nwords = (S->n_frames + 31u) >> 5;
+        for (uint32_t w = 0; w < nwords; w++) {
+            uint32_t bits = ld_rlx(&S->dirty_bits[w]);
+            while (bits) {
+                uint32_t b = (uint32_t)(__ffs(bits) - 1);
+                bits &= bits - 1u;
+                uint32_t fr = (w << 5) | b;
+                if (key_file(ld_rlx64(&S->frames[fr].key)) == (uint32_t)fd)
+                    flush_frame(S, fr, (uint32_t)fd, gen, host_fd, oflags);
+            }
+        }
+    }
+    Req r = {};
+    r.op = GFS_OP_TRUNC;
+    r.host_fd = (int)ld_rlx((const uint32_t*)&fe->host_fd);
+    r.file = (uint32_t)fd;
+    r.length = size;
+    int rc = rpc_call(S, r, &fe->done);
+    if (rc < 0) return rc;
+    atomicAdd(&fe->gen, 1u);
+    st_rlx64(&fe->size, size);
+    __threadfence();
+    return 0;
+}
+
+/* single-thread fsync */
+__device__ __noinline__ int st_fsync(gfs_state* S, int fd) {
+    if (fd < 0 || (uint32_t)fd >= S->n_files) return -GFS_EBADF;
+    gfs_file* fe = &S->files[fd];
+    uint32_t gen = ld_rlx(&fe->gen);
+    int host_fd = (int)ld_rlx((const uint32_t*)&fe->host_fd);
+    int oflags = (int)ld_rlx((const uint32_t*)&fe->flags);
+    uint32_t nwords = (S->n_frames + 31u) >> 5;
+    int err = 0;
+    for (uint32_t w = 0; w < nwords; w++) {
+        uint32_t bits = ld_rlx(&S->dirty_bits[w]);
+        while (bits) {
+            uint32_t b = (uint32_t)(__ffs(bits) - 1);
+            bits &= bits - 1u;
+            uint32_t fr = (w << 5) | b;
+            if (key_file(ld_rlx64(&S->frames[fr].key)) == (uint32_t)fd) {
+                int rc = flush_frame(S, fr, (uint32_t)fd, gen, host_fd, oflags);
+                if (rc < 0 && !err) err = rc;
+            }
+        }
+    }
+    return err;
+}
+
+/* gunlink: remove the host file; a cached closed copy is invalidated. */
+__device__ __noinline__ int st_unlink(gfs_state* S, const char* name) {
+    int len = 0;
+    while (len < GFS_NAME_MAX && name[len]) len++;
+    if (len == 0 || len >= GFS_NAME_MAX) return -GFS_EINVAL;
+    uint64_t h = name_hash(name);
+    int slot = file_find(S, name, h);
+    Waiter w(S->timeout_ns);
+    if (slot < 0) {
+        if (!spin_lock(&S->table_lock, w)) return -GFS_ETIMEDOUT;
+        slot = file_find(S, name, h);
+        if (slot < 0) slot = file_claim(S, name, h);
+        spin_unlock(&S->table_lock);
+        if (slot < 0) return -GFS_EMFILE;
+    }
+    gfs_file* fe = &S->files[slot];
+    Req r = {};
+    r.op = GFS_OP_UNLINK;
+    r.file = (uint32_t)slot;
+    r.name = fe->name;
+    int rc = rpc_call(S, r, &fe->done);
+    uint32_t st = ld_acq(&fe->st);
+    if (sstatus(st) == GFS_SS_CLOSED) {
+        atomicAdd(&fe->gen, 1u);
+        st_rlx64(&fe->cached_ctime, 0ULL);
+        st_rlx64(&fe->cached_size, ~0ULL);
+    }
+    return rc < 0 ? rc : 0;
+}
+
+} // namespace
+} // namespace gfsd
+#endif

@@ -1,0 +1,153 @@
+/*
+ * The reference's kernel-callable file API, same names and signatures as
+ * libgpufs/fs_calls.cu.h:34-65, implemented over the GB300 buffer cache.
+ *
+ * Semantics kept from the reference:
+ *   - calls are collective: every thread of the block calls with the same
+ *     arguments (warp for the _warp forms); single_thread_* are per-thread;
+ *   - gread/gwrite move bytes through HBM page frames; write-once files
+ *     (O_GWRONCE) are never read from the host and are OR-merged into the
+ *     host file at write-back (host_loop.h:76-137);
+ *   - data reaches the host file at gclose (last close), gfsync, gmsync, or
+ *     when the clock evictor needs the frame.
+ * Differences (a strict superset): errors come back as negative values or
+ * GMAP_FAILED instead of compiled-out asserts; gread clamps at end of file
+ * and returns the bytes read; gftruncate accepts any size; gunlink works.
+ */
+#include <stdio.h>
+#include "gfs_block.cuh"
+
+/* The file-system state of the current session; set by gfs_create(). */
+__device__ gfs_state* g_gfs;
+
+using namespace gfsd;
+
+/* fs_calls.cu:227-236 */
+__device__ int gopen(const char* filename, int flags) { return blk_open(g_gfs, filename, flags); }
+
+/* fs_calls.cu:152-225 */
+__device__ int single_thread_open(const char* filename, int flags) { return file_open(g_gfs, filename, flags); }
+
+/* fs_calls.cu:35-105 */
+__device__ int gclose(int fd) { return blk_close(g_gfs, fd); }
+
+/* fs_calls.cu:689-737 */
+__device__ size_t gread(int fd, size_t offset, size_t size, unsigned char* buffer) {
+    long long r = blk_read(g_gfs, fd, offset, size, buffer);
+    return r < 0 ? (size_t)r : (size_t)r;
+}
+
+/* fs_calls.cu:739-802 */
+__device__ size_t gwrite(int fd, size_t offset, size_t size, unsigned char* buffer) {
+    long long r = blk_write(g_gfs, fd, offset, size, buffer);
+    return (size_t)r;
+}
+
+/* fs_calls.cu:422-481 */
+__device__ volatile void* gmmap(void* addr, size_t size, int prot, int flags, int fd, off_t offset) {
+    (void)addr;
+    (void)prot;
+    (void)flags;
+    return (volatile void*)blk_mmap(g_gfs, fd, (uint64_t)offset, size);
+}
+
+/* fs_calls.cu:385-401 */
+__device__ int gmunmap(volatile void* addr, size_t length) {
+    (void)length;
+    return blk_munmap(g_gfs, addr);
+}
+
+/* fs_calls.cu:618-683: warp-collective mapping; `ref` pins are taken */
+__device__ volatile void* gmmap_warp(void* addr, size_t size, int prot, int flags, int fd, off_t offset, int ref) {
+    (void)addr;
+    (void)prot;
+    (void)flags;
+    gfs_state* S = g_gfs;
+    const unsigned mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int r = 0;
+    bool fresh = false;
+    if (lane == leader) r = map_pin(S, fd, (uint64_t)offset, size, &fresh, ref < 1 ? 1 : ref);
+    r = __shfl_sync(mask, r, leader);
+    int fz = __shfl_sync(mask, (int)fresh, leader);
+    if (r < 0) return (volatile void*)-1;
+    if (fz) {
+        int rank = __popc(mask & ((1u << lane) - 1u)), cnt = __popc(mask);
+        uint8_t* d = frame_data(S, (uint32_t)r);
+        for (uint32_t k = (uint32_t)rank * 16u; k < S->page_size; k += (uint32_t)cnt * 16u)
+            *(uint4*)(d + k) = make_uint4(0, 0, 0, 0);
+        __syncwarp(mask);
+        if (lane == leader) publish_valid(S, (uint32_t)r);
+        __syncwarp(mask);
+    }
+    return (volatile void*)(frame_data(S, (uint32_t)r) + ((uint64_t)offset & (S->page_size - 1u)));
+}
+
+/* fs_calls.cu:403-420 */
+__device__ int gmunmap_warp(volatile void* addr, size_t length, int ref) {
+    (void)length;
+    __threadfence();
+    const unsigned mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int r = 0;
+    if (lane == leader) r = unmap_one(g_gfs, addr, ref < 1 ? 1 : ref);
+    return __shfl_sync(mask, r, leader);
+}
+
+/* fs_calls.cu:804-843: write the mapped page back now (single thread) */
+__device__ int gmsync(volatile void* addr, size_t length, int flags) {
+    (void)length;
+    (void)flags;
+    gfs_state* S = g_gfs;
+    int fr = addr_frame(S, addr);
+    if (fr < 0) return -1;
+    __threadfence();
+    uint64_t key = ld_rlx64(&S->frames[fr].key);
+    uint32_t f = key_file(key);
+    if (f >= S->n_files) return -1;
+    gfs_file* fe = &S->files[f];
+    mark_dirty(S, (uint32_t)fr);
+    return flush_frame(S, (uint32_t)fr, f, ld_rlx(&fe->gen), (int)ld_rlx((const uint32_t*)&fe->host_fd),
+                       (int)ld_rlx((const uint32_t*)&fe->flags));
+}
+
+/* fs_calls.cu:107-125 */
+__device__ int gfsync(int fd) { return blk_flush(g_gfs, fd); }
+
+__device__ int single_thread_fsync(int fd) { return st_fsync(g_gfs, fd); }
+
+/* fs_calls.cu:127-140 */
+__device__ int single_thread_ftruncate(int fd, int size) { return st_truncate(g_gfs, fd, (uint64_t)(size < 0 ? 0 : size)); }
+
+/* fs_calls.cu:143-149 */
+__device__ int gftruncate(int fd, int size) {
+    __shared__ int s_r;
+    __syncthreads();
+    if (blk_tid() == 0) s_r = single_thread_ftruncate(fd, size);
+    __syncthreads();
+    return s_r;
+}
+
+/* fs_calls.cu:845-850 (unimplemented in the reference) */
+__device__ unsigned int gunlink(char* filename) {
+    int r = st_unlink(g_gfs, filename);
+    return (unsigned int)(r < 0 ? -r : 0);
+}
+
+/* fs_calls.cu:851-854 */
+__device__ size_t fstat(int fd) {
+    gfs_state* S = g_gfs;
+    if (fd < 0 || (uint32_t)fd >= S->n_files) return 0;
+    return (size_t)ld_rlx64(&S->files[fd].size);
+}
+
+/* device side of the samples' INIT_LOCK / LAST_SEMAPHORE / ERROR helpers */
+__device__ unsigned int g_gfs_user_error;
+__device__ void gfs_report_user_error(const char* msg, const char* file, int line) {
+    atomicOr(&g_gfs_user_error, 1u);
+    if (g_gfs) atomicOr(&g_gfs->error, GFS_ERRB_ARG);
+    printf("gpufs: %s (%s:%d)\n", msg, file, line);
+}
+__device__ unsigned long long gfs_globaltimer() { return gtimer(); }

@@ -1,0 +1,525 @@
+/*
+ * Host runtime of the GB300 GPU file system.
+ *
+ * Replaces the reference's host side:
+ *   GPUGlobals / GPUStreamManager / initializer  libgpufs/fs_initializer.cu(.h)
+ *   run_gpufs_handler, open_loop, rw_task,        libgpufs/host_loop.h:156-656
+ *   mainLoop, async_close_loop, diff_and_merge
+ *
+ * The reference runs five busy-polling threads only while
+ * run_gpufs_handler() blocks, one 4-byte flag per request, a mutex/condvar
+ * hand-off per batch, an extra device staging copy per page, and a D2H copy
+ * plus stream synchronisation per written page.  Here:
+ *   - `host_workers` threads consume one MPMC request ring (mapped pinned
+ *     memory, 128-byte slots, sequence-numbered) for the whole lifetime of
+ *     the session, so kernels may run at any time, not only inside the
+ *     handler call;
+ *   - reads go pread -> pinned staging -> cudaMemcpyAsync straight into the
+ *     page frame on the worker's own stream, then cuStreamWriteValue32 puts
+ *     the completion word in device memory in stream order, so the waiting
+ *     block sees it only after the bytes have landed;
+ *   - writes go D2H -> (OR-merge for write-once files) -> pwrite;
+ *   - staging slots are recycled by CUDA events, never by a blocking flag.
+ */
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <errno.h>
+#include <fcntl.h>
+#include <sched.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+#include <sys/time.h>
+#include <time.h>
+#include <unistd.h>
+
+#include <atomic>
+#include <thread>
+#include <vector>
+
+#include "gfs_types.h"
+#include "gfs_runtime.h"
+
+extern __device__ gfs_state* g_gfs;
+
+namespace {
+
+struct Worker {
+    int id = 0;
+    cudaStream_t stream = nullptr;
+    uint8_t* staging = nullptr; /* depth * slot_bytes, pinned */
+    uint8_t* merge = nullptr;   /* OR-merge scratch */
+    size_t slot_bytes = 0;
+    int depth = 0;
+    std::vector<cudaEvent_t> ev;
+    std::vector<char> pending;
+    int next = 0;
+    std::thread th;
+};
+
+__global__ void k_init_frames(gfs_frame* f, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        gfs_frame z;
+        z.st = 0u;
+        z.content = 0u;
+        z.key = ~0ULL;
+        z.done = 0u;
+        z.pad0 = 0u;
+        z.pad1 = 0ULL;
+        f[i] = z;
+    }
+}
+
+uint32_t next_pow2(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return (uint32_t)p;
+}
+
+ssize_t pread_full(int fd, uint8_t* buf, size_t len, off_t off) {
+    size_t got = 0;
+    while (got < len) {
+        ssize_t r = pread(fd, buf + got, len - got, off + (off_t)got);
+        if (r < 0) {
+            if (errno == EINTR) continue;
+            return -1;
+        }
+        if (r == 0) break;
+        got += (size_t)r;
+    }
+    return (ssize_t)got;
+}
+
+ssize_t pwrite_full(int fd, const uint8_t* buf, size_t len, off_t off) {
+    size_t put = 0;
+    while (put < len) {
+        ssize_t r = pwrite(fd, buf + put, len - put, off + (off_t)put);
+        if (r < 0) {
+            if (errno == EINTR) continue;
+            return -1;
+        }
+        put += (size_t)r;
+    }
+    return (ssize_t)put;
+}
+
+} // namespace
+
+struct gfs_ctx {
+    gfs_config cfg{};
+    gfs_state hs{};
+    gfs_state* ds = nullptr;
+    gfs_req* ring_h = nullptr;
+    cudaStream_t kstream = nullptr;
+    std::atomic<uint32_t> head{0};
+    std::atomic<int> stop{0};
+    std::atomic<int> paused{0};
+    std::atomic<int> inject_count{0};
+    int inject_err = EIO;
+    std::vector<Worker*> workers;
+    std::atomic<unsigned long long> h_reads{0}, h_read_bytes{0}, h_writes{0}, h_write_bytes{0}, h_opens{0},
+        h_errors{0}, h_requests{0};
+    char* d_scratch = nullptr; /* small device scratch for names/results of C-ABI calls */
+    /* driver entry point, resolved through the runtime so the library does
+     * not link libcuda directly (it loads on machines without a driver) */
+    PFN_cuStreamWriteValue32_v11070 write_value = nullptr;
+    size_t d_scratch_cap = 0;
+};
+
+static uint32_t staging_take(Worker* w) {
+    int k = w->next;
+    w->next = (k + 1) % w->depth;
+    if (w->pending[k]) {
+        cudaEventSynchronize(w->ev[k]);
+        w->pending[k] = 0;
+    }
+    return (uint32_t)k;
+}
+
+static void complete(gfs_ctx* c, Worker* w, const gfs_req& r, uint32_t code, int slot_used) {
+    c->write_value((CUstream)w->stream, (CUdeviceptr)r.done_addr, code, CU_STREAM_WRITE_VALUE_DEFAULT);
+    if (slot_used >= 0) {
+        cudaEventRecord(w->ev[slot_used], w->stream);
+        w->pending[slot_used] = 1;
+    }
+    if (code & GFS_DONE_ERR) c->h_errors++;
+}
+
+static int host_open_flags(int oflags) {
+    /* the reference turns write-once into O_RDWR|O_CREAT (host_loop.h:169-173);
+     * write-only files are opened read-write as well so partial-page writes
+     * can be filled from the file */
+    if (oflags == (O_CREAT | O_WRONLY)) return O_RDWR | O_CREAT;
+    if ((oflags & O_ACCMODE) == O_WRONLY) return (oflags & ~O_ACCMODE) | O_RDWR;
+    return oflags;
+}
+
+static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
+    c->h_requests++;
+    switch (r.op) {
+    case GFS_OP_OPEN: {
+        char name[GFS_NAME_MAX + 1];
+        memcpy(name, r.name, GFS_NAME_MAX);
+        name[GFS_NAME_MAX] = 0;
+        int fd = open(name, host_open_flags(r.oflags) | O_CLOEXEC, 0644);
+        int err = fd < 0 ? errno : 0;
+        gfs_open_reply rep{};
+        rep.host_fd = fd;
+        rep.err = err;
+        if (fd >= 0) {
+            struct stat s;
+            if (fstat(fd, &s) == 0) {
+                rep.size = (uint64_t)s.st_size;
+                rep.ctime_ns = (int64_t)s.st_ctim.tv_sec * 1000000000LL + s.st_ctim.tv_nsec;
+            }
+        }
+        uint32_t k = staging_take(w);
+        memcpy(w->staging + (size_t)k * w->slot_bytes, &rep, sizeof rep);
+        cudaMemcpyAsync((void*)(uintptr_t)r.dev_addr, w->staging + (size_t)k * w->slot_bytes, sizeof rep,
+                        cudaMemcpyHostToDevice, w->stream);
+        c->h_opens++;
+        complete(c, w, r, fd >= 0 ? 1u : (GFS_DONE_ERR | (uint32_t)err), (int)k);
+        break;
+    }
+    case GFS_OP_CLOSE: {
+        int rc = r.host_fd >= 0 ? close(r.host_fd) : 0;
+        complete(c, w, r, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno), -1);
+        break;
+    }
+    case GFS_OP_READ: {
+        if (c->inject_count.load() > 0 && c->inject_count.fetch_sub(1) > 0) {
+            complete(c, w, r, GFS_DONE_ERR | (uint32_t)c->inject_err, -1);
+            break;
+        }
+        size_t len = (size_t)r.length;
+        if (len > w->slot_bytes) len = w->slot_bytes;
+        uint32_t k = staging_take(w);
+        uint8_t* buf = w->staging + (size_t)k * w->slot_bytes;
+        ssize_t n = pread_full(r.host_fd, buf, len, (off_t)r.offset);
+        if (n < 0) {
+            complete(c, w, r, GFS_DONE_ERR | (uint32_t)errno, -1);
+            break;
+        }
+        size_t cp = ((size_t)n + 4095u) & ~(size_t)4095u;
+        if (cp > w->slot_bytes) cp = w->slot_bytes;
+        if (cp > (size_t)n) memset(buf + n, 0, cp - (size_t)n);
+        if (cp) cudaMemcpyAsync((void*)(uintptr_t)r.dev_addr, buf, cp, cudaMemcpyHostToDevice, w->stream);
+        c->h_reads++;
+        c->h_read_bytes += (unsigned long long)n;
+        complete(c, w, r, 1u + (uint32_t)n, (int)k);
+        break;
+    }
+    case GFS_OP_WRITE: {
+        size_t len = (size_t)r.length;
+        if (len > w->slot_bytes) len = w->slot_bytes;
+        uint32_t k = staging_take(w);
+        uint8_t* buf = w->staging + (size_t)k * w->slot_bytes;
+        cudaMemcpyAsync(buf, (const void*)(uintptr_t)r.dev_addr, len, cudaMemcpyDeviceToHost, w->stream);
+        cudaStreamSynchronize(w->stream);
+        w->pending[k] = 0;
+        if (r.rflags & GFS_RF_DIFF) {
+            /* write-once pages were never read: OR them into what is there
+             * (diff_and_merge, host_loop.h:76-137) */
+            ssize_t m = pread_full(r.host_fd, w->merge, len, (off_t)r.offset);
+            for (ssize_t i = 0; i < m; i++) buf[i] |= w->merge[i];
+        }
+        ssize_t put = pwrite_full(r.host_fd, buf, len, (off_t)r.offset);
+        c->h_writes++;
+        if (put >= 0) c->h_write_bytes += (unsigned long long)put;
+        complete(c, w, r, put == (ssize_t)len ? 1u + (uint32_t)len : (GFS_DONE_ERR | (uint32_t)(put < 0 ? errno : EIO)),
+                 -1);
+        break;
+    }
+    case GFS_OP_TRUNC: {
+        int rc = ftruncate(r.host_fd, (off_t)r.length);
+        complete(c, w, r, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno), -1);
+        break;
+    }
+    case GFS_OP_UNLINK: {
+        char name[GFS_NAME_MAX + 1];
+        memcpy(name, r.name, GFS_NAME_MAX);
+        name[GFS_NAME_MAX] = 0;
+        int rc = unlink(name);
+        complete(c, w, r, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno), -1);
+        break;
+    }
+    default:
+        complete(c, w, r, GFS_DONE_ERR | (uint32_t)EINVAL, -1);
+    }
+}
+
+static void worker_main(gfs_ctx* c, Worker* w) {
+    cudaSetDevice(c->cfg.device);
+    cudaFree(nullptr);
+    const uint32_t R = c->cfg.ring_slots, mask = R - 1;
+    while (!c->stop.load(std::memory_order_relaxed)) {
+        uint32_t t = c->head.fetch_add(1);
+        gfs_req* slot = &c->ring_h[t & mask];
+        unsigned spins = 0;
+        while (__atomic_load_n(&slot->seq, __ATOMIC_ACQUIRE) != t + 1u) {
+            if (c->stop.load(std::memory_order_relaxed)) return;
+            ++spins;
+            if (spins < 4096u) continue;
+            if (spins < 8192u) { sched_yield(); continue; }
+            struct timespec ts = {0, 20000};
+            nanosleep(&ts, nullptr);
+        }
+        while (c->paused.load(std::memory_order_relaxed) && !c->stop.load(std::memory_order_relaxed)) {
+            struct timespec ts = {0, 200000};
+            nanosleep(&ts, nullptr);
+        }
+        if (c->stop.load(std::memory_order_relaxed)) return;
+        gfs_req r;
+        memcpy(&r, (const void*)slot, sizeof r);
+        __atomic_store_n(&slot->seq, t + R, __ATOMIC_RELEASE);
+        handle(c, w, r);
+    }
+}
+
+#define CK(x)                                                                                     \
+    do {                                                                                          \
+        cudaError_t e_ = (x);                                                                     \
+        if (e_ != cudaSuccess) {                                                                  \
+            fprintf(stderr, "gpufs_gb300: %s failed: %s (%s:%d)\n", #x, cudaGetErrorString(e_), __FILE__, \
+                    __LINE__);                                                                    \
+            rc = -(int)e_;                                                                        \
+            goto fail;                                                                            \
+        }                                                                                         \
+    } while (0)
+
+static gfs_ctx* g_current = nullptr; /* session g_gfs points at */
+
+extern "C" {
+
+/* Point the device API (g_gfs) at this session, in stream order. */
+int gfs__activate(gfs_ctx* c) {
+    if (g_current == c) return 0;
+    cudaError_t e = cudaMemcpyToSymbolAsync(g_gfs, &c->ds, sizeof(gfs_state*), 0, cudaMemcpyHostToDevice, c->kstream);
+    if (e != cudaSuccess) return -GFS_EIO;
+    cudaStreamSynchronize(c->kstream);
+    g_current = c;
+    return 0;
+}
+
+void gfs_default_config(gfs_config* c) {
+    memset(c, 0, sizeof *c);
+    c->log_page = 16;
+    c->pool_bytes = 2ull << 30;
+    c->max_files = 1024;
+    c->ring_slots = 4096;
+    c->host_workers = 8;
+    c->staging_depth = 8;
+    c->timeout_ns = 30ull * 1000000000ull;
+    c->device = 0;
+}
+
+int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
+    int rc = 0;
+    gfs_ctx* c = new gfs_ctx();
+    c->cfg = *cfg_in;
+    gfs_config& cfg = c->cfg;
+    *out = nullptr;
+    if (cfg.log_page < 12 || cfg.log_page > 21) { delete c; return -GFS_EINVAL; }
+    if (cfg.host_workers < 1) cfg.host_workers = 1;
+    if (cfg.host_workers > 64) cfg.host_workers = 64;
+    if (cfg.staging_depth < 2) cfg.staging_depth = 2;
+    if (cfg.timeout_ns == 0) cfg.timeout_ns = 30ull * 1000000000ull;
+    cfg.ring_slots = next_pow2(cfg.ring_slots < 64 ? 64 : cfg.ring_slots);
+    cfg.max_files = next_pow2(cfg.max_files < 64 ? 64 : cfg.max_files);
+    if (cfg.max_files > (1u << 20)) { delete c; return -GFS_EINVAL; }
+    {
+        uint64_t page = 1ull << cfg.log_page;
+        uint64_t nf = cfg.pool_bytes / page;
+        if (nf < 64) nf = 64;
+        if (nf > GFS_MAX_FRAMES - 1) nf = GFS_MAX_FRAMES - 1;
+        gfs_state& s = c->hs;
+        s.log_page = cfg.log_page;
+        s.page_size = (uint32_t)page;
+        s.n_frames = (uint32_t)nf;
+        s.n_buckets = next_pow2((nf + 3) / 4 < 64 ? 64 : (nf + 3) / 4);
+        s.n_files = cfg.max_files;
+        s.ring_slots = cfg.ring_slots;
+        s.timeout_ns = cfg.timeout_ns;
+        CK(cudaSetDevice(cfg.device));
+        cudaSetDeviceFlags(cudaDeviceMapHost);
+        cudaGetLastError();
+        {
+            void* fn = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            CK(cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &fn, 12000, cudaEnableDefault, &q));
+            if (!fn || q != cudaDriverEntryPointSuccess) {
+                rc = -GFS_EINVAL;
+                goto fail;
+            }
+            c->write_value = (PFN_cuStreamWriteValue32_v11070)fn;
+        }
+        CK(cudaMalloc(&s.pool, nf * page));
+        CK(cudaMalloc(&s.frames, nf * sizeof(gfs_frame)));
+        CK(cudaMalloc(&s.index, (size_t)s.n_buckets * GFS_WAYS * sizeof(uint32_t)));
+        CK(cudaMemset(s.index, 0, (size_t)s.n_buckets * GFS_WAYS * sizeof(uint32_t)));
+        CK(cudaMalloc(&s.bucket_lock, (size_t)s.n_buckets * sizeof(uint32_t)));
+        CK(cudaMemset(s.bucket_lock, 0, (size_t)s.n_buckets * sizeof(uint32_t)));
+        CK(cudaMalloc(&s.files, (size_t)s.n_files * sizeof(gfs_file)));
+        CK(cudaMemset(s.files, 0, (size_t)s.n_files * sizeof(gfs_file)));
+        CK(cudaMalloc(&s.dirty_bits, ((nf + 31) / 32) * sizeof(uint32_t)));
+        CK(cudaMemset(s.dirty_bits, 0, ((nf + 31) / 32) * sizeof(uint32_t)));
+        k_init_frames<<<256, 256>>>(s.frames, (uint32_t)nf);
+        CK(cudaGetLastError());
+        CK(cudaHostAlloc((void**)&c->ring_h, (size_t)cfg.ring_slots * sizeof(gfs_req),
+                         cudaHostAllocMapped | cudaHostAllocPortable));
+        memset(c->ring_h, 0, (size_t)cfg.ring_slots * sizeof(gfs_req));
+        for (uint32_t i = 0; i < cfg.ring_slots; i++) c->ring_h[i].seq = i;
+        CK(cudaHostGetDevicePointer((void**)&s.ring, c->ring_h, 0));
+        CK(cudaMalloc(&c->ds, sizeof(gfs_state)));
+        CK(cudaMemcpy(c->ds, &s, sizeof(gfs_state), cudaMemcpyHostToDevice));
+        CK(cudaMemcpyToSymbol(g_gfs, &c->ds, sizeof(gfs_state*)));
+        g_current = c;
+        CK(cudaStreamCreateWithFlags(&c->kstream, cudaStreamNonBlocking));
+        c->d_scratch_cap = 1 << 20;
+        CK(cudaMalloc(&c->d_scratch, c->d_scratch_cap));
+        CK(cudaDeviceSynchronize());
+        for (uint32_t i = 0; i < cfg.host_workers; i++) {
+            Worker* w = new Worker();
+            w->id = (int)i;
+            w->depth = (int)cfg.staging_depth;
+            w->slot_bytes = (size_t)page;
+            c->workers.push_back(w);
+            CK(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+            CK(cudaHostAlloc((void**)&w->staging, (size_t)w->depth * w->slot_bytes, cudaHostAllocPortable));
+            w->merge = (uint8_t*)malloc(w->slot_bytes);
+            w->ev.resize((size_t)w->depth);
+            w->pending.assign((size_t)w->depth, 0);
+            for (int k = 0; k < w->depth; k++) CK(cudaEventCreateWithFlags(&w->ev[(size_t)k], cudaEventDisableTiming));
+        }
+        for (Worker* w : c->workers) w->th = std::thread(worker_main, c, w);
+    }
+    *out = c;
+    return 0;
+fail:
+    gfs_destroy(c);
+    return rc ? rc : -1;
+}
+
+int gfs_destroy(gfs_ctx* c) {
+    if (!c) return 0;
+    if (c->kstream) cudaStreamSynchronize(c->kstream);
+    c->stop.store(1);
+    for (Worker* w : c->workers)
+        if (w->th.joinable()) w->th.join();
+    cudaDeviceSynchronize();
+    for (Worker* w : c->workers) {
+        for (cudaEvent_t e : w->ev)
+            if (e) cudaEventDestroy(e);
+        if (w->stream) cudaStreamDestroy(w->stream);
+        if (w->staging) cudaFreeHost(w->staging);
+        free(w->merge);
+        delete w;
+    }
+    c->workers.clear();
+    gfs_state& s = c->hs;
+    gfs_state* none = nullptr;
+    if (c->ds && g_current == c) {
+        cudaMemcpyToSymbol(g_gfs, &none, sizeof none);
+        g_current = nullptr;
+    }
+    cudaFree(s.pool);
+    cudaFree(s.frames);
+    cudaFree(s.index);
+    cudaFree(s.bucket_lock);
+    cudaFree(s.files);
+    cudaFree(s.dirty_bits);
+    cudaFree(c->ds);
+    cudaFree(c->d_scratch);
+    if (c->ring_h) cudaFreeHost(c->ring_h);
+    if (c->kstream) cudaStreamDestroy(c->kstream);
+    delete c;
+    return 0;
+}
+
+void* gfs_kernel_stream(gfs_ctx* c) { return (void*)c->kstream; }
+void* gfs_device_state(gfs_ctx* c) { return (void*)c->ds; }
+uint32_t gfs_page_size(gfs_ctx* c) { return c->hs.page_size; }
+uint32_t gfs_num_frames(gfs_ctx* c) { return c->hs.n_frames; }
+void* gfs_pool_base(gfs_ctx* c) { return (void*)c->hs.pool; }
+
+int gfs_run_handler(gfs_ctx* c, int gpuid) {
+    (void)gpuid;
+    cudaError_t e = cudaStreamSynchronize(c->kstream);
+    return (int)e;
+}
+
+uint32_t gfs_last_error(gfs_ctx* c, int clear) {
+    uint32_t v = 0;
+    cudaMemcpy(&v, &c->ds->error, sizeof v, cudaMemcpyDeviceToHost);
+    if (clear) {
+        uint32_t z = 0;
+        cudaMemcpy(&c->ds->error, &z, sizeof z, cudaMemcpyHostToDevice);
+    }
+    return v;
+}
+
+int gfs_get_stats(gfs_ctx* c, unsigned long long* out, int n) {
+    gfs_stats st;
+    if (cudaMemcpy(&st, &c->ds->stats, sizeof st, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    unsigned long long v[GFS_NSTATS] = {
+        st.hits, st.misses, st.evictions, st.writebacks, st.read_rpcs, st.bytes_read_rpc, st.opens, st.closes,
+        st.timeouts, st.errors, st.conflict_evictions, c->h_requests.load(), c->h_reads.load(),
+        c->h_read_bytes.load(), c->h_writes.load(), c->h_write_bytes.load(), c->h_opens.load(), c->h_errors.load()};
+    int k = n < GFS_NSTATS ? n : GFS_NSTATS;
+    for (int i = 0; i < k; i++) out[i] = v[i];
+    return k;
+}
+
+int gfs_reset_stats(gfs_ctx* c) {
+    gfs_stats z;
+    memset(&z, 0, sizeof z);
+    cudaMemcpy(&c->ds->stats, &z, sizeof z, cudaMemcpyHostToDevice);
+    c->h_requests = 0;
+    c->h_reads = 0;
+    c->h_read_bytes = 0;
+    c->h_writes = 0;
+    c->h_write_bytes = 0;
+    c->h_opens = 0;
+    c->h_errors = 0;
+    return 0;
+}
+
+int gfs_set_paused(gfs_ctx* c, int paused) {
+    c->paused.store(paused ? 1 : 0);
+    return 0;
+}
+
+int gfs_inject_read_errors(gfs_ctx* c, int count, int err) {
+    c->inject_err = err > 0 ? err : EIO;
+    c->inject_count.store(count);
+    return 0;
+}
+
+/* device scratch for the C-ABI helpers (names, per-block results) */
+void* gfs__scratch(gfs_ctx* c, size_t bytes) {
+    if (bytes > c->d_scratch_cap) {
+        cudaFree(c->d_scratch);
+        size_t cap = c->d_scratch_cap;
+        while (cap < bytes) cap <<= 1;
+        if (cudaMalloc(&c->d_scratch, cap) != cudaSuccess) {
+            c->d_scratch = nullptr;
+            c->d_scratch_cap = 0;
+            return nullptr;
+        }
+        c->d_scratch_cap = cap;
+    }
+    return c->d_scratch;
+}
+
+const gfs_state* gfs__host_state(gfs_ctx* c) { return &c->hs; }
+
+double _timestamp() {
+    struct timeval tv;
+    gettimeofday(&tv, nullptr);
+    return 1e6 * (double)tv.tv_sec + (double)tv.tv_usec;
+}
+
+} /* extern "C" */

@@ -1,0 +1,117 @@
+/*
+ * gpufs_gb300 -- C ABI of the GB300 GPU file system.
+ *
+ * Plain C: pointers, sizes and integers only.  A host program (or an FFI
+ * such as Python ctypes) binds these symbols from libgpufs_gb300.so.  Each
+ * entry point names the reference interface it replaces (paths relative to
+ * the GPUfs source tree).
+ *
+ * Device memory arguments are raw device addresses (void*); host memory
+ * arguments are ordinary host pointers.  Functions return 0 / a non-negative
+ * count on success and a negative errno-style code on failure.  Every call
+ * that runs a kernel waits for it before returning.  One session may be
+ * live per process at a time (the device API reaches it through one
+ * __device__ global, as the reference's g_* globals do).
+ */
+#ifndef GPUFS_GB300_H
+#define GPUFS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gfs_ctx gfs_ctx;
+
+/* Session configuration.  Compile-time constants of the reference
+ * (libgpufs/fs_constants.h:26-77) become run-time fields here. */
+typedef struct gfs_config {
+    uint32_t log_page;      /* page = 1 << log_page bytes, 12..21 (FS_LOGBLOCKSIZE) */
+    uint32_t max_files;     /* open-file table slots, rounded up to 2^k (MAX_NUM_FILES) */
+    uint64_t pool_bytes;    /* HBM buffer cache (PPOOL_SIZE) */
+    uint32_t ring_slots;    /* host request ring slots, 2^k (RW_IPC_SIZE) */
+    uint32_t host_workers;  /* host I/O threads (RW_HOST_WORKERS) */
+    uint32_t staging_depth; /* pinned staging pages per worker (RW_SCRATCH_PER_WORKER) */
+    uint32_t pad0;
+    uint64_t timeout_ns;    /* bound on every device-side wait (the reference waits forever) */
+    int32_t device;         /* CUDA device ordinal */
+    uint32_t pad1;
+} gfs_config;
+
+#define GFS_NSTATS 18
+/* gfs_get_stats order: device hits(page accesses), misses, evictions,
+ * writebacks, read_rpcs, bytes_read_rpc, opens, closes, timeouts, errors,
+ * conflict_evictions; host requests, reads, read_bytes, writes, write_bytes,
+ * opens, errors */
+
+/* ---- session ---- */
+/* defaults: 64 KiB pages, 2 GiB pool, 1024 files, 4096 ring slots, 8 workers */
+void gfs_default_config(gfs_config* cfg);
+/* replaces initializer() / GPUGlobals::GPUGlobals (libgpufs/fs_initializer.cu:116-167,
+ * fs_initializer.cu.h:139-178); host workers start here and serve until destroy */
+int gfs_create(const gfs_config* cfg, gfs_ctx** out);
+/* replaces GPUGlobals::~GPUGlobals (libgpufs/fs_initializer.cu.h:180-198) */
+int gfs_destroy(gfs_ctx* ctx);
+/* replaces run_gpufs_handler (libgpufs/host_loop.h:559-656): waits until the
+ * kernel stream is idle; returns the CUDA error code of the stream (0 ok) */
+int gfs_run_handler(gfs_ctx* ctx, int gpuid);
+/* gpuGlobals->streamMgr->kernelStream (libgpufs/fs_initializer.cu.h:90): a cudaStream_t */
+void* gfs_kernel_stream(gfs_ctx* ctx);
+/* device address of the session state (for kernels that take it explicitly) */
+void* gfs_device_state(gfs_ctx* ctx);
+uint32_t gfs_page_size(gfs_ctx* ctx);
+uint32_t gfs_num_frames(gfs_ctx* ctx);
+void* gfs_pool_base(gfs_ctx* ctx);
+/* sticky device error bits (1 timeout, 2 io, 4 no frame, 8 table full, 16 bad argument) */
+uint32_t gfs_last_error(gfs_ctx* ctx, int clear);
+/* counters; replaces the PRINT_* statistics of libgpufs/fs_debug.cu.h:99-148 */
+int gfs_get_stats(gfs_ctx* ctx, unsigned long long* out, int n);
+int gfs_reset_stats(gfs_ctx* ctx);
+
+/* ---- host-side fault injection (tests only; no GPU fault is ever made) ---- */
+/* stall (1) or resume (0) the host service: device waits then time out */
+int gfs_set_paused(gfs_ctx* ctx, int paused);
+/* the next `count` host page reads fail with `err` (errno) */
+int gfs_inject_read_errors(gfs_ctx* ctx, int count, int err);
+
+/* ---- device API, driven from the host (each call runs one kernel whose
+ * blocks call the reference-named device functions) ---- */
+/* gopen(O_GRDONLY) + gread + gclose over [off, off+size) split into page-aligned
+ * slices, one per block (libgpufs/fs_calls.cu:227,689,35).  host_out: host buffer.
+ * Returns bytes read (clamped at end of file) or -error. */
+long long gfs_pread(gfs_ctx* ctx, const char* path, uint64_t off, uint64_t size, void* host_out, int nblocks,
+                    int nthreads);
+/* same into a device buffer; *kernel_ms (optional) = kernel time (CUDA events) */
+long long gfs_pread_dev(gfs_ctx* ctx, const char* path, uint64_t off, uint64_t size, void* dev_out, int nblocks,
+                        int nthreads, float* kernel_ms);
+/* gopen(oflags) + gwrite + gclose (libgpufs/fs_calls.cu:739); the last close
+ * writes the dirty pages back to the host file. */
+long long gfs_pwrite(gfs_ctx* ctx, const char* path, int oflags, uint64_t off, uint64_t size, const void* host_in,
+                     int nblocks, int nthreads);
+/* read through gmmap/gmunmap (use_warp_api: gmmap_warp/gmunmap_warp)
+ * (libgpufs/fs_calls.cu:385-481,618-683) */
+long long gfs_mmap_read(gfs_ctx* ctx, const char* path, uint64_t off, uint64_t size, void* host_out, int nblocks,
+                        int nthreads, int use_warp_api);
+/* gopen + fstat + gclose (libgpufs/fs_calls.cu:851) */
+long long gfs_fstat_path(gfs_ctx* ctx, const char* path);
+/* gopen(O_GRDWR) + gftruncate + gclose (libgpufs/fs_calls.cu:127-149) */
+int gfs_truncate_path(gfs_ctx* ctx, const char* path, long long size);
+/* gunlink (libgpufs/fs_calls.cu:845; unimplemented there) */
+int gfs_unlink_path(gfs_ctx* ctx, const char* path);
+/* gopen(O_GRDWR) + gwrite + gfsync (data on the host file while still open) + gclose */
+long long gfs_pwrite_fsync(gfs_ctx* ctx, const char* path, uint64_t off, uint64_t size, const void* host_in);
+
+/* memcopy sample, samples/memcopy/cp.cu:73-108 test_cpy: every block copies
+ * pages blockIdx*PAGE, stride gridDim*PAGE, from src to a new dst (O_GWRONCE).
+ * mode 0: gread/gwrite through a per-block buffer, as the reference;
+ * mode 1: gmmap both pages and copy frame to frame (half the HBM traffic).
+ * *kernel_ms (optional): kernel time. */
+int gfs_memcopy(gfs_ctx* ctx, const char* src, const char* dst, int nblocks, int nthreads, int mode,
+                float* kernel_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
