@@ -19,6 +19,10 @@ INC = os.path.join(ROOT, "include")
 OUT = os.path.join(HERE, "_build")
 
 CUDA_SOURCES = ["gfs_calls.cu", "gfs_runtime.cu", "gfs_workloads.cu"]
+# Device-API translation units are linked as relocatable code into kernels of
+# any block size (up to 1024 threads): cap them at 64 registers per thread.
+PER_FILE_FLAGS = {"gfs_calls.cu": ["-maxrregcount=64"], "gfs_workloads.cu": ["-maxrregcount=64"],
+                  "gfs_runtime.cu": ["-maxrregcount=64"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-rdc=true", "-std=c++17", "-Xcompiler", "-fPIC",
               "-I" + INC, "-I" + CSRC, "--expt-relaxed-constexpr"]
@@ -65,7 +69,7 @@ def build(verbose=False, ptxas_v=False):
         objs.append(obj)
         if not _newer(obj, [src] + hdrs):
             extra = ["-Xptxas", "-v"] if ptxas_v else []
-            jobs.append([nv] + ARCH + NVCC_FLAGS + extra + ["-c", src, "-o", obj])
+            jobs.append([nv] + ARCH + NVCC_FLAGS + PER_FILE_FLAGS.get(s, []) + extra + ["-c", src, "-o", obj])
     dg_src = os.path.join(CSRC, "datagen.c")
     dg_so = os.path.join(OUT, "libgfs_datagen.so")
     if not _newer(dg_so, [dg_src]):
