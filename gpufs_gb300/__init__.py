@@ -71,6 +71,16 @@ _SIGS = {
     "gfs_unlink_path": (_int, [_c_p, _c_s]),
     "gfs_pwrite_fsync": (_i64, [_c_p, _c_s, _u64, _u64, _c_p]),
     "gfs_memcopy": (_int, [_c_p, _c_s, _c_s, _int, _int, _int, ctypes.POINTER(ctypes.c_float)]),
+    "gfs_grep_open": (_int, [_c_p, _c_s, ctypes.POINTER(_c_s), _int, ctypes.POINTER(_c_p)]),
+    "gfs_grep_run": (_int, [_c_p, _int, ctypes.POINTER(ctypes.c_float)]),
+    "gfs_grep_counts": (_int, [_c_p, _c_p]),
+    "gfs_grep_device_counts": (_c_p, [_c_p]),
+    "gfs_grep_info": (_int, [_c_p, ctypes.POINTER(ctypes.c_longlong), _int]),
+    "gfs_grep_close": (_int, [_c_p]),
+    "gfs_grep_text": (_int, [_c_p, _c_s, ctypes.POINTER(_c_s), _int, _c_p, _int]),
+    "gfs_grep_bench": (_int, [_c_p, _int, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "gfs_drop_cache": (_i64, [_c_p]),
+    "gfs_measure_link": (_int, [_u64, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
 }
 
 
@@ -206,8 +216,82 @@ class Session:
     def last_error(self, clear=True):
         return int(self.L.gfs_last_error(self._h, 1 if clear else 0))
 
+    def drop_cache(self):
+        return _check(self.L.gfs_drop_cache(self._h), "gfs_drop_cache")
+
     def set_paused(self, paused):
         self.L.gfs_set_paused(self._h, 1 if paused else 0)
 
     def inject_read_errors(self, count, err=5):
         self.L.gfs_inject_read_errors(self._h, count, err)
+
+
+def _paths(paths):
+    arr = (ctypes.c_char_p * len(paths))(*[_p(x) for x in paths])
+    return arr
+
+
+class Grep:
+    """grep_text plan: dictionary table on the device, corpus files open in
+    the session (samples/grep_text/grep_text_gpu.cu:193-387)."""
+
+    def __init__(self, sess, dict_path, paths):
+        self.s = sess
+        self.paths = list(paths)
+        h = ctypes.c_void_p()
+        _check(sess.L.gfs_grep_open(sess.handle, _p(dict_path), _paths(self.paths), len(self.paths),
+                                    ctypes.byref(h)), "gfs_grep_open")
+        self._h = h
+        info = (ctypes.c_longlong * 6)()
+        sess.L.gfs_grep_info(h, info, 6)
+        self.n_words, self.n_files, self.buckets, self.smem_table, self.smem_bytes, self.chunks = [int(v) for v in info]
+
+    def run(self, n_ctas=0):
+        ms = ctypes.c_float(0)
+        _check(self.s.L.gfs_grep_run(self._h, n_ctas, ctypes.byref(ms)), "gfs_grep_run")
+        return ms.value
+
+    def counts(self):
+        out = np.zeros((self.n_words, self.n_files), dtype=np.uint32)
+        _check(self.s.L.gfs_grep_counts(self._h, out.ctypes.data), "gfs_grep_counts")
+        return out
+
+    def bench(self, steps, n_ctas=0):
+        """(total_ms, mean scan-kernel ms) of `steps` back-to-back runs."""
+        tot = ctypes.c_float(0)
+        scan = ctypes.c_float(0)
+        _check(self.s.L.gfs_grep_bench(self._h, n_ctas, steps, ctypes.byref(tot), ctypes.byref(scan)),
+               "gfs_grep_bench")
+        return tot.value, scan.value
+
+    def device_counts(self):
+        return self.s.L.gfs_grep_device_counts(self._h)
+
+    def close(self):
+        if self._h:
+            rc = self.s.L.gfs_grep_close(self._h)
+            self._h = None
+            _check(rc, "gfs_grep_close")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def grep_text(sess, dict_path, paths, n_ctas=0):
+    """One call: open + scan + counts + close; returns counts[word, file]."""
+    n_words = os.path.getsize(dict_path) // 32
+    out = np.zeros((n_words, len(paths)), dtype=np.uint32)
+    _check(sess.L.gfs_grep_text(sess.handle, _p(dict_path), _paths(paths), len(paths),
+                                out.ctypes.data if out.size else None, n_ctas), "gfs_grep_text")
+    return out
+
+
+def measure_link(nbytes=1 << 30, reps=5):
+    """Pinned host->device and device->host copy bandwidth in GB/s."""
+    a = ctypes.c_float(0)
+    b = ctypes.c_float(0)
+    _check(lib().gfs_measure_link(nbytes, reps, ctypes.byref(a), ctypes.byref(b)), "gfs_measure_link")
+    return a.value, b.value

@@ -302,12 +302,21 @@ __device__ __noinline__ int writeback_frame(gfs_state* S, uint32_t fr, uint64_t 
 /* Take a frame out of VALID (refcount 0) into EVICTING and then CLAIMED:
  * drop it from the index, wait out transient pins.  Dirty frames must have
  * been written back by the caller (or be stale). */
-__device__ __forceinline__ bool finish_evict(gfs_state* S, uint32_t fr, uint64_t key, bool was_dirty, Waiter& w) {
+__device__ __forceinline__ bool finish_evict(gfs_state* S, uint32_t fr, uint64_t key, bool was_dirty) {
     gfs_frame* F = &S->frames[fr];
     index_remove(S, key, fr);
     if (was_dirty) dirty_bit_clear(S, fr);
-    while ((ld_rlx(&F->st) & GFS_F_PINS) != 0u)
-        if (!w.tick(256)) return false; /* leave it EVICTING: unusable, not unsafe */
+    /* pinners that raced the CAS see EVICTING and back off at once; the
+     * drain has its own bound, independent of the caller's budget */
+    Waiter w(S->timeout_ns);
+    while ((ld_rlx(&F->st) & GFS_F_PINS) != 0u) {
+        if (!w.tick(256)) {
+            /* never reuse a frame somebody still holds: retire it */
+            atomicAdd(&F->st, (GFS_FS_DEAD - GFS_FS_EVICTING) << GFS_F_SHIFT);
+            set_error(S, GFS_ERRB_TIMEOUT);
+            return false;
+        }
+    }
     atomicAnd(&F->st, ~(GFS_F_DIRTY | GFS_F_REF));
     atomicAdd(&F->st, (GFS_FS_CLAIMED - GFS_FS_EVICTING) << GFS_F_SHIFT);
     count(S, &S->stats.evictions);
@@ -346,7 +355,7 @@ __device__ __noinline__ uint32_t alloc_frame(gfs_state* S, uint64_t budget_ns) {
                                                  ld_rlx((const uint32_t*)&fe->flags));
                         if (rc >= 0) {
                             count(S, &S->stats.writebacks);
-                            if (finish_evict(S, h, key, true, w)) return h;
+                            if (finish_evict(S, h, key, true)) return h;
                         } else {
                             /* put it back: still dirty */
                             atomicAdd(&F->st, (GFS_FS_VALID - GFS_FS_EVICTING) << GFS_F_SHIFT);
@@ -355,7 +364,7 @@ __device__ __noinline__ uint32_t alloc_frame(gfs_state* S, uint64_t budget_ns) {
                 }
             } else {
                 if (atomicCAS(&F->st, st, GFS_FS_EVICTING << GFS_F_SHIFT | (st & GFS_F_DIRTY)) == st) {
-                    if (finish_evict(S, h, key, (st & GFS_F_DIRTY) != 0u, w)) return h;
+                    if (finish_evict(S, h, key, (st & GFS_F_DIRTY) != 0u)) return h;
                 }
             }
         }
@@ -478,7 +487,7 @@ __device__ __noinline__ int pin_page(gfs_state* S, const PinFile& pf, uint32_t b
                 bool vstale = key_stale(S, vkey);
                 if ((vst & GFS_F_DIRTY) && !vstale) continue;
                 if (atomicCAS(&V->st, vst, GFS_FS_EVICTING << GFS_F_SHIFT | (vst & GFS_F_DIRTY)) != vst) continue;
-                if (finish_evict(S, vf, vkey, (vst & GFS_F_DIRTY) != 0u, w)) {
+                if (finish_evict(S, vf, vkey, (vst & GFS_F_DIRTY) != 0u)) {
                     /* finish_evict left it CLAIMED and ours: free it */
                     release_owned(S, vf, GFS_FS_CLAIMED, 0u);
                     count(S, &S->stats.conflict_evictions);

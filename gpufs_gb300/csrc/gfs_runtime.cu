@@ -292,6 +292,30 @@ static void worker_main(gfs_ctx* c, Worker* w) {
 
 static gfs_ctx* g_current = nullptr; /* session g_gfs points at */
 
+/* drop clean, unpinned, valid frames: first their index ways, then the frames */
+__global__ void k_drop_ways(gfs_state* S) {
+    size_t n = (size_t)S->n_buckets * GFS_WAYS;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        uint32_t v = S->index[i];
+        if (!v) continue;
+        uint32_t st = S->frames[v & 0x3FFFFFu].st;
+        if (((st >> GFS_F_SHIFT) & 0xFu) == GFS_FS_VALID && !(st & (GFS_F_PINS | GFS_F_DIRTY))) S->index[i] = 0u;
+    }
+}
+__global__ void k_drop_frames(gfs_state* S, unsigned long long* kept) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < S->n_frames; i += gridDim.x * blockDim.x) {
+        gfs_frame* F = &S->frames[i];
+        uint32_t st = F->st;
+        uint32_t s = (st >> GFS_F_SHIFT) & 0xFu;
+        if (s == GFS_FS_VALID && !(st & (GFS_F_PINS | GFS_F_DIRTY))) {
+            F->key = ~0ULL;
+            F->st = 0u;
+        } else if (s != GFS_FS_FREE) {
+            atomicAdd(kept, 1ULL);
+        }
+    }
+}
+
 extern "C" {
 
 /* Point the device API (g_gfs) at this session, in stream order. */
@@ -515,6 +539,64 @@ void* gfs__scratch(gfs_ctx* c, size_t bytes) {
 }
 
 const gfs_state* gfs__host_state(gfs_ctx* c) { return &c->hs; }
+
+/* Empty the buffer cache (clean, unpinned pages); returns frames kept. */
+long long gfs_drop_cache(gfs_ctx* c) {
+    cudaStream_t s = c->kstream;
+    cudaStreamSynchronize(s);
+    unsigned long long* kept = nullptr;
+    if (cudaMalloc(&kept, sizeof *kept) != cudaSuccess) return -GFS_ENOMEM;
+    cudaMemsetAsync(kept, 0, sizeof *kept, s);
+    k_drop_ways<<<1024, 256, 0, s>>>(c->ds);
+    k_drop_frames<<<1024, 256, 0, s>>>(c->ds, kept);
+    unsigned long long h = 0;
+    cudaMemcpyAsync(&h, kept, sizeof h, cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    cudaFree(kept);
+    return e == cudaSuccess ? (long long)h : -GFS_EIO;
+}
+
+/* Pinned host <-> device copy bandwidth (best of `reps`), the cold-read
+ * roofline: copy-engine cudaMemcpyAsync of `bytes` each way. */
+int gfs_measure_link(uint64_t bytes, int reps, float* h2d_gbs, float* d2h_gbs) {
+    void* h = nullptr;
+    void* d = nullptr;
+    if (cudaHostAlloc(&h, bytes, cudaHostAllocDefault) != cudaSuccess) return -GFS_ENOMEM;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) {
+        cudaFreeHost(h);
+        return -GFS_ENOMEM;
+    }
+    memset(h, 1, bytes);
+    cudaStream_t s;
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best_h2d = 0, best_d2h = 0;
+    for (int dir = 0; dir < 2; dir++) {
+        for (int r = 0; r < reps + 1; r++) {
+            cudaEventRecord(a, s);
+            if (dir == 0) cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s);
+            else cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, s);
+            cudaEventRecord(b, s);
+            cudaEventSynchronize(b);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, a, b);
+            float gbs = (float)((double)bytes / (ms * 1e-3) / 1e9);
+            if (r == 0) continue; /* warm-up */
+            if (dir == 0 && gbs > best_h2d) best_h2d = gbs;
+            if (dir == 1 && gbs > best_d2h) best_d2h = gbs;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaStreamDestroy(s);
+    cudaFree(d);
+    cudaFreeHost(h);
+    if (h2d_gbs) *h2d_gbs = best_h2d;
+    if (d2h_gbs) *d2h_gbs = best_d2h;
+    return 0;
+}
 
 double _timestamp() {
     struct timeval tv;

@@ -69,6 +69,11 @@ uint32_t gfs_last_error(gfs_ctx* ctx, int clear);
 /* counters; replaces the PRINT_* statistics of libgpufs/fs_debug.cu.h:99-148 */
 int gfs_get_stats(gfs_ctx* ctx, unsigned long long* out, int n);
 int gfs_reset_stats(gfs_ctx* ctx);
+/* empty the buffer cache of clean, unpinned pages (no kernel may be running);
+ * returns the number of frames kept (pinned or dirty) */
+long long gfs_drop_cache(gfs_ctx* ctx);
+/* pinned host<->device cudaMemcpyAsync bandwidth, best of `reps` (GB/s) */
+int gfs_measure_link(uint64_t bytes, int reps, float* h2d_gbs, float* d2h_gbs);
 
 /* ---- host-side fault injection (tests only; no GPU fault is ever made) ---- */
 /* stall (1) or resume (0) the host service: device waits then time out */
@@ -110,6 +115,31 @@ long long gfs_pwrite_fsync(gfs_ctx* ctx, const char* path, uint64_t off, uint64_
  * *kernel_ms (optional): kernel time. */
 int gfs_memcopy(gfs_ctx* ctx, const char* src, const char* dst, int nblocks, int nthreads, int mode,
                 float* kernel_ms);
+
+/* ---- grep_text (samples/grep_text/grep_text_gpu.cu:193-387) ----
+ * Whole-word occurrence counts of every record of a dictionary file (32-byte
+ * NUL-padded records, the reference's dict.gpu format) in every corpus file,
+ * read through the buffer cache.  counts[w * n_files + f] (uint32).
+ * gfs_grep_open reads the dictionary, builds its hash table, uploads it and
+ * opens the corpus files on the device; gfs_grep_run scans (files stay open
+ * and cached between runs); gfs_grep_close closes them. */
+typedef struct gfs_grep gfs_grep;
+int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths, int n_files, gfs_grep** out);
+/* n_ctas <= 0: one per SM.  *kernel_ms (optional): device time of the scan. */
+int gfs_grep_run(gfs_grep* g, int n_ctas, float* kernel_ms);
+int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts);
+/* device address of the counts (n_words * n_files uint32) */
+void* gfs_grep_device_counts(gfs_grep* g);
+/* out: n_words, n_files, buckets, table in shared memory (0/1), dynamic shared
+ * bytes, chunks */
+int gfs_grep_info(gfs_grep* g, long long* out, int n);
+int gfs_grep_close(gfs_grep* g);
+/* `steps` runs back to back on the kernel stream; *total_ms: all of them
+ * (CUDA events), *scan_ms: mean duration of one scan kernel */
+int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* scan_ms);
+/* one call: open + run + counts to host + close (the reference sample's whole run) */
+int gfs_grep_text(gfs_ctx* ctx, const char* dict_path, const char* const* paths, int n_files, uint32_t* host_counts,
+                  int n_ctas);
 
 #ifdef __cplusplus
 }

@@ -24,7 +24,7 @@ def build():
     if not os.path.exists(REF_SRC) and os.path.isdir(REFERENCE_ROOT):
         subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT])
     if os.path.exists(REF_SRC) and (not os.path.exists(REF_SO) or os.path.getmtime(REF_SO) < os.path.getmtime(REF_SRC)):
-        subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-o", REF_SO, REF_SRC])
+        subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-pthread", "-o", REF_SO, REF_SRC])
 
 
 _L = None
@@ -65,8 +65,26 @@ def ref():
         r = ctypes.CDLL(REF_SO)
         r.ref_match_string.restype = ctypes.c_int
         r.ref_match_string.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
+        if hasattr(r, "ref_grep_counts"):
+            vp = ctypes.c_void_p
+            r.ref_grep_counts.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, ctypes.c_int]
         _R = r
     return _R
+
+
+def ref_grep_counts(dict_bytes, files, nthreads=None):
+    """The reference's own matcher driven through its window walk (CPU), or
+    None when the reference-derived library was not built."""
+    r = ref()
+    if r is None or not hasattr(r, "ref_grep_counts"):
+        return None
+    d = np.ascontiguousarray(np.frombuffer(dict_bytes, dtype=np.uint8))
+    nw = d.size // 32
+    arrs, ptrs, sizes = _files_arrays(files)
+    out = np.zeros((nw, len(arrs)), dtype=np.uint32)
+    r.ref_grep_counts(d.ctypes.data, nw, ptrs, sizes, len(arrs), out.ctypes.data,
+                      nthreads or max(1, os.cpu_count() or 1))
+    return out
 
 
 def xxh64(data, seed=0):

@@ -1,0 +1,130 @@
+"""grep_text on the GPU equals the oracle (the reference's match_string
+semantics, including its chunk-walk cuts of long letter runs)."""
+import os
+
+import numpy as np
+import pytest
+
+import gpufs_gb300 as g
+from gpufs_gb300 import datagen
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sess(built):
+    s = g.Session(log_page=16, pool_bytes=512 << 20, max_files=256, timeout_s=20)
+    yield s
+    s.close()
+
+
+def _check(sess, dpath, paths, n_ctas=0):
+    with g.Grep(sess, dpath, paths) as gr:
+        gr.run(n_ctas)
+        got = gr.counts()
+        gr.run(n_ctas)  # second run: cache-resident, same answer
+        got2 = gr.counts()
+    want = oracle.grep_counts(open(dpath, "rb").read(), [open(p, "rb").read() for p in paths], mode="fast")
+    assert got.shape == want.shape
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, (bad[:5], got[tuple(bad[0])], want[tuple(bad[0])])
+    assert np.array_equal(got, got2)
+    return got
+
+
+def test_zipf_corpus(sess, shm_dir):
+    paths, dpath = datagen.grep_corpus(shm_dir, n_files=5, total_bytes=9 * (1 << 20) + 12345, n_vocab=5000,
+                                       n_dict=2000, seed=3)
+    got = _check(sess, dpath, paths)
+    assert got.sum() > 100000
+    assert sess.last_error() == 0
+
+
+@pytest.mark.parametrize("n_ctas", [1, 7, 152, 600])
+def test_grid_sizes(sess, shm_dir, n_ctas):
+    paths, dpath = datagen.grep_corpus(shm_dir, n_files=3, total_bytes=3 * (1 << 20) + 777, n_vocab=3000,
+                                       n_dict=1000, seed=4)
+    _check(sess, dpath, paths, n_ctas)
+
+
+def _write(path, data):
+    with open(path, "wb") as f:
+        f.write(data)
+
+
+def test_adversarial_tokens(sess, shm_dir):
+    """Upper case, underscores, digits, bytes >= 0x80, NULs, tokens of 31/32/33+
+    letters, and long letter runs across the reference's 16384-byte windows."""
+    rng = np.random.default_rng(7)
+    words = [b"cat", b"Cat", b"c_t", b"_", b"a", b"zz" * 16, b"q" * 31, b"r" * 32, b"tail", b"kkkk", b"ab" * 8]
+    recs = b"".join(w + b"\0" * (32 - len(w)) for w in words) + b"\0" * 32 + b"cat" + b"\0" * 29
+    dpath = os.path.join(shm_dir, "d.gpu")
+    _write(dpath, recs)
+    paths = []
+    for fi in range(4):
+        parts = []
+        n = 0
+        while n < 150000 + 40000 * fi:
+            r = rng.random()
+            if r < 0.6:
+                t = words[int(rng.integers(0, len(words)))]
+            elif r < 0.7:
+                t = bytes(rng.integers(0, 256, int(rng.integers(1, 6)), dtype=np.uint8))
+            elif r < 0.8:
+                t = b"k" * int(rng.integers(30, 70))
+            else:
+                t = b"".join(words[int(rng.integers(0, 4))] for _ in range(int(rng.integers(1, 4))))
+            parts.append(t)
+            parts.append(bytes([int(rng.choice(list(b" \n\t.,;09'-\x00\xff")))]))
+            n += len(t) + 1
+        data = bytearray(b"".join(parts))
+        # letter runs crossing window edges (16384, 32768+overlap, ...)
+        for base in (16370, 32760, 65530):
+            data[base:base + 80] = b"k" * 76 + b"tail"
+        p = os.path.join(shm_dir, "adv%d.txt" % fi)
+        _write(p, bytes(data))
+        paths.append(p)
+    assert any(len(oracle.split_points(open(p, "rb").read())) for p in paths)
+    _check(sess, dpath, paths)
+
+
+def test_page_sizes_and_tiny_files(built, shm_dir):
+    paths, dpath = datagen.grep_corpus(shm_dir, n_files=4, total_bytes=2 * (1 << 20) + 99, n_vocab=2000,
+                                       n_dict=500, seed=5)
+    t1 = os.path.join(shm_dir, "t1.txt")
+    _write(t1, b"")
+    t2 = os.path.join(shm_dir, "t2.txt")
+    words = open(dpath, "rb").read()
+    first = words[:32].rstrip(b"\0")
+    _write(t2, first)  # a word right at end of file, no delimiter
+    paths = paths + [t1, t2]
+    for lp in (12, 14, 16, 20):
+        with g.Session(log_page=lp, pool_bytes=128 << 20, timeout_s=20) as s:
+            _check(s, dpath, paths)
+
+
+def test_large_dictionary_global_table(sess, shm_dir):
+    """A dictionary too large for shared memory uses the table in global memory."""
+    voc = datagen.vocab(60000, seed=9, minlen=3, maxlen=12)
+    dpath = os.path.join(shm_dir, "big.gpu")
+    datagen.dictionary(dpath, voc, 58112, seed=2)
+    paths = [os.path.join(shm_dir, "z%d.txt" % i) for i in range(2)]
+    datagen.zipf_files(paths, [1 << 20, (1 << 20) + 5], voc, s=1.1, seed=8)
+    with g.Grep(sess, dpath, paths) as gr:
+        assert gr.smem_table == 0
+    _check(sess, dpath, paths)
+
+
+def test_pool_smaller_than_corpus(built, shm_dir):
+    paths, dpath = datagen.grep_corpus(shm_dir, n_files=3, total_bytes=24 << 20, n_vocab=3000, n_dict=1000, seed=6)
+    with g.Session(log_page=16, pool_bytes=8 << 20, timeout_s=20) as s:
+        _check(s, dpath, paths, n_ctas=8)
+        assert s.stats()["evictions"] > 0
+
+
+def test_one_shot_grep_text(sess, shm_dir):
+    paths, dpath = datagen.grep_corpus(shm_dir, n_files=2, total_bytes=1 << 20, n_vocab=1000, n_dict=300, seed=10)
+    got = g.grep_text(sess, dpath, paths)
+    want = oracle.grep_counts(open(dpath, "rb").read(), [open(p, "rb").read() for p in paths])
+    assert np.array_equal(got, want)

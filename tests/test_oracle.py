@@ -160,3 +160,18 @@ def test_reference_fixture_counts(built):
         g = json.load(f)
     assert int(fast.sum()) == g["total"]
     assert oracle.xxh64(fast.astype("<u4").tobytes()) == int(g["xxh64"], 16)
+
+
+def test_reference_cpu_path_equals_faithful(built):
+    """The reference's own match_string, driven through its window walk,
+    equals the faithful restatement (also on long runs across windows)."""
+    rng = np.random.default_rng(11)
+    words = [b"cat", b"at", b"kkkk", b"k" * 32, b"tail"]
+    recs = b"".join(w + b"\0" * (32 - len(w)) for w in words)
+    data = bytearray(rng.choice(list(b"catk \n."), 60000).astype(np.uint8).tobytes())
+    data[16370:16450] = b"k" * 76 + b"tail"
+    got = oracle.ref_grep_counts(recs, [bytes(data), bytes(data[:30000])], nthreads=2)
+    if got is None:
+        pytest.skip("reference matcher not built")
+    want = oracle.grep_counts(recs, [bytes(data), bytes(data[:30000])], mode="faithful")
+    assert np.array_equal(got, want)
