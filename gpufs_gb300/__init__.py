@@ -28,7 +28,7 @@ O_GWRONCE = O_CREAT | O_WRONLY
 
 STAT_NAMES = ["hits", "misses", "evictions", "writebacks", "read_rpcs", "bytes_read_rpc", "opens", "closes",
               "timeouts", "errors", "conflict_evictions", "host_requests", "host_reads", "host_read_bytes",
-              "host_writes", "host_write_bytes", "host_opens", "host_errors"]
+              "host_writes", "host_write_bytes", "host_opens", "host_errors", "err_site", "rpc_submitted"]
 
 ERR_TIMEOUT, ERR_IO, ERR_NOMEM, ERR_TABLE, ERR_ARG = 1, 2, 4, 8, 16
 
@@ -213,6 +213,11 @@ class Session:
     def reset_stats(self):
         self.L.gfs_reset_stats(self._h)
 
+    def error_report(self):
+        st = self.stats()
+        return "error bits 0x%x, first failure site %d errno %d, stats %s" % (
+            self.last_error(clear=False), st.get("err_site", 0) >> 16, st.get("err_site", 0) & 0xFFFF, st)
+
     def last_error(self, clear=True):
         return int(self.L.gfs_last_error(self._h, 1 if clear else 0))
 
@@ -242,13 +247,21 @@ class Grep:
         _check(sess.L.gfs_grep_open(sess.handle, _p(dict_path), _paths(self.paths), len(self.paths),
                                     ctypes.byref(h)), "gfs_grep_open")
         self._h = h
-        info = (ctypes.c_longlong * 6)()
-        sess.L.gfs_grep_info(h, info, 6)
-        self.n_words, self.n_files, self.buckets, self.smem_table, self.smem_bytes, self.chunks = [int(v) for v in info]
+        self._info()
+
+    def _info(self):
+        info = (ctypes.c_longlong * 8)()
+        self.s.L.gfs_grep_info(self._h, info, 8)
+        (self.n_words, self.n_files, self.buckets, self.smem_table, self.smem_bytes, self.chunks, self.status,
+         self.status_site) = [int(v) for v in info]
 
     def run(self, n_ctas=0):
         ms = ctypes.c_float(0)
-        _check(self.s.L.gfs_grep_run(self._h, n_ctas, ctypes.byref(ms)), "gfs_grep_run")
+        rc = self.s.L.gfs_grep_run(self._h, n_ctas, ctypes.byref(ms))
+        if rc < 0:
+            self._info()
+            raise GfsError(-rc, "gfs_grep_run failed: status 0x%x site 0x%x, session %s" % (
+                self.status, self.status_site, self.s.error_report()))
         return ms.value
 
     def counts(self):

@@ -249,9 +249,11 @@ static int write_zipf_text(const char* path, uint64_t nbytes, uint64_t seed, uin
         buf[fill++] = ' ';
         line += len + 1;
         if (fill >= BUF) {
-            if (write_all(fd, buf, fill, (off_t)written)) { err = 1; break; }
-            written += fill;
-            fill = 0;
+            /* keep the last separator in the buffer: it may become a newline */
+            if (write_all(fd, buf, fill - 1, (off_t)written)) { err = 1; break; }
+            written += fill - 1;
+            buf[0] = buf[fill - 1];
+            fill = 1;
         }
     }
     if (!err && fill) {

@@ -133,6 +133,11 @@ __device__ __forceinline__ void count(gfs_state* S, unsigned long long* c, unsig
     atomicAdd(c, v);
 }
 __device__ __forceinline__ void set_error(gfs_state* S, uint32_t bit) { atomicOr(&S->error, bit); }
+/* record the first failure's site (for diagnosis) and set the sticky bit */
+__device__ __forceinline__ void fail_at(gfs_state* S, uint32_t bit, uint32_t site, int err) {
+    atomicOr(&S->error, bit);
+    atomicCAS(&S->stats.err_site, 0ULL, ((unsigned long long)site << 16) | (unsigned long long)(err < 0 ? -err : err));
+}
 
 /* ------------------------------------------------------------------ */
 /* keys and hashing                                                    */
@@ -229,7 +234,7 @@ __device__ __noinline__ int rpc_call(gfs_state* S, const Req& r, uint32_t* done)
     while (ld_acq_sys(&slot->seq) != t) {
         if (!w.tick(2048)) {
             count(S, &S->stats.timeouts);
-            set_error(S, GFS_ERRB_TIMEOUT);
+            fail_at(S, GFS_ERRB_TIMEOUT, 1, GFS_ETIMEDOUT); /* ring slot never freed */
             return -GFS_ETIMEDOUT;
         }
     }
@@ -252,11 +257,12 @@ __device__ __noinline__ int rpc_call(gfs_state* S, const Req& r, uint32_t* done)
     }
     __threadfence_system();
     st_rel_sys(&slot->seq, t + 1u);
+    count(S, &S->stats.rpc_submitted);
     uint32_t c;
     while ((c = ld_acq(done)) == 0u) {
         if (!w.tick(1024)) {
             count(S, &S->stats.timeouts);
-            set_error(S, GFS_ERRB_TIMEOUT);
+            fail_at(S, GFS_ERRB_TIMEOUT, 2 + 16 * (uint32_t)r.op, GFS_ETIMEDOUT); /* no completion */
             return -GFS_ETIMEDOUT;
         }
     }
@@ -313,7 +319,7 @@ __device__ __forceinline__ bool finish_evict(gfs_state* S, uint32_t fr, uint64_t
         if (!w.tick(256)) {
             /* never reuse a frame somebody still holds: retire it */
             atomicAdd(&F->st, (GFS_FS_DEAD - GFS_FS_EVICTING) << GFS_F_SHIFT);
-            set_error(S, GFS_ERRB_TIMEOUT);
+            fail_at(S, GFS_ERRB_TIMEOUT, 3, GFS_ETIMEDOUT); /* pins never drained */
             return false;
         }
     }
@@ -437,7 +443,7 @@ __device__ __noinline__ int pin_page(gfs_state* S, const PinFile& pf, uint32_t b
                         if (!w.tick(1024)) {
                             atomicSub(&F->st, 1u);
                             count(S, &S->stats.timeouts);
-                            set_error(S, GFS_ERRB_TIMEOUT);
+                            fail_at(S, GFS_ERRB_TIMEOUT, 4, GFS_ETIMEDOUT); /* LOADING never ended */
                             return -GFS_ETIMEDOUT;
                         }
                     }
@@ -452,7 +458,7 @@ __device__ __noinline__ int pin_page(gfs_state* S, const PinFile& pf, uint32_t b
         /* miss: allocate outside the bucket lock, insert under it */
         uint32_t nf = alloc_frame(S, soft ? 2000000ull : S->timeout_ns);
         if (nf == GFS_NO_FRAME) {
-            if (!soft) { set_error(S, GFS_ERRB_NOMEM); count(S, &S->stats.errors); }
+            if (!soft) { fail_at(S, GFS_ERRB_NOMEM, 5, GFS_ENOMEM); count(S, &S->stats.errors); }
             return -GFS_ENOMEM;
         }
         gfs_frame* F = &S->frames[nf];
@@ -464,7 +470,7 @@ __device__ __noinline__ int pin_page(gfs_state* S, const PinFile& pf, uint32_t b
         if (!spin_lock(&S->bucket_lock[bidx], w)) {
             release_owned(S, nf, GFS_FS_LOADING, 1u);
             count(S, &S->stats.timeouts);
-            set_error(S, GFS_ERRB_TIMEOUT);
+            fail_at(S, GFS_ERRB_TIMEOUT, 6, GFS_ETIMEDOUT);
             return -GFS_ETIMEDOUT;
         }
         if (index_find(S, key, h) != GFS_NO_FRAME) {
@@ -539,7 +545,7 @@ __device__ __noinline__ int pin_page(gfs_state* S, const PinFile& pf, uint32_t b
         return (int)nf;
     }
     count(S, &S->stats.timeouts);
-    set_error(S, GFS_ERRB_TIMEOUT);
+    fail_at(S, GFS_ERRB_TIMEOUT, 7, GFS_ETIMEDOUT); /* stale pins / full bucket retries */
     return -GFS_ETIMEDOUT;
 }
 
@@ -575,7 +581,7 @@ __device__ __noinline__ int flush_frame(gfs_state* S, uint32_t fr, uint32_t slot
         uint32_t st = ld_acq(&F->st);
         uint32_t s = fstate(st);
         if (s == GFS_FS_EVICTING) {
-            if (!w.tick(1024)) { set_error(S, GFS_ERRB_TIMEOUT); return -GFS_ETIMEDOUT; }
+            if (!w.tick(1024)) { fail_at(S, GFS_ERRB_TIMEOUT, 8, GFS_ETIMEDOUT); return -GFS_ETIMEDOUT; }
             continue;
         }
         if (s != GFS_FS_VALID || !(st & GFS_F_DIRTY)) return 0;

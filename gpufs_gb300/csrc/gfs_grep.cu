@@ -75,7 +75,8 @@ struct GrepDev {
     const int32_t* next_dup;      /* next record with the same word, -1 */
     uint32_t* counts;             /* n_words x n_files */
     uint32_t* long_flags;         /* per file: a run of >= 33 letters was seen */
-    uint32_t* status;             /* error word */
+    uint32_t* status;             /* [0] error bits, [1] first failure: site << 16 | errno */
+    uint32_t win_data;            /* data pages per window (window = data + look-behind/ahead) */
 };
 
 namespace {
@@ -207,24 +208,26 @@ __device__ __forceinline__ void count_key(const GrepDev& P, uint32_t* tbl, const
     }
 }
 
-/* Pin the window's pages (warp 0; one lane per page).  Returns 0 or -err. */
+/* Pin the window's pages (warp 0; one lane per page).  Returns 0, -GFS_ENOMEM
+ * when the pool could not hold the whole window (nothing is left pinned;
+ * the caller shrinks the window), or another -err. */
 __device__ int pin_window(const Ctx& C, Shared& sh, int fd, uint64_t fsize, uint32_t lb, int n) {
     const int lane = threadIdx.x & 31;
     int r = 0;
     if (lane < n) {
         PinFile pf = pin_file(C.S, fd);
         bool fresh;
-        r = pin_page(C.S, pf, lb + (uint32_t)lane, GFS_PIN_READ, &fresh);
+        r = pin_page(C.S, pf, lb + (uint32_t)lane, GFS_PIN_READ | (n > 1 ? GFS_PIN_NOALLOC : 0), &fresh);
         if (r >= 0 && fresh) { /* beyond the host file: cannot happen below fsize */
             publish_valid(C.S, (uint32_t)r);
         }
         sh.win_frames[lane] = r;
     }
-    unsigned bad = __ballot_sync(0xFFFFFFFFu, lane < n && r < 0);
-    if (bad) {
+    unsigned bad = __ballot_sync(0xFFFFFFFFu, lane < n && r < 0 && r != -GFS_ENOMEM);
+    unsigned nomem = __ballot_sync(0xFFFFFFFFu, lane < n && r == -GFS_ENOMEM);
+    if (bad || nomem) {
         if (lane < n && r >= 0) unpin(C.S, (uint32_t)r);
-        int e = __shfl_sync(0xFFFFFFFFu, r, __ffs(bad) - 1);
-        return e;
+        return bad ? __shfl_sync(0xFFFFFFFFu, r, __ffs(bad) - 1) : -GFS_ENOMEM;
     }
     return 0;
 }
@@ -381,7 +384,14 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
     const uint32_t page = S->page_size;
     const uint32_t chunks_per_page = page >= GR_CH ? page / GR_CH : 1u;
     const uint32_t pages_per_chunk = page >= GR_CH ? 1u : GR_CH / page;
-    const uint32_t data_pages = page >= GR_CH ? (GR_WIN - 2) : ((GR_WIN - 2) / pages_per_chunk) * pages_per_chunk;
+    __shared__ uint32_t s_wdp; /* data pages per window; halved when the pool is short */
+    if (threadIdx.x == 0) {
+        uint32_t w = P.win_data ? P.win_data : (GR_WIN - 2);
+        if (w > GR_WIN - 2) w = GR_WIN - 2;
+        w = w / pages_per_chunk * pages_per_chunk;
+        s_wdp = w ? w : pages_per_chunk;
+    }
+    __syncthreads();
 
     uint64_t cur = c0;
     while (cur < c1 && !sh.err) {
@@ -402,7 +412,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
         while (k < kend && !sh.err) {
             /* window: data pages from the page of chunk k */
             const uint32_t dp0 = (uint32_t)((k * GR_CH) >> C.lp);
-            uint32_t dp1 = dp0 + data_pages;
+            uint32_t dp1 = dp0 + s_wdp;
             const uint32_t need_end = (uint32_t)(((kend * GR_CH < fsize ? kend * GR_CH : fsize) + page - 1) >> C.lp);
             if (dp1 > need_end) dp1 = need_end;
             uint32_t lb = dp0;
@@ -419,9 +429,23 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
                 }
                 __syncwarp();
                 int e = pin_window(C, sh, fd, fsize, lb, (int)(ub - lb));
-                if (lane == 0 && e) sh.err = e;
+                if (lane == 0 && e) {
+                    if (e == -GFS_ENOMEM && s_wdp > pages_per_chunk) {
+                        s_wdp = (s_wdp / 2 + pages_per_chunk - 1) / pages_per_chunk * pages_per_chunk;
+                        sh.err = 1; /* retry this window smaller */
+                    } else {
+                        sh.err = e;
+                        atomicCAS(&P.status[1], 0u, (2u << 16) | (uint32_t)(-e));
+                    }
+                }
             }
             __syncthreads();
+            if (sh.err == 1) {
+                __syncthreads();
+                if (threadIdx.x == 0) sh.err = 0;
+                __syncthreads();
+                continue;
+            }
             if (sh.err) break;
             if (threadIdx.x == 0 && first_window) {
                 sh.prev_alpha[parity] = k == 0 ? 0u : (uint32_t)is_alpha(gbyte(C, sh, fsize, k * GR_CH - 1));
@@ -467,6 +491,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
                             if (threadIdx.x == 0) {
                                 sh.err = -GFS_ETIMEDOUT;
                                 atomicOr(P.status, GFS_ERRB_TIMEOUT);
+                                atomicCAS(&P.status[1], 0u, (1u << 16) | (uint32_t)(g & 0xFFFFu));
                             }
                             break;
                         }
@@ -713,7 +738,16 @@ struct gfs_grep {
     bool smem = true;
     size_t smem_bytes = 0;
     int sms = 0;
+    uint32_t last_status[2] = {0, 0};
 };
+
+/* Data pages per window so that all CTAs' windows fit in half the pool. */
+static void set_window(gfs_grep* g, int n_ctas) {
+    uint32_t frames = gfs_num_frames(g->ctx);
+    uint64_t per = (uint64_t)frames / 2u / (uint64_t)(n_ctas > 0 ? n_ctas : 1);
+    uint32_t w = per > 2u ? (uint32_t)(per - 2u) : 1u;
+    g->dev.win_data = w > GR_WIN - 2 ? GR_WIN - 2 : w;
+}
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -814,8 +848,9 @@ int gfs_grep_run(gfs_grep* g, int n_ctas, float* kernel_ms) {
     GrepDev& d = g->dev;
     cudaMemsetAsync(d.counts, 0, (size_t)g->n_words * g->n_files * 4, s);
     cudaMemsetAsync(d.long_flags, 0, (size_t)g->n_files * 4, s);
-    cudaMemsetAsync(d.status, 0, 4, s);
+    cudaMemsetAsync(d.status, 0, 8, s);
     if (n_ctas <= 0) n_ctas = g->sms;
+    set_window(g, n_ctas);
     cudaEvent_t a, b;
     if (kernel_ms) {
         cudaEventCreate(&a);
@@ -838,9 +873,11 @@ int gfs_grep_run(gfs_grep* g, int n_ctas, float* kernel_ms) {
         fprintf(stderr, "gpufs_gb300: grep kernel failed: %s\n", cudaGetErrorString(le != cudaSuccess ? le : e));
         return -GFS_EIO;
     }
-    uint32_t status = 0;
-    cudaMemcpy(&status, d.status, 4, cudaMemcpyDeviceToHost);
-    return status ? -((status & GFS_ERRB_TIMEOUT) ? GFS_ETIMEDOUT : GFS_EIO) : 0;
+    uint32_t status[2] = {0, 0};
+    cudaMemcpy(status, d.status, 8, cudaMemcpyDeviceToHost);
+    g->last_status[0] = status[0];
+    g->last_status[1] = status[1];
+    return status[0] ? -((status[0] & GFS_ERRB_TIMEOUT) ? GFS_ETIMEDOUT : GFS_EIO) : 0;
 }
 
 /* `steps` back-to-back runs on the kernel stream without host round trips;
@@ -855,7 +892,8 @@ int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* s
     gfs_state* S = (gfs_state*)gfs_device_state(g->ctx);
     std::vector<cudaEvent_t> ev((size_t)steps * 2 + 2);
     for (auto& e : ev) cudaEventCreate(&e);
-    cudaMemsetAsync(d.status, 0, 4, s);
+    cudaMemsetAsync(d.status, 0, 8, s);
+    set_window(g, n_ctas);
     cudaEventRecord(ev[0], s);
     for (int i = 0; i < steps; i++) {
         cudaMemsetAsync(d.counts, 0, (size_t)g->n_words * g->n_files * 4, s);
@@ -879,9 +917,11 @@ int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* s
     if (total_ms) *total_ms = tot;
     if (scan_ms) *scan_ms = sum / (float)steps;
     if (e != cudaSuccess) return -GFS_EIO;
-    uint32_t status = 0;
-    cudaMemcpy(&status, d.status, 4, cudaMemcpyDeviceToHost);
-    return status ? -GFS_EIO : 0;
+    uint32_t status[2] = {0, 0};
+    cudaMemcpy(status, d.status, 8, cudaMemcpyDeviceToHost);
+    g->last_status[0] = status[0];
+    g->last_status[1] = status[1];
+    return status[0] ? -GFS_EIO : 0;
 }
 
 int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts) {
@@ -894,9 +934,9 @@ int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts) {
 }
 
 int gfs_grep_info(gfs_grep* g, long long* out, int n) {
-    long long v[6] = {g->n_words, g->n_files, (long long)g->T.nb, g->smem ? 1 : 0, (long long)g->smem_bytes,
-                      (long long)g->dev.total_chunks};
-    int k = n < 6 ? n : 6;
+    long long v[8] = {g->n_words, g->n_files, (long long)g->T.nb, g->smem ? 1 : 0, (long long)g->smem_bytes,
+                      (long long)g->dev.total_chunks, (long long)g->last_status[0], (long long)g->last_status[1]};
+    int k = n < 8 ? n : 8;
     for (int i = 0; i < k; i++) out[i] = v[i];
     return k;
 }

@@ -491,7 +491,8 @@ int gfs_get_stats(gfs_ctx* c, unsigned long long* out, int n) {
     unsigned long long v[GFS_NSTATS] = {
         st.hits, st.misses, st.evictions, st.writebacks, st.read_rpcs, st.bytes_read_rpc, st.opens, st.closes,
         st.timeouts, st.errors, st.conflict_evictions, c->h_requests.load(), c->h_reads.load(),
-        c->h_read_bytes.load(), c->h_writes.load(), c->h_write_bytes.load(), c->h_opens.load(), c->h_errors.load()};
+        c->h_read_bytes.load(), c->h_writes.load(), c->h_write_bytes.load(), c->h_opens.load(), c->h_errors.load(),
+        st.err_site, st.rpc_submitted};
     int k = n < GFS_NSTATS ? n : GFS_NSTATS;
     for (int i = 0; i < k; i++) out[i] = v[i];
     return k;

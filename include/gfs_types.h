@@ -156,7 +156,9 @@ typedef struct gfs_stats {
     unsigned long long timeouts;
     unsigned long long errors;
     unsigned long long conflict_evictions;
-    unsigned long long pad[5];
+    unsigned long long err_site; /* first error: site << 16 | errno */
+    unsigned long long rpc_submitted;
+    unsigned long long pad[3];
 } gfs_stats;
 
 typedef struct gfs_state {

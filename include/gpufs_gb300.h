@@ -40,11 +40,11 @@ typedef struct gfs_config {
     uint32_t pad1;
 } gfs_config;
 
-#define GFS_NSTATS 18
+#define GFS_NSTATS 20
 /* gfs_get_stats order: device hits(page accesses), misses, evictions,
  * writebacks, read_rpcs, bytes_read_rpc, opens, closes, timeouts, errors,
  * conflict_evictions; host requests, reads, read_bytes, writes, write_bytes,
- * opens, errors */
+ * opens, errors; first device failure (site << 16 | errno); requests submitted */
 
 /* ---- session ---- */
 /* defaults: 64 KiB pages, 2 GiB pool, 1024 files, 4096 ring slots, 8 workers */

@@ -168,7 +168,7 @@ def test_dirty_eviction_writes_back(built, shm_dir):
         s.pwrite(p, data, 0, g.O_GWRONCE, nblocks=2)
         st = s.stats()
         assert st["writebacks"] >= (12 << 20) // s.page_size
-        assert s.last_error() == 0
+        assert s.last_error(clear=False) == 0, s.error_report()
     assert np.array_equal(np.fromfile(p, dtype=np.uint8), data)
 
 
