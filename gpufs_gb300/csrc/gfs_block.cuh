@@ -435,7 +435,7 @@ __device__ __noinline__ int st_truncate(gfs_state* S, int fd, uint64_t size) {
     r.host_fd = (int)ld_rlx((const uint32_t*)&fe->host_fd);
     r.file = (uint32_t)fd;
     r.length = size;
-    int rc = rpc_call(S, r, &fe->done);
+    int rc = rpc_call(S, r, file_done(S, (uint32_t)fd));
     if (rc < 0) return rc;
     atomicAdd(&fe->gen, 1u);
     st_rlx64(&fe->size, size);
@@ -487,7 +487,7 @@ __device__ __noinline__ int st_unlink(gfs_state* S, const char* name) {
     r.op = GFS_OP_UNLINK;
     r.file = (uint32_t)slot;
     r.name = fe->name;
-    int rc = rpc_call(S, r, &fe->done);
+    int rc = rpc_call(S, r, file_done(S, (uint32_t)slot));
     uint32_t st = ld_acq(&fe->st);
     if (sstatus(st) == GFS_SS_CLOSED) {
         atomicAdd(&fe->gen, 1u);

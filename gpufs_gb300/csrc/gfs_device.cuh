@@ -87,6 +87,19 @@ __device__ __forceinline__ uint32_t ld_acq_sys(const uint32_t* p) {
 __device__ __forceinline__ void st_rel_sys(uint32_t* p, uint32_t v) {
     asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ void st_rlx_sys(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_rlx_sys64(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_rlx_sys(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ uint32_t atom_add_ar(uint32_t* p, uint32_t v) {
     uint32_t old;
     asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
@@ -223,11 +236,16 @@ struct Req {
     const char* name; /* device pointer, <= GFS_NAME_MAX bytes, may be null */
 };
 
-/* Publish one request and wait for its completion word.  Returns the
+/* completion words in mapped host memory, written by the host CPU */
+__device__ __forceinline__ uint32_t* frame_done(gfs_state* S, uint32_t fr) { return S->hdone + fr; }
+__device__ __forceinline__ uint32_t* file_done(gfs_state* S, uint32_t slot) { return S->hdone + S->n_frames + slot; }
+
+/* Publish one request and wait for its completion word (in mapped host
+ * memory; the host CPU writes it once the data has landed).  Returns the
  * non-negative result (bytes moved, or 0) or -errno / -GFS_ETIMEDOUT. */
 __device__ __noinline__ int rpc_call(gfs_state* S, const Req& r, uint32_t* done) {
-    st_rlx(done, 0u);
-    __threadfence();
+    st_rlx_sys(done, 0u);
+    __threadfence_system();
     Waiter w(S->timeout_ns);
     uint32_t t = atomicAdd(&S->ring_tail, 1u);
     gfs_req* slot = S->ring + (t & (S->ring_slots - 1));
@@ -259,7 +277,7 @@ __device__ __noinline__ int rpc_call(gfs_state* S, const Req& r, uint32_t* done)
     st_rel_sys(&slot->seq, t + 1u);
     count(S, &S->stats.rpc_submitted);
     uint32_t c;
-    while ((c = ld_acq(done)) == 0u) {
+    while ((c = ld_acq_sys(done)) == 0u) {
         if (!w.tick(1024)) {
             count(S, &S->stats.timeouts);
             fail_at(S, GFS_ERRB_TIMEOUT, 2 + 16 * (uint32_t)r.op, GFS_ETIMEDOUT); /* no completion */
@@ -524,7 +542,7 @@ __device__ __noinline__ int pin_page(gfs_state* S, const PinFile& pf, uint32_t b
             r.length = left < S->page_size ? left : S->page_size;
             r.dev_addr = (uint64_t)(uintptr_t)frame_data(S, nf);
             count(S, &S->stats.read_rpcs);
-            int got = rpc_call(S, r, &F->done);
+            int got = rpc_call(S, r, frame_done(S, nf));
             if (got < 0) {
                 index_remove(S, key, nf);
                 if (got == -GFS_ETIMEDOUT) {
@@ -568,7 +586,7 @@ __device__ __noinline__ int writeback_frame(gfs_state* S, uint32_t fr, uint64_t 
     r.offset = (uint64_t)key_block(key) << S->log_page;
     r.length = content;
     r.dev_addr = (uint64_t)(uintptr_t)frame_data(S, fr);
-    return rpc_call(S, r, &F->done);
+    return rpc_call(S, r, frame_done(S, fr));
 }
 
 /* Flush one dirty frame of file `slot` (single thread).  Returns 0 or -err. */
@@ -702,10 +720,18 @@ __device__ __noinline__ int file_open(gfs_state* S, const char* name, int oflags
                 r.op = GFS_OP_OPEN;
                 r.file = (uint32_t)slot;
                 r.oflags = oflags;
-                r.dev_addr = (uint64_t)(uintptr_t)&fe->host_fd;
                 r.name = fe->name;
                 count(S, &S->stats.opens);
-                int rc = rpc_call(S, r, &fe->done);
+                int rc = rpc_call(S, r, file_done(S, (uint32_t)slot));
+                if (rc >= 0) {
+                    /* the reply sits in mapped host memory: copy it in */
+                    const gfs_open_reply* rep = S->hreply + slot;
+                    st_rlx((uint32_t*)&fe->host_fd, ld_rlx_sys((const uint32_t*)&rep->host_fd));
+                    st_rlx((uint32_t*)&fe->err, 0u);
+                    st_rlx64(&fe->size, ld_rlx_sys64(&rep->size));
+                    st_rlx64((uint64_t*)&fe->ctime_ns, ld_rlx_sys64((const uint64_t*)&rep->ctime_ns));
+                    __threadfence();
+                }
                 if (rc < 0) {
                     st_rlx((uint32_t*)&fe->err, (uint32_t)(-rc));
                     __threadfence();
@@ -774,7 +800,7 @@ __device__ __forceinline__ int file_close_finish(gfs_state* S, int fd) {
     r.host_fd = (int)ld_rlx((const uint32_t*)&fe->host_fd);
     r.file = (uint32_t)fd;
     count(S, &S->stats.closes);
-    int rc = rpc_call(S, r, &fe->done);
+    int rc = rpc_call(S, r, file_done(S, (uint32_t)fd));
     __threadfence();
     uint32_t to = (rc == -GFS_ETIMEDOUT) ? GFS_SS_BROKEN : GFS_SS_CLOSED;
     atomicAdd(&fe->st, (to - GFS_SS_CLOSING) << GFS_S_SHIFT);

@@ -753,6 +753,15 @@ static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 extern "C" {
 
+void gfs__preload_grep() {
+    cudaFuncAttributes a;
+    cudaFuncGetAttributes(&a, k_grep_scan<true>);
+    cudaFuncGetAttributes(&a, k_grep_scan<false>);
+    cudaFuncGetAttributes(&a, k_grep_fixup);
+    cudaFuncGetAttributes(&a, k_open_files);
+    cudaFuncGetAttributes(&a, k_close_files);
+}
+
 int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths, int n_files, gfs_grep** out) {
     *out = nullptr;
     if (n_files < 1 || !dict_path) return -GFS_EINVAL;

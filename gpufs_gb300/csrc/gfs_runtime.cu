@@ -15,15 +15,19 @@
  *     the session, so kernels may run at any time, not only inside the
  *     handler call;
  *   - reads go pread -> pinned staging -> cudaMemcpyAsync straight into the
- *     page frame on the worker's own stream, then cuStreamWriteValue32 puts
- *     the completion word in device memory in stream order, so the waiting
- *     block sees it only after the bytes have landed;
+ *     page frame on the worker's own stream (no device staging copy); the
+ *     worker itself writes the request's completion word, in mapped host
+ *     memory, once the copy's event has fired -- nothing in the completion
+ *     path is executed by the GPU, so a kernel that occupies every SM while
+ *     it waits cannot hold up its own completions;
+ *   - open replies are written into mapped host memory, no copy at all;
  *   - writes go D2H -> (OR-merge for write-once files) -> pwrite;
- *   - staging slots are recycled by CUDA events, never by a blocking flag.
+ *   - staging slots are recycled in issue order as their events complete;
+ *   - every kernel is loaded at session creation: a lazily loaded kernel
+ *     launched while a file-system kernel runs stalls driver calls.
  */
 #include <cuda.h>
 #include <cuda_runtime.h>
-#include <cudaTypedefs.h>
 
 #include <errno.h>
 #include <fcntl.h>
@@ -47,6 +51,11 @@ extern __device__ gfs_state* g_gfs;
 
 namespace {
 
+struct Pending { /* a read whose H2D copy is in flight */
+    uint32_t* done; /* host pointer of the completion word */
+    uint32_t code;
+};
+
 struct Worker {
     int id = 0;
     cudaStream_t stream = nullptr;
@@ -55,8 +64,11 @@ struct Worker {
     size_t slot_bytes = 0;
     int depth = 0;
     std::vector<cudaEvent_t> ev;
-    std::vector<char> pending;
-    int next = 0;
+    std::vector<Pending> pend; /* per staging slot */
+    std::vector<char> busy;    /* slot has a copy in flight */
+    int next = 0;              /* next slot to use (ring order = completion order) */
+    int oldest = 0;            /* oldest busy slot */
+    int nbusy = 0;
     std::thread th;
 };
 
@@ -66,7 +78,7 @@ __global__ void k_init_frames(gfs_frame* f, uint32_t n) {
         z.st = 0u;
         z.content = 0u;
         z.key = ~0ULL;
-        z.done = 0u;
+        z.pad2 = 0u;
         z.pad0 = 0u;
         z.pad1 = 0ULL;
         f[i] = z;
@@ -125,27 +137,53 @@ struct gfs_ctx {
     char* d_scratch = nullptr; /* small device scratch for names/results of C-ABI calls */
     /* driver entry point, resolved through the runtime so the library does
      * not link libcuda directly (it loads on machines without a driver) */
-    PFN_cuStreamWriteValue32_v11070 write_value = nullptr;
+    uint8_t* hmap = nullptr;   /* mapped block: completion words + open replies (host view) */
+    uint8_t* hmap_d = nullptr; /* same, device view */
+    size_t hmap_bytes = 0;
+    std::atomic<int> logged{0};
     size_t d_scratch_cap = 0;
 };
 
-static uint32_t staging_take(Worker* w) {
-    int k = w->next;
-    w->next = (k + 1) % w->depth;
-    if (w->pending[k]) {
-        cudaEventSynchronize(w->ev[k]);
-        w->pending[k] = 0;
-    }
-    return (uint32_t)k;
+static uint32_t* host_word(gfs_ctx* c, uint64_t dev_addr) {
+    uint64_t base = (uint64_t)(uintptr_t)c->hmap_d;
+    if (dev_addr < base || dev_addr + 4 > base + c->hmap_bytes) return nullptr;
+    return (uint32_t*)(c->hmap + (dev_addr - base));
 }
 
-static void complete(gfs_ctx* c, Worker* w, const gfs_req& r, uint32_t code, int slot_used) {
-    c->write_value((CUstream)w->stream, (CUdeviceptr)r.done_addr, code, CU_STREAM_WRITE_VALUE_DEFAULT);
-    if (slot_used >= 0) {
-        cudaEventRecord(w->ev[slot_used], w->stream);
-        w->pending[slot_used] = 1;
-    }
+static void set_done(gfs_ctx* c, uint32_t* d, uint32_t code) {
+    if (!d) return;
     if (code & GFS_DONE_ERR) c->h_errors++;
+    __atomic_store_n(d, code, __ATOMIC_RELEASE);
+}
+
+static void log_failure(gfs_ctx* c, const gfs_req& r, int err) {
+    if (c->logged.fetch_add(1) < 8)
+        fprintf(stderr, "gpufs_gb300: host op %d failed: %s (fd %d, offset %llu, length %llu)\n", (int)r.op,
+                strerror(err), r.host_fd, (unsigned long long)r.offset, (unsigned long long)r.length);
+}
+
+/* Complete in-flight reads whose copies have landed (in issue order). */
+static void drain(gfs_ctx* c, Worker* w, bool block) {
+    while (w->nbusy) {
+        int k = w->oldest;
+        cudaError_t e = block ? cudaEventSynchronize(w->ev[(size_t)k]) : cudaEventQuery(w->ev[(size_t)k]);
+        if (e == cudaErrorNotReady) return;
+        Pending p = w->pend[(size_t)k];
+        set_done(c, p.done, e == cudaSuccess ? p.code : (GFS_DONE_ERR | (uint32_t)EIO));
+        w->busy[(size_t)k] = 0;
+        w->oldest = (k + 1) % w->depth;
+        w->nbusy--;
+        if (!block) continue;
+        return;
+    }
+}
+
+/* A free staging slot (waits for the oldest copy when all are in flight). */
+static int slot_take(gfs_ctx* c, Worker* w) {
+    while (w->busy[(size_t)w->next]) drain(c, w, true);
+    int k = w->next;
+    w->next = (k + 1) % w->depth;
+    return k;
 }
 
 static int host_open_flags(int oflags) {
@@ -159,6 +197,7 @@ static int host_open_flags(int oflags) {
 
 static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
     c->h_requests++;
+    uint32_t* done = host_word(c, r.done_addr);
     switch (r.op) {
     case GFS_OP_OPEN: {
         char name[GFS_NAME_MAX + 1];
@@ -170,56 +209,82 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         rep.host_fd = fd;
         rep.err = err;
         if (fd >= 0) {
-            struct stat s;
-            if (fstat(fd, &s) == 0) {
-                rep.size = (uint64_t)s.st_size;
-                rep.ctime_ns = (int64_t)s.st_ctim.tv_sec * 1000000000LL + s.st_ctim.tv_nsec;
+            struct stat st;
+            if (fstat(fd, &st) == 0) {
+                rep.size = (uint64_t)st.st_size;
+                rep.ctime_ns = (int64_t)st.st_ctim.tv_sec * 1000000000LL + st.st_ctim.tv_nsec;
             }
         }
-        uint32_t k = staging_take(w);
-        memcpy(w->staging + (size_t)k * w->slot_bytes, &rep, sizeof rep);
-        cudaMemcpyAsync((void*)(uintptr_t)r.dev_addr, w->staging + (size_t)k * w->slot_bytes, sizeof rep,
-                        cudaMemcpyHostToDevice, w->stream);
+        if (r.file < c->hs.n_files) {
+            gfs_open_reply* dst = (gfs_open_reply*)(c->hmap + (size_t)(c->hs.n_frames + c->hs.n_files) * 4 +
+                                                    (size_t)r.file * sizeof(gfs_open_reply));
+            *dst = rep;
+        }
         c->h_opens++;
-        complete(c, w, r, fd >= 0 ? 1u : (GFS_DONE_ERR | (uint32_t)err), (int)k);
+        if (fd < 0 && err != ENOENT) log_failure(c, r, err);
+        set_done(c, done, fd >= 0 ? 1u : (GFS_DONE_ERR | (uint32_t)err));
         break;
     }
     case GFS_OP_CLOSE: {
         int rc = r.host_fd >= 0 ? close(r.host_fd) : 0;
-        complete(c, w, r, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno), -1);
+        set_done(c, done, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno));
         break;
     }
     case GFS_OP_READ: {
         if (c->inject_count.load() > 0 && c->inject_count.fetch_sub(1) > 0) {
-            complete(c, w, r, GFS_DONE_ERR | (uint32_t)c->inject_err, -1);
+            set_done(c, done, GFS_DONE_ERR | (uint32_t)c->inject_err);
             break;
         }
         size_t len = (size_t)r.length;
         if (len > w->slot_bytes) len = w->slot_bytes;
-        uint32_t k = staging_take(w);
+        int k = slot_take(c, w);
         uint8_t* buf = w->staging + (size_t)k * w->slot_bytes;
         ssize_t n = pread_full(r.host_fd, buf, len, (off_t)r.offset);
         if (n < 0) {
-            complete(c, w, r, GFS_DONE_ERR | (uint32_t)errno, -1);
+            int e = errno;
+            log_failure(c, r, e);
+            set_done(c, done, GFS_DONE_ERR | (uint32_t)e);
             break;
         }
         size_t cp = ((size_t)n + 4095u) & ~(size_t)4095u;
         if (cp > w->slot_bytes) cp = w->slot_bytes;
         if (cp > (size_t)n) memset(buf + n, 0, cp - (size_t)n);
-        if (cp) cudaMemcpyAsync((void*)(uintptr_t)r.dev_addr, buf, cp, cudaMemcpyHostToDevice, w->stream);
         c->h_reads++;
         c->h_read_bytes += (unsigned long long)n;
-        complete(c, w, r, 1u + (uint32_t)n, (int)k);
+        if (!cp) {
+            set_done(c, done, 1u);
+            break;
+        }
+        /* copy-engine copy straight into the page frame; the completion
+         * word is written by this thread once the copy's event has fired */
+        cudaError_t e = cudaMemcpyAsync((void*)(uintptr_t)r.dev_addr, buf, cp, cudaMemcpyHostToDevice, w->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(w->ev[(size_t)k], w->stream);
+        if (e != cudaSuccess) {
+            log_failure(c, r, EIO);
+            set_done(c, done, GFS_DONE_ERR | (uint32_t)EIO);
+            break;
+        }
+        w->pend[(size_t)k] = Pending{done, 1u + (uint32_t)n};
+        w->busy[(size_t)k] = 1;
+        w->nbusy++;
+        drain(c, w, false);
         break;
     }
     case GFS_OP_WRITE: {
         size_t len = (size_t)r.length;
         if (len > w->slot_bytes) len = w->slot_bytes;
-        uint32_t k = staging_take(w);
+        int k = slot_take(c, w);
         uint8_t* buf = w->staging + (size_t)k * w->slot_bytes;
-        cudaMemcpyAsync(buf, (const void*)(uintptr_t)r.dev_addr, len, cudaMemcpyDeviceToHost, w->stream);
-        cudaStreamSynchronize(w->stream);
-        w->pending[k] = 0;
+        cudaError_t e = cudaMemcpyAsync(buf, (const void*)(uintptr_t)r.dev_addr, len, cudaMemcpyDeviceToHost,
+                                        w->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(w->ev[(size_t)k], w->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(w->ev[(size_t)k]);
+        drain(c, w, false); /* earlier reads on this stream have landed too */
+        if (e != cudaSuccess) {
+            log_failure(c, r, EIO);
+            set_done(c, done, GFS_DONE_ERR | (uint32_t)EIO);
+            break;
+        }
         if (r.rflags & GFS_RF_DIFF) {
             /* write-once pages were never read: OR them into what is there
              * (diff_and_merge, host_loop.h:76-137) */
@@ -227,15 +292,16 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
             for (ssize_t i = 0; i < m; i++) buf[i] |= w->merge[i];
         }
         ssize_t put = pwrite_full(r.host_fd, buf, len, (off_t)r.offset);
+        int err = put < 0 ? errno : EIO;
         c->h_writes++;
         if (put >= 0) c->h_write_bytes += (unsigned long long)put;
-        complete(c, w, r, put == (ssize_t)len ? 1u + (uint32_t)len : (GFS_DONE_ERR | (uint32_t)(put < 0 ? errno : EIO)),
-                 -1);
+        if (put != (ssize_t)len) log_failure(c, r, err);
+        set_done(c, done, put == (ssize_t)len ? 1u + (uint32_t)len : (GFS_DONE_ERR | (uint32_t)err));
         break;
     }
     case GFS_OP_TRUNC: {
         int rc = ftruncate(r.host_fd, (off_t)r.length);
-        complete(c, w, r, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno), -1);
+        set_done(c, done, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno));
         break;
     }
     case GFS_OP_UNLINK: {
@@ -243,11 +309,11 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         memcpy(name, r.name, GFS_NAME_MAX);
         name[GFS_NAME_MAX] = 0;
         int rc = unlink(name);
-        complete(c, w, r, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno), -1);
+        set_done(c, done, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno));
         break;
     }
     default:
-        complete(c, w, r, GFS_DONE_ERR | (uint32_t)EINVAL, -1);
+        set_done(c, done, GFS_DONE_ERR | (uint32_t)EINVAL);
     }
 }
 
@@ -261,9 +327,12 @@ static void worker_main(gfs_ctx* c, Worker* w) {
         unsigned spins = 0;
         while (__atomic_load_n(&slot->seq, __ATOMIC_ACQUIRE) != t + 1u) {
             if (c->stop.load(std::memory_order_relaxed)) return;
-            ++spins;
+            if ((++spins & 63u) == 0) drain(c, w, false);
             if (spins < 4096u) continue;
-            if (spins < 8192u) { sched_yield(); continue; }
+            if (spins < 8192u) {
+                sched_yield();
+                continue;
+            }
             struct timespec ts = {0, 20000};
             nanosleep(&ts, nullptr);
         }
@@ -291,6 +360,8 @@ static void worker_main(gfs_ctx* c, Worker* w) {
     } while (0)
 
 static gfs_ctx* g_current = nullptr; /* session g_gfs points at */
+
+void gfs__preload_runtime();
 
 /* drop clean, unpinned, valid frames: first their index ways, then the frames */
 __global__ void k_drop_ways(gfs_state* S) {
@@ -370,16 +441,10 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
         CK(cudaSetDevice(cfg.device));
         cudaSetDeviceFlags(cudaDeviceMapHost);
         cudaGetLastError();
-        {
-            void* fn = nullptr;
-            cudaDriverEntryPointQueryResult q;
-            CK(cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &fn, 12000, cudaEnableDefault, &q));
-            if (!fn || q != cudaDriverEntryPointSuccess) {
-                rc = -GFS_EINVAL;
-                goto fail;
-            }
-            c->write_value = (PFN_cuStreamWriteValue32_v11070)fn;
-        }
+        /* load every kernel of the library now: a lazily loaded kernel
+         * launched while a file-system kernel waits on the host would stall
+         * the driver calls the host workers make */
+        gfs__preload_kernels();
         CK(cudaMalloc(&s.pool, nf * page));
         CK(cudaMalloc(&s.frames, nf * sizeof(gfs_frame)));
         CK(cudaMalloc(&s.index, (size_t)s.n_buckets * GFS_WAYS * sizeof(uint32_t)));
@@ -397,6 +462,12 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
         memset(c->ring_h, 0, (size_t)cfg.ring_slots * sizeof(gfs_req));
         for (uint32_t i = 0; i < cfg.ring_slots; i++) c->ring_h[i].seq = i;
         CK(cudaHostGetDevicePointer((void**)&s.ring, c->ring_h, 0));
+        c->hmap_bytes = (size_t)(nf + s.n_files) * 4 + (size_t)s.n_files * sizeof(gfs_open_reply);
+        CK(cudaHostAlloc((void**)&c->hmap, c->hmap_bytes, cudaHostAllocMapped | cudaHostAllocPortable));
+        memset(c->hmap, 0, c->hmap_bytes);
+        CK(cudaHostGetDevicePointer((void**)&c->hmap_d, c->hmap, 0));
+        s.hdone = (uint32_t*)c->hmap_d;
+        s.hreply = (gfs_open_reply*)(c->hmap_d + (size_t)(nf + s.n_files) * 4);
         CK(cudaMalloc(&c->ds, sizeof(gfs_state)));
         CK(cudaMemcpy(c->ds, &s, sizeof(gfs_state), cudaMemcpyHostToDevice));
         CK(cudaMemcpyToSymbol(g_gfs, &c->ds, sizeof(gfs_state*)));
@@ -415,7 +486,8 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
             CK(cudaHostAlloc((void**)&w->staging, (size_t)w->depth * w->slot_bytes, cudaHostAllocPortable));
             w->merge = (uint8_t*)malloc(w->slot_bytes);
             w->ev.resize((size_t)w->depth);
-            w->pending.assign((size_t)w->depth, 0);
+            w->pend.resize((size_t)w->depth);
+            w->busy.assign((size_t)w->depth, 0);
             for (int k = 0; k < w->depth; k++) CK(cudaEventCreateWithFlags(&w->ev[(size_t)k], cudaEventDisableTiming));
         }
         for (Worker* w : c->workers) w->th = std::thread(worker_main, c, w);
@@ -458,6 +530,7 @@ int gfs_destroy(gfs_ctx* c) {
     cudaFree(c->ds);
     cudaFree(c->d_scratch);
     if (c->ring_h) cudaFreeHost(c->ring_h);
+    if (c->hmap) cudaFreeHost(c->hmap);
     if (c->kstream) cudaStreamDestroy(c->kstream);
     delete c;
     return 0;
@@ -540,6 +613,19 @@ void* gfs__scratch(gfs_ctx* c, size_t bytes) {
 }
 
 const gfs_state* gfs__host_state(gfs_ctx* c) { return &c->hs; }
+
+void gfs__preload_runtime() {
+    cudaFuncAttributes a;
+    cudaFuncGetAttributes(&a, k_init_frames);
+    cudaFuncGetAttributes(&a, k_drop_ways);
+    cudaFuncGetAttributes(&a, k_drop_frames);
+}
+
+void gfs__preload_kernels() {
+    gfs__preload_runtime();
+    gfs__preload_workloads();
+    gfs__preload_grep();
+}
 
 /* Empty the buffer cache (clean, unpinned pages); returns frames kept. */
 long long gfs_drop_cache(gfs_ctx* c) {

@@ -10,6 +10,10 @@ extern "C" {
 #endif
 void* gfs__scratch(gfs_ctx* c, size_t bytes);
 int gfs__activate(gfs_ctx* c);
+void gfs__preload_kernels(void);
+void gfs__preload_runtime(void);
+void gfs__preload_workloads(void);
+void gfs__preload_grep(void);
 const gfs_state* gfs__host_state(gfs_ctx* c);
 double _timestamp(void);
 #ifdef __cplusplus

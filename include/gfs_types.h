@@ -97,12 +97,12 @@ typedef struct gfs_frame {
     uint32_t st;      /* pins | REF | DIRTY | state<<24 */
     uint32_t content; /* valid bytes in the frame */
     uint64_t key;     /* file:20 << 44 | gen:12 << 32 | page index:32 */
-    uint32_t done;    /* completion word for this frame's data requests */
+    uint32_t pad2;
     uint32_t pad0;
     uint64_t pad1;
 } gfs_frame;
 
-/* host reply to an OPEN, copied into gfs_file.host_fd.. by the stream */
+/* host reply to an OPEN, written into mapped host memory per file slot */
 typedef struct gfs_open_reply {
     int32_t host_fd;
     int32_t err;
@@ -114,7 +114,7 @@ typedef struct gfs_file {
     uint32_t st;      /* status:4 | incarnation:8 | open count:20 */
     uint32_t gen;     /* page-key generation (12 bits used) */
     int32_t flags;    /* O_G* flags of the current open */
-    uint32_t done;    /* completion word for this slot's control requests */
+    uint32_t pad3;
     /* -- written by the host reply (gfs_open_reply layout) -- */
     int32_t host_fd;
     int32_t err;
@@ -138,7 +138,7 @@ typedef struct gfs_req {
     uint64_t offset;
     uint64_t length;
     uint64_t dev_addr;  /* data frame, or reply destination */
-    uint64_t done_addr; /* device address of the completion word */
+    uint64_t done_addr; /* completion word (mapped host memory, device address) */
     int32_t oflags;
     uint32_t pad[5];
     char name[GFS_NAME_MAX];
@@ -179,6 +179,8 @@ typedef struct gfs_state {
     uint32_t* dirty_bits; /* one bit per frame */
     /* mapped pinned host memory (device view) */
     gfs_req* ring;
+    uint32_t* hdone;          /* completion words: [0, n_frames) frames, then files */
+    gfs_open_reply* hreply;   /* open replies, one per file slot */
     /* counters */
     uint32_t ring_tail;
     uint32_t clock_hand;
