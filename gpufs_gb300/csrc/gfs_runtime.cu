@@ -140,6 +140,7 @@ struct gfs_ctx {
     uint8_t* hmap = nullptr;   /* mapped block: completion words + open replies (host view) */
     uint8_t* hmap_d = nullptr; /* same, device view */
     size_t hmap_bytes = 0;
+    size_t reply_off = 0;
     std::atomic<int> logged{0};
     size_t d_scratch_cap = 0;
 };
@@ -166,6 +167,10 @@ static void log_failure(gfs_ctx* c, const gfs_req& r, int err) {
 static void drain(gfs_ctx* c, Worker* w, bool block) {
     while (w->nbusy) {
         int k = w->oldest;
+        if (!w->busy[(size_t)k]) { /* a slot used synchronously (write) */
+            w->oldest = (k + 1) % w->depth;
+            continue;
+        }
         cudaError_t e = block ? cudaEventSynchronize(w->ev[(size_t)k]) : cudaEventQuery(w->ev[(size_t)k]);
         if (e == cudaErrorNotReady) return;
         Pending p = w->pend[(size_t)k];
@@ -216,8 +221,7 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
             }
         }
         if (r.file < c->hs.n_files) {
-            gfs_open_reply* dst = (gfs_open_reply*)(c->hmap + (size_t)(c->hs.n_frames + c->hs.n_files) * 4 +
-                                                    (size_t)r.file * sizeof(gfs_open_reply));
+            gfs_open_reply* dst = (gfs_open_reply*)(c->hmap + c->reply_off + (size_t)r.file * sizeof(gfs_open_reply));
             *dst = rep;
         }
         c->h_opens++;
@@ -462,12 +466,14 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
         memset(c->ring_h, 0, (size_t)cfg.ring_slots * sizeof(gfs_req));
         for (uint32_t i = 0; i < cfg.ring_slots; i++) c->ring_h[i].seq = i;
         CK(cudaHostGetDevicePointer((void**)&s.ring, c->ring_h, 0));
-        c->hmap_bytes = (size_t)(nf + s.n_files) * 4 + (size_t)s.n_files * sizeof(gfs_open_reply);
+        const size_t reply_off = ((size_t)(nf + s.n_files) * 4 + 15) & ~(size_t)15;
+        c->hmap_bytes = reply_off + (size_t)s.n_files * sizeof(gfs_open_reply);
         CK(cudaHostAlloc((void**)&c->hmap, c->hmap_bytes, cudaHostAllocMapped | cudaHostAllocPortable));
         memset(c->hmap, 0, c->hmap_bytes);
         CK(cudaHostGetDevicePointer((void**)&c->hmap_d, c->hmap, 0));
         s.hdone = (uint32_t*)c->hmap_d;
-        s.hreply = (gfs_open_reply*)(c->hmap_d + (size_t)(nf + s.n_files) * 4);
+        s.hreply = (gfs_open_reply*)(c->hmap_d + reply_off);
+        c->reply_off = reply_off;
         CK(cudaMalloc(&c->ds, sizeof(gfs_state)));
         CK(cudaMemcpy(c->ds, &s, sizeof(gfs_state), cudaMemcpyHostToDevice));
         CK(cudaMemcpyToSymbol(g_gfs, &c->ds, sizeof(gfs_state*)));
