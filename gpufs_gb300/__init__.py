@@ -80,6 +80,9 @@ _SIGS = {
     "gfs_grep_text": (_int, [_c_p, _c_s, ctypes.POINTER(_c_s), _int, _c_p, _int]),
     "gfs_grep_bench": (_int, [_c_p, _int, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "gfs_drop_cache": (_i64, [_c_p]),
+    "gfs_bigmatrix": (_int, [_c_p, _c_s, _c_s, _c_s, _int, _int, ctypes.POINTER(ctypes.c_float)]),
+    "gfs_xxh64_files": (_int, [_c_p, ctypes.POINTER(_c_s), _int, ctypes.POINTER(ctypes.c_ulonglong),
+                               ctypes.POINTER(ctypes.c_float)]),
     "gfs_measure_link": (_int, [_u64, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
 }
 
@@ -203,6 +206,21 @@ class Session:
         _check(self.L.gfs_memcopy(self._h, _p(src), _p(dst), nblocks, nthreads, mode, ctypes.byref(ms)),
                "gfs_memcopy")
         return ms.value
+
+    def bigmatrix(self, vec_path, mat_path, out_path, nblocks=152, nthreads=256):
+        """y = A x through gmmap (samples/bigmatrix_mmap); returns kernel ms."""
+        ms = ctypes.c_float(0)
+        _check(self.L.gfs_bigmatrix(self._h, _p(vec_path), _p(mat_path), _p(out_path), nblocks, nthreads,
+                                    ctypes.byref(ms)), "gfs_bigmatrix")
+        return ms.value
+
+    def xxh64_files(self, paths):
+        """XXH64 (seed 0) of each file, read through the buffer cache."""
+        out = (ctypes.c_ulonglong * len(paths))()
+        ms = ctypes.c_float(0)
+        _check(self.L.gfs_xxh64_files(self._h, _paths(paths), len(paths), out, ctypes.byref(ms)),
+               "gfs_xxh64_files")
+        return [int(v) for v in out], ms.value
 
     # -- introspection / fault injection --
     def stats(self):

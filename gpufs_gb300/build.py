@@ -18,11 +18,11 @@ CSRC = os.path.join(HERE, "csrc")
 INC = os.path.join(ROOT, "include")
 OUT = os.path.join(HERE, "_build")
 
-CUDA_SOURCES = ["gfs_calls.cu", "gfs_runtime.cu", "gfs_workloads.cu", "gfs_grep.cu"]
+CUDA_SOURCES = ["gfs_calls.cu", "gfs_runtime.cu", "gfs_workloads.cu", "gfs_grep.cu", "gfs_apps.cu"]
 # Device-API translation units are linked as relocatable code into kernels of
 # any block size (up to 1024 threads): cap them at 64 registers per thread.
 PER_FILE_FLAGS = {"gfs_calls.cu": ["-maxrregcount=64"], "gfs_workloads.cu": ["-maxrregcount=64"],
-                  "gfs_runtime.cu": ["-maxrregcount=64"]}
+                  "gfs_runtime.cu": ["-maxrregcount=64"], "gfs_apps.cu": ["-maxrregcount=64"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-rdc=true", "-std=c++17", "-Xcompiler", "-fPIC",
               "-I" + INC, "-I" + CSRC, "--expt-relaxed-constexpr"]

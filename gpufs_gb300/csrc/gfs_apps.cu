@@ -1,0 +1,440 @@
+/*
+ * Sample workloads over the GPU file system, beside grep_text:
+ *
+ *   bigmatrix_mmap  samples/bigmatrix_mmap/bigmatrix_mmap.cu:66-168 -- y = A x
+ *                   with A (rows x cols FP32, row-major) and x read through
+ *                   gmmap, y written through gmmap of a write-once file;
+ *   xxh64           per-file XXH64 of files read through the buffer cache
+ *                   (the checksum the memcopy/batched/served forms report).
+ *
+ * bigmatrix: each block owns a contiguous run of rows and keeps one matrix
+ * page mapped at a time (the reference's get_row, :45-60, remaps only when
+ * the cursor leaves the page); a row is a block-wide FP32 dot product with
+ * 16-byte loads, reduced in a fixed order (warp shuffles, then one warp over
+ * the partials), so results are deterministic -- the reference adds the
+ * per-thread partials with a shared-memory float atomicAdd (:35), whose
+ * order varies run to run.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+#include <sys/stat.h>
+
+#include <vector>
+
+#include "fs_calls.cu.h"
+#include "gfs_device.cuh"
+#include "gfs_block.cuh"
+#include "gfs_runtime.h"
+
+extern __device__ gfs_state* g_gfs;
+
+namespace {
+
+__device__ unsigned int g_init_lock; /* INIT_LOCK of the reference sample */
+
+/* block-wide sum of one float per thread, fixed order */
+__device__ float block_sum(float v, float* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    float r = 0.f;
+    if (warp == 0) {
+        r = lane < nw ? red[lane] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xFFFFFFFFu, r, o);
+    }
+    __syncthreads();
+    return r; /* valid in warp 0 */
+}
+
+/* partial dot of n floats (a, b 16-byte aligned when n4 path) */
+__device__ float dot_part(const float* a, const float* b, uint32_t n) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    const uint32_t n4 = ((((uintptr_t)a | (uintptr_t)b) & 15u) == 0u) ? n / 4u : 0u;
+    const float4* a4 = (const float4*)a;
+    const float4* b4 = (const float4*)b;
+    for (uint32_t i = threadIdx.x; i < n4; i += blockDim.x) {
+        float4 p = __ldcg(a4 + i), q = __ldg(b4 + i);
+        s0 = fmaf(p.x, q.x, s0);
+        s1 = fmaf(p.y, q.y, s1);
+        s2 = fmaf(p.z, q.z, s2);
+        s3 = fmaf(p.w, q.w, s3);
+    }
+    for (uint32_t i = 4u * n4 + threadIdx.x; i < n; i += blockDim.x) s0 = fmaf(a[i], b[i], s0);
+    return (s0 + s1) + (s2 + s3);
+}
+
+/* y = A x.  vec/mat/out: device file names; x_buf: cols floats of scratch
+ * per block when x does not fit in one page. */
+__global__ void k_bigmatrix(const char* f_v, const char* f_m, const char* f_o, float* x_scratch, long long* res) {
+    __shared__ float red[32];
+    __shared__ int s_fail;
+    const uint32_t page = g_gfs->page_size;
+    int zfd_m = gopen(f_m, O_GRDONLY);
+    int zfd_o = gopen(f_o, O_GWRONCE);
+    int zfd_v = gopen(f_v, O_GRDONLY);
+    if (zfd_m < 0 || zfd_o < 0 || zfd_v < 0) {
+        if (threadIdx.x == 0) res[blockIdx.x] = zfd_m < 0 ? zfd_m : (zfd_o < 0 ? zfd_o : zfd_v);
+        if (zfd_m >= 0) gclose(zfd_m);
+        if (zfd_o >= 0) gclose(zfd_o);
+        if (zfd_v >= 0) gclose(zfd_v);
+        return;
+    }
+    /* the first block truncates the output, the others wait for it
+     * (bigmatrix_mmap.cu:88-97, INIT_LOCK) */
+    if (threadIdx.x == 0) {
+        s_fail = 0;
+        unsigned int prev = atomicCAS(&g_init_lock, 0u, 1u);
+        if (prev == 0u) {
+            single_thread_ftruncate(zfd_o, 0);
+            __threadfence();
+            atomicExch(&g_init_lock, 2u);
+        } else {
+            unsigned long long deadline = gfs_globaltimer() + 30000000000ULL;
+            while (atomicAdd(&g_init_lock, 0u) != 2u) {
+                if (gfs_globaltimer() > deadline) { s_fail = -GFS_ETIMEDOUT; break; }
+                __nanosleep(1000);
+            }
+        }
+    }
+    __syncthreads();
+    const uint64_t size_v = fstat(zfd_v) / 4, size_m = fstat(zfd_m) / 4;
+    const uint64_t cols = size_v, rows = cols ? size_m / cols : 0;
+    long long result = s_fail;
+    const float* x = nullptr;
+    volatile void* xmap = (volatile void*)-1;
+    if (!result && cols) {
+        if (cols * 4 <= page) {
+            xmap = gmmap(NULL, cols * 4, 0, O_GRDONLY, zfd_v, 0);
+            if (xmap == (volatile void*)-1) result = -GFS_EIO;
+            x = (const float*)xmap;
+        } else {
+            float* xs = x_scratch + (size_t)blockIdx.x * cols;
+            long long got = (long long)gread(zfd_v, 0, cols * 4, (uchar*)xs);
+            if (got != (long long)(cols * 4)) result = got < 0 ? got : -GFS_EIO;
+            x = xs;
+        }
+    }
+    const uint64_t per = rows ? (rows + gridDim.x - 1) / gridDim.x : 0;
+    const uint64_t r0 = (uint64_t)blockIdx.x * per, r1 = r0 + per < rows ? r0 + per : rows;
+    volatile uint8_t* mpage = (volatile uint8_t*)-1;
+    uint64_t mbase = ~0ull;
+    volatile uint8_t* opage = (volatile uint8_t*)-1;
+    uint64_t obase = ~0ull;
+    for (uint64_t r = r0; r < r1 && !result; r++) {
+        /* the row may span pages: walk its segments */
+        const uint64_t rbeg = r * cols * 4, rend = rbeg + cols * 4;
+        float acc = 0.f;
+        for (uint64_t pos = rbeg; pos < rend && !result;) {
+            const uint64_t pb = pos / page * page;
+            if (pb != mbase) {
+                if (mpage != (volatile uint8_t*)-1) gmunmap(mpage, 0);
+                uint64_t mlen = size_m * 4 - pb < page ? size_m * 4 - pb : page;
+                mpage = (volatile uint8_t*)gmmap(NULL, mlen, 0, O_GRDONLY, zfd_m, (off_t)pb);
+                if (mpage == (volatile uint8_t*)-1) { result = -GFS_EIO; mbase = ~0ull; break; }
+                mbase = pb;
+            }
+            const uint64_t seg_end = pb + page < rend ? pb + page : rend;
+            acc += dot_part((const float*)(mpage + (pos - pb)), x + (pos - rbeg) / 4, (uint32_t)((seg_end - pos) / 4));
+            pos = seg_end;
+        }
+        if (result) break;
+        float y = block_sum(acc, red);
+        /* output: map the page holding y[r] */
+        const uint64_t oo = r * 4, ob = oo / page * page;
+        if (ob != obase) {
+            if (opage != (volatile uint8_t*)-1) gmunmap(opage, 0);
+            uint64_t olen = rows * 4 - ob < page ? rows * 4 - ob : page;
+            opage = (volatile uint8_t*)gmmap(NULL, olen, 0, O_GWRONCE, zfd_o, (off_t)ob);
+            if (opage == (volatile uint8_t*)-1) { result = -GFS_EIO; obase = ~0ull; break; }
+            obase = ob;
+        }
+        if (threadIdx.x == 0) *(volatile float*)(opage + (oo - ob)) = y;
+        __syncthreads();
+    }
+    if (mpage != (volatile uint8_t*)-1) gmunmap(mpage, 0);
+    if (opage != (volatile uint8_t*)-1) gmunmap(opage, 0);
+    if (xmap != (volatile void*)-1) gmunmap(xmap, 0);
+    int c0 = gclose(zfd_m), c1 = gclose(zfd_v), c2 = gclose(zfd_o);
+    if (threadIdx.x == 0)
+        res[blockIdx.x] = result ? result : (c0 < 0 ? c0 : (c1 < 0 ? c1 : (c2 < 0 ? c2 : (long long)(r1 > r0 ? r1 - r0 : 0))));
+}
+
+/* ---------------- XXH64 (public xxHash specification) ---------------- */
+#define XP1 0x9E3779B185EBCA87ULL
+#define XP2 0xC2B2AE3D27D4EB4FULL
+#define XP3 0x165667B19E3779F9ULL
+#define XP4 0x85EBCA77C2B2AE63ULL
+#define XP5 0x27D4EB2F165667C5ULL
+
+__device__ __forceinline__ uint64_t xrotl(uint64_t x, int r) { return (x << r) | (x >> (64 - r)); }
+__device__ __forceinline__ uint64_t xround(uint64_t acc, uint64_t in) {
+    acc += in * XP2;
+    acc = xrotl(acc, 31);
+    return acc * XP1;
+}
+__device__ __forceinline__ uint64_t xmerge(uint64_t acc, uint64_t v) {
+    acc ^= xround(0, v);
+    return acc * XP1 + XP4;
+}
+
+/* One warp per file: pages are pinned one at a time by lane 0; every 512
+ * bytes are staged in shared memory by the whole warp (16 B per lane) and
+ * lanes 0..3 run the four accumulator lanes of the stripes over them.  The
+ * tail (< 32 bytes) and the final avalanche run on lane 0. */
+__global__ void k_xxh64(const int* fds, const uint64_t* sizes, int n, unsigned long long* out, int* err) {
+    __shared__ __align__(16) uint8_t stage[8][512 + 32];
+    gfs_state* S = g_gfs;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int warps = (int)(blockDim.x >> 5);
+    uint8_t* st = stage[wib & 7];
+    for (int f = (int)(blockIdx.x * warps) + wib; f < n; f += (int)(gridDim.x * warps)) {
+        const uint64_t size = sizes[f];
+        gfsd::PinFile pf = gfsd::pin_file(S, fds[f]);
+        uint64_t v1 = XP1 + XP2, v2 = XP2, v3 = 0, v4 = 0ULL - XP1;
+        const uint64_t body = size >= 32 ? size / 32 * 32 : 0;
+        /* stripes are consumed 512 bytes at a time; a page holds whole 512s */
+        int fr = -1;
+        uint64_t cur_page = ~0ull;
+        int bad = 0;
+        for (uint64_t pos = 0; pos < body && !bad; pos += 512) {
+            uint64_t pg = pos >> S->log_page;
+            if (pg != cur_page) {
+                if (lane == 0) {
+                    if (fr >= 0) gfsd::unpin(S, (uint32_t)fr);
+                    bool fresh;
+                    fr = gfsd::pin_page(S, pf, (uint32_t)pg, GFS_PIN_READ, &fresh);
+                    if (fr >= 0 && fresh) gfsd::publish_valid(S, (uint32_t)fr);
+                }
+                fr = __shfl_sync(0xFFFFFFFFu, fr, 0);
+                if (fr < 0) { bad = fr; break; }
+                cur_page = pg;
+            }
+            const uint64_t chunk = body - pos < 512 ? body - pos : 512;
+            const uint8_t* src = S->pool + ((size_t)fr << S->log_page) + (pos & (S->page_size - 1u));
+            if ((uint64_t)lane * 16 < chunk) *(uint4*)(st + lane * 16) = gfsd::ld_cg4(src + lane * 16);
+            __syncwarp();
+            if (lane < 4) {
+                uint64_t v = lane == 0 ? v1 : lane == 1 ? v2 : lane == 2 ? v3 : v4;
+                for (uint32_t s = 0; s < chunk / 32; s++) v = xround(v, *(const uint64_t*)(st + s * 32 + lane * 8));
+                if (lane == 0) v1 = v; else if (lane == 1) v2 = v; else if (lane == 2) v3 = v; else v4 = v;
+            }
+            __syncwarp();
+        }
+        v1 = __shfl_sync(0xFFFFFFFFu, v1, 0);
+        v2 = __shfl_sync(0xFFFFFFFFu, v2, 1);
+        v3 = __shfl_sync(0xFFFFFFFFu, v3, 2);
+        v4 = __shfl_sync(0xFFFFFFFFu, v4, 3);
+        if (lane == 0 && !bad) {
+            uint64_t h;
+            if (size >= 32) {
+                h = xrotl(v1, 1) + xrotl(v2, 7) + xrotl(v3, 12) + xrotl(v4, 18);
+                h = xmerge(h, v1);
+                h = xmerge(h, v2);
+                h = xmerge(h, v3);
+                h = xmerge(h, v4);
+            } else {
+                h = XP5;
+            }
+            h += size;
+            /* tail bytes [body, size) */
+            uint8_t tail[32];
+            for (uint64_t q = body; q < size && !bad; q++) {
+                uint64_t pg = q >> S->log_page;
+                if (pg != cur_page) {
+                    if (fr >= 0) gfsd::unpin(S, (uint32_t)fr);
+                    bool fresh;
+                    fr = gfsd::pin_page(S, pf, (uint32_t)pg, GFS_PIN_READ, &fresh);
+                    if (fr >= 0 && fresh) gfsd::publish_valid(S, (uint32_t)fr);
+                    if (fr < 0) { bad = fr; break; }
+                    cur_page = pg;
+                }
+                tail[q - body] = S->pool[((size_t)fr << S->log_page) + (q & (S->page_size - 1u))];
+            }
+            uint32_t tn = (uint32_t)(size - body), i = 0;
+            for (; i + 8 <= tn; i += 8) {
+                uint64_t k = 0;
+                for (int b = 7; b >= 0; b--) k = (k << 8) | tail[i + b];
+                h ^= xround(0, k);
+                h = xrotl(h, 27) * XP1 + XP4;
+            }
+            if (i + 4 <= tn) {
+                uint64_t k = (uint64_t)tail[i] | ((uint64_t)tail[i + 1] << 8) | ((uint64_t)tail[i + 2] << 16) |
+                             ((uint64_t)tail[i + 3] << 24);
+                h ^= k * XP1;
+                h = xrotl(h, 23) * XP2 + XP3;
+                i += 4;
+            }
+            for (; i < tn; i++) {
+                h ^= (uint64_t)tail[i] * XP5;
+                h = xrotl(h, 11) * XP1;
+            }
+            h ^= h >> 33;
+            h *= XP2;
+            h ^= h >> 29;
+            h *= XP3;
+            h ^= h >> 32;
+            out[f] = h;
+        }
+        if (lane == 0 && fr >= 0) gfsd::unpin(S, (uint32_t)fr);
+        bad = __shfl_sync(0xFFFFFFFFu, bad, 0);
+        if (lane == 0 && bad) atomicCAS(err, 0, bad);
+        __syncwarp();
+    }
+}
+
+__global__ void k_open_many(const char* names, int n, int oflags, int* fds, uint64_t* sizes) {
+    int f = blockIdx.x;
+    if (f >= n) return;
+    int fd = gfsd::blk_open(g_gfs, names + (size_t)f * GFS_NAME_MAX, oflags);
+    if (threadIdx.x == 0) {
+        fds[f] = fd;
+        sizes[f] = fd >= 0 ? gfsd::ld_rlx64(&g_gfs->files[fd].size) : 0;
+    }
+}
+
+__global__ void k_close_many(const int* fds, int n, int* rcs) {
+    int f = blockIdx.x;
+    if (f >= n) return;
+    int r = fds[f] >= 0 ? gfsd::blk_close(g_gfs, fds[f]) : 0;
+    if (threadIdx.x == 0) rcs[f] = r;
+}
+
+long long sum_results(long long* d, int n, cudaStream_t s) {
+    long long* h = new long long[(size_t)n];
+    cudaMemcpyAsync(h, d, sizeof(long long) * (size_t)n, cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    long long sum = 0, worst = 0;
+    for (int i = 0; i < n; i++) {
+        if (h[i] < worst) worst = h[i];
+        if (h[i] > 0) sum += h[i];
+    }
+    delete[] h;
+    if (e != cudaSuccess) return -GFS_EIO;
+    return worst < 0 ? worst : sum;
+}
+
+} // namespace
+
+extern "C" {
+
+void gfs__preload_apps() {
+    cudaFuncAttributes a;
+    cudaFuncGetAttributes(&a, k_bigmatrix);
+    cudaFuncGetAttributes(&a, k_xxh64);
+    cudaFuncGetAttributes(&a, k_open_many);
+    cudaFuncGetAttributes(&a, k_close_many);
+}
+
+int gfs_bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
+                  int nthreads, float* kernel_ms) {
+    if (!vec_path || !mat_path || !out_path || nblocks < 1 || nthreads < 32 || nthreads > 1024) return -GFS_EINVAL;
+    if (strlen(vec_path) >= GFS_NAME_MAX || strlen(mat_path) >= GFS_NAME_MAX || strlen(out_path) >= GFS_NAME_MAX)
+        return -GFS_EINVAL;
+    if (gfs__activate(ctx)) return -GFS_EIO;
+    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
+    char names[3 * GFS_NAME_MAX];
+    memset(names, 0, sizeof names);
+    memcpy(names, vec_path, strlen(vec_path));
+    memcpy(names + GFS_NAME_MAX, mat_path, strlen(mat_path));
+    memcpy(names + 2 * GFS_NAME_MAX, out_path, strlen(out_path));
+    char* d = (char*)gfs__scratch(ctx, 256 + sizeof(long long) * (size_t)nblocks);
+    if (!d) return -GFS_ENOMEM;
+    long long* res = (long long*)(d + 256);
+    cudaMemcpyAsync(d, names, sizeof names, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(res, 0, sizeof(long long) * (size_t)nblocks, s);
+    unsigned int zero = 0;
+    cudaMemcpyToSymbolAsync(g_init_lock, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, s);
+    /* x scratch only when x does not fit a page */
+    float* xs = nullptr;
+    long long vbytes = 0;
+    {
+        struct stat st;
+        if (stat(vec_path, &st) == 0) vbytes = (long long)st.st_size;
+    }
+    if ((uint64_t)vbytes > gfs_page_size(ctx) && cudaMalloc(&xs, (size_t)vbytes * (size_t)nblocks) != cudaSuccess)
+        return -GFS_ENOMEM;
+    cudaEvent_t a, b;
+    if (kernel_ms) {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, s);
+    }
+    k_bigmatrix<<<nblocks, nthreads, 0, s>>>(d, d + GFS_NAME_MAX, d + 2 * GFS_NAME_MAX, xs, res);
+    cudaError_t le = cudaGetLastError();
+    if (kernel_ms) {
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(kernel_ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+    long long r = le == cudaSuccess ? sum_results(res, nblocks, s) : -GFS_EINVAL;
+    if (xs) cudaFree(xs);
+    return r < 0 ? (int)r : 0;
+}
+
+/* XXH64 of each file (read through the buffer cache), seed 0. */
+int gfs_xxh64_files(gfs_ctx* ctx, const char* const* paths, int n, unsigned long long* host_out, float* kernel_ms) {
+    if (n < 1) return -GFS_EINVAL;
+    for (int i = 0; i < n; i++)
+        if (!paths[i] || strlen(paths[i]) >= GFS_NAME_MAX) return -GFS_EINVAL;
+    if (gfs__activate(ctx)) return -GFS_EIO;
+    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
+    size_t nb = (size_t)n * GFS_NAME_MAX;
+    char* names = nullptr;
+    int* fds = nullptr;
+    uint64_t* sizes = nullptr;
+    unsigned long long* out = nullptr;
+    int* err = nullptr;
+    char* blk = nullptr;
+    size_t total = nb + (size_t)n * (4 + 8 + 8 + 4) + 256;
+    if (cudaMalloc(&blk, total) != cudaSuccess) return -GFS_ENOMEM;
+    names = blk;
+    sizes = (uint64_t*)(blk + ((nb + 15) & ~(size_t)15));
+    out = (unsigned long long*)(sizes + n);
+    fds = (int*)(out + n);
+    err = fds + n;
+    int* rcs = err + 1;
+    char* hn = new char[nb];
+    memset(hn, 0, nb);
+    for (int i = 0; i < n; i++) memcpy(hn + (size_t)i * GFS_NAME_MAX, paths[i], strlen(paths[i]));
+    cudaMemcpyAsync(names, hn, nb, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(err, 0, 4, s);
+    k_open_many<<<n, 64, 0, s>>>(names, n, O_GRDONLY, fds, sizes);
+    cudaEvent_t a, b;
+    if (kernel_ms) {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, s);
+    }
+    int warps = 8;
+    int grid = (n + warps - 1) / warps;
+    k_xxh64<<<grid, warps * 32, 0, s>>>(fds, sizes, n, out, err);
+    if (kernel_ms) {
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(kernel_ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+    k_close_many<<<n, 64, 0, s>>>(fds, n, rcs);
+    int herr = 0;
+    cudaMemcpyAsync(host_out, out, sizeof(unsigned long long) * (size_t)n, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s);
+    std::vector<int> hfds((size_t)n);
+    cudaMemcpyAsync(hfds.data(), fds, 4 * (size_t)n, cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    delete[] hn;
+    cudaFree(blk);
+    if (e != cudaSuccess) return -GFS_EIO;
+    for (int i = 0; i < n; i++)
+        if (hfds[(size_t)i] < 0) return hfds[(size_t)i];
+    return herr;
+}
+
+} /* extern "C" */

@@ -631,6 +631,7 @@ void gfs__preload_kernels() {
     gfs__preload_runtime();
     gfs__preload_workloads();
     gfs__preload_grep();
+    gfs__preload_apps();
 }
 
 /* Empty the buffer cache (clean, unpinned pages); returns frames kept. */

@@ -116,6 +116,16 @@ long long gfs_pwrite_fsync(gfs_ctx* ctx, const char* path, uint64_t off, uint64_
 int gfs_memcopy(gfs_ctx* ctx, const char* src, const char* dst, int nblocks, int nthreads, int mode,
                 float* kernel_ms);
 
+/* bigmatrix_mmap sample (samples/bigmatrix_mmap/bigmatrix_mmap.cu:66-168):
+ * y = A x, A read through gmmap page windows (rows x cols FP32 row-major,
+ * cols = size(vec)/4), x mapped once (read with gread when larger than a
+ * page), y written through gmmap of out_path (write-once, truncated first).
+ * FP32 accumulation, deterministic reduction order. */
+int gfs_bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
+                  int nthreads, float* kernel_ms);
+/* XXH64 (seed 0) of each file, read through the buffer cache; one warp per file */
+int gfs_xxh64_files(gfs_ctx* ctx, const char* const* paths, int n, unsigned long long* host_out, float* kernel_ms);
+
 /* ---- grep_text (samples/grep_text/grep_text_gpu.cu:193-387) ----
  * Whole-word occurrence counts of every record of a dictionary file (32-byte
  * NUL-padded records, the reference's dict.gpu format) in every corpus file,

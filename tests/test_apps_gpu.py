@@ -1,0 +1,60 @@
+"""bigmatrix_mmap and per-file XXH64 through the GPU file system, against
+the oracle (FP64 host GEMV; XXH64 from the public specification)."""
+import os
+
+import numpy as np
+import pytest
+
+import gpufs_gb300 as g
+from gpufs_gb300 import datagen
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("rows,cols,log_page", [(512, 4096, 16), (300, 65536, 21), (97, 1000, 12), (64, 70000, 16)])
+def test_bigmatrix_matches_fp64(built, shm_dir, rows, cols, log_page):
+    vp, mp, op = (os.path.join(shm_dir, n) for n in ("v.f32", "m.f32", "o.f32"))
+    datagen.normal_f32(vp, cols, seed=3)
+    datagen.normal_f32(mp, rows * cols, seed=4)
+    with open(op, "wb") as f:
+        f.write(b"\xff" * 1000)  # stale bytes: the sample truncates its output first
+    with g.Session(log_page=log_page, pool_bytes=256 << 20, timeout_s=20) as s:
+        s.bigmatrix(vp, mp, op, nblocks=37, nthreads=256)
+        assert s.last_error() == 0, s.error_report()
+    A = np.fromfile(mp, dtype=np.float32).reshape(rows, cols)
+    x = np.fromfile(vp, dtype=np.float32)
+    y = np.fromfile(op, dtype=np.float32)
+    assert y.size == rows
+    y64, ay = oracle.gemv_f64(A, x)
+    # norm-wise and per-element (relative to sum |a_ij x_j|) within 1e-5
+    assert np.linalg.norm(y - y64) / np.linalg.norm(y64) <= 1e-5
+    assert np.all(np.abs(y - y64) <= 1e-5 * ay)
+
+
+def test_bigmatrix_deterministic(built, shm_dir):
+    vp, mp = os.path.join(shm_dir, "v.f32"), os.path.join(shm_dir, "m.f32")
+    datagen.normal_f32(vp, 8192, seed=5)
+    datagen.normal_f32(mp, 256 * 8192, seed=6)
+    outs = []
+    with g.Session(log_page=16, pool_bytes=64 << 20, timeout_s=20) as s:
+        for i in range(2):
+            op = os.path.join(shm_dir, "o%d.f32" % i)
+            s.bigmatrix(vp, mp, op, nblocks=19, nthreads=128)
+            outs.append(open(op, "rb").read())
+    assert outs[0] == outs[1]
+
+
+def test_xxh64_files(built, shm_dir):
+    sizes = [0, 1, 7, 31, 32, 33, 100, 4095, 4096, 65537, 1 << 20, 3 * (1 << 20) + 17]
+    paths = []
+    for i, n in enumerate(sizes):
+        p = os.path.join(shm_dir, "x%02d.bin" % i)
+        datagen.uniform_bytes(p, n, seed=40 + i)
+        paths.append(p)
+    for lp in (12, 16):
+        with g.Session(log_page=lp, pool_bytes=64 << 20, timeout_s=20) as s:
+            got, _ = s.xxh64_files(paths)
+            want = oracle.xxh64_many([np.fromfile(p, dtype=np.uint8) for p in paths])
+            assert got == want
+            assert s.last_error() == 0
