@@ -306,8 +306,8 @@ __global__ void k_close_many(const int* fds, int n, int* rcs) {
 
 long long sum_results(long long* d, int n, cudaStream_t s) {
     long long* h = new long long[(size_t)n];
-    cudaMemcpyAsync(h, d, sizeof(long long) * (size_t)n, cudaMemcpyDeviceToHost, s);
-    cudaError_t e = cudaStreamSynchronize(s);
+    cudaError_t e = cudaStreamSynchronize(s); /* kernel first, then copy back */
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(long long) * (size_t)n, cudaMemcpyDeviceToHost);
     long long sum = 0, worst = 0;
     for (int i = 0; i < n; i++) {
         if (h[i] < worst) worst = h[i];
@@ -424,11 +424,11 @@ int gfs_xxh64_files(gfs_ctx* ctx, const char* const* paths, int n, unsigned long
     }
     k_close_many<<<n, 64, 0, s>>>(fds, n, rcs);
     int herr = 0;
-    cudaMemcpyAsync(host_out, out, sizeof(unsigned long long) * (size_t)n, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s);
     std::vector<int> hfds((size_t)n);
-    cudaMemcpyAsync(hfds.data(), fds, 4 * (size_t)n, cudaMemcpyDeviceToHost, s);
-    cudaError_t e = cudaStreamSynchronize(s);
+    cudaError_t e = cudaStreamSynchronize(s); /* kernels first, then copies back */
+    if (e == cudaSuccess) e = cudaMemcpy(host_out, out, sizeof(unsigned long long) * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(hfds.data(), fds, 4 * (size_t)n, cudaMemcpyDeviceToHost);
     delete[] hn;
     cudaFree(blk);
     if (e != cudaSuccess) return -GFS_EIO;

@@ -936,10 +936,11 @@ int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* s
 int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts) {
     if (!g) return -GFS_EINVAL;
     cudaStream_t s = (cudaStream_t)gfs_kernel_stream(g->ctx);
-    if (cudaMemcpyAsync(host_counts, g->dev.counts, (size_t)g->n_words * g->n_files * 4, cudaMemcpyDeviceToHost, s) !=
-        cudaSuccess)
-        return -GFS_EIO;
-    return cudaStreamSynchronize(s) == cudaSuccess ? 0 : -GFS_EIO;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -GFS_EIO;
+    return cudaMemcpy(host_counts, g->dev.counts, (size_t)g->n_words * g->n_files * 4, cudaMemcpyDeviceToHost) ==
+                   cudaSuccess
+               ? 0
+               : -GFS_EIO;
 }
 
 int gfs_grep_info(gfs_grep* g, long long* out, int n) {

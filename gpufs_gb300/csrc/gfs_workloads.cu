@@ -51,8 +51,10 @@ int stage(gfs_ctx* c, const char* n1, const char* n2, int nblocks, Names* out) {
 long long collect(gfs_ctx* c, const Names& n, int nblocks) {
     cudaStream_t st = (cudaStream_t)gfs_kernel_stream(c);
     long long* h = new long long[(size_t)nblocks];
-    cudaError_t e = cudaMemcpyAsync(h, n.results, sizeof(long long) * (size_t)nblocks, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    /* wait for the kernel before any copy back: a host copy queued behind a
+     * file-system kernel would hold up the workers' own copies it waits on */
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaMemcpy(h, n.results, sizeof(long long) * (size_t)nblocks, cudaMemcpyDeviceToHost);
     long long sum = 0, worst = 0;
     for (int i = 0; i < nblocks && e == cudaSuccess; i++) {
         if (h[i] < 0 && h[i] < worst) worst = h[i];
