@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the link-bandwidth measurement")
+    ap.add_argument("--corpus-mb", type=int, default=TOTAL_BYTES >> 20,
+                    help="smaller corpora are for profiling only; the benchmark is 1024")
     return ap.parse_args()
 
 
@@ -120,16 +123,18 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def make_data(d):
+def make_data(d, total=TOTAL_BYTES):
     from gpufs_gb300 import datagen
+    if total != TOTAL_BYTES:
+        d = d + "_%dmb" % (total >> 20)
     stamp = os.path.join(d, "STAMP")
-    want = "%d %d %d %d %d" % (N_FILES, TOTAL_BYTES, N_VOCAB, N_DICT, SEED)
+    want = "%d %d %d %d %d" % (N_FILES, total, N_VOCAB, N_DICT, SEED)
     paths = [os.path.join(d, "c%03d.txt" % i) for i in range(N_FILES)]
     dpath = os.path.join(d, "dict.gpu")
     if os.path.exists(stamp) and open(stamp).read() == want and all(os.path.exists(p) for p in paths):
         return paths, dpath
     os.makedirs(d, exist_ok=True)
-    paths, dpath = datagen.grep_corpus(d, N_FILES, TOTAL_BYTES, n_vocab=N_VOCAB, n_dict=N_DICT, seed=SEED)
+    paths, dpath = datagen.grep_corpus(d, N_FILES, total, n_vocab=N_VOCAB, n_dict=N_DICT, seed=SEED)
     with open(stamp, "w") as f:
         f.write(want)
     return paths, dpath
@@ -210,15 +215,16 @@ def main():
         run_reference(args, rank, ws, td, data_dir)
         return
     import __graft_entry__
+    total_bytes = args.corpus_mb << 20
     if rank == 0:
         __graft_entry__.build()
-        make_data(data_dir)
+        make_data(data_dir, total_bytes)
     barrier(td)
     if rank != 0:
         __graft_entry__.build()
     import numpy as np
     import gpufs_gb300 as g
-    paths, dpath = make_data(data_dir)
+    paths, dpath = make_data(data_dir, total_bytes)
     corpus = sum(os.path.getsize(p) for p in paths)
     n_words = os.path.getsize(dpath) // 32
     counts_bytes = n_words * N_FILES * 4
@@ -255,6 +261,8 @@ def main():
     # ---- extras: cache-hit / cold gread, link bandwidth ----
     extra = {}
     try:
+        if args.no_extra:
+            raise RuntimeError("skipped")
         h2d, d2h = g.measure_link(1 << 30, 5)
         extra["link_h2d_gbs"] = h2d
         extra["link_d2h_gbs"] = d2h

@@ -241,8 +241,8 @@ __device__ void unpin_window(const Ctx& C, Shared& sh) {
  * clen: valid bytes, cpos: file offset of the chunk. */
 template <bool SMEM>
 __device__ __forceinline__ void scan_chunk(const Ctx& C, Shared& sh, uint32_t* tbl, const uint8_t* base, uint32_t clen,
-                                           uint64_t cpos, uint64_t fsize, int f, uint16_t* slist, uint16_t* elist,
-                                           uint8_t* wscratch, int parity) {
+                                           uint32_t avail, uint64_t cpos, uint64_t fsize, int f, uint16_t* slist,
+                                           uint16_t* elist, uint8_t* wscratch, int parity) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t seg0 = (uint32_t)warp * GR_SEG;
     const bool last_in_file = cpos + clen >= fsize;
@@ -291,16 +291,17 @@ __device__ __forceinline__ void scan_chunk(const Ctx& C, Shared& sh, uint32_t* t
                 len = (int)elist[ei] - (int)st + 1;
                 in_stage = true;
             } else {
-                /* open at the segment end: scan forward (stage, then file) */
+                /* open at the segment end: scan forward through the staged
+                 * bytes (chunk + look-ahead); past `avail` lies end of file */
                 uint32_t p = st + 1u;
                 bool open = true;
                 while (open && p - st <= 32u) {
-                    uint32_t c = p < clen ? base[p] : gbyte(C, sh, fsize, cpos + p);
-                    if (!is_alpha(c) || (p >= clen && cpos + p >= fsize)) open = false;
+                    uint32_t c = p < avail ? base[p] : (cpos + p >= fsize ? 0u : gbyte(C, sh, fsize, cpos + p));
+                    if (!is_alpha(c)) open = false;
                     else p++;
                 }
                 len = (int)(p - st);
-                in_stage = p <= clen;
+                in_stage = p <= avail; /* always, given 64 bytes of look-ahead */
                 if (open) len = 33;
             }
             if (len > 32) {
@@ -359,7 +360,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
     const uint32_t tbl_bytes = SMEM ? 16u * P.nb : 0u;
     uint32_t* tbl = SMEM ? (uint32_t*)dsm : (uint32_t*)P.table;
     uint8_t* stages = dsm + ((tbl_bytes + 127u) & ~127u);
-    const uint32_t stage_bytes = GR_CH + 64u;
+    const uint32_t stage_bytes = GR_CH + 96u; /* chunk + 64 look-ahead + read slack */
     uint16_t* lists = (uint16_t*)(stages + GR_STAGES * stage_bytes);
     uint8_t* scratch = (uint8_t*)(lists + GR_WARPS * 2 * GR_LIST);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -458,8 +459,10 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
                 const uint32_t g = gi + i;
                 uint8_t* dst = stages + (g % GR_STAGES) * stage_bytes;
                 uint64_t pos = kk * GR_CH;
-                uint32_t len = (uint32_t)(fsize - pos < GR_CH ? fsize - pos : GR_CH);
-                uint32_t clen16 = (len + 15u) & ~15u;
+                /* the chunk plus 64 bytes of look-ahead (tokens that start in the
+                 * chunk end at most 33 bytes past it), rounded to 16 bytes */
+                uint64_t cov = fsize - pos < (uint64_t)GR_CH + 64u ? fsize - pos : (uint64_t)GR_CH + 64u;
+                uint32_t clen16 = ((uint32_t)cov + 15u) & ~15u;
                 mbar_expect_tx(&sh.mbar[g % GR_STAGES], clen16);
                 uint32_t done = 0;
                 while (done < clen16) {
@@ -501,8 +504,9 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
                 const uint64_t kk = k + i;
                 const uint64_t pos = kk * GR_CH;
                 const uint32_t clen = (uint32_t)(fsize - pos < GR_CH ? fsize - pos : GR_CH);
+                const uint32_t avail = (uint32_t)(fsize - pos < (uint64_t)GR_CH + 64u ? fsize - pos : (uint64_t)GR_CH + 64u);
                 const uint8_t* base = stages + (g % GR_STAGES) * stage_bytes;
-                scan_chunk<SMEM>(C, sh, tbl, base, clen, pos, fsize, f, slist, elist, wscratch, parity);
+                scan_chunk<SMEM>(C, sh, tbl, base, clen, avail, pos, fsize, f, slist, elist, wscratch, parity);
                 parity ^= 1;
                 __syncthreads();
             }
@@ -840,7 +844,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     g->sms = sms;
-    size_t fixed = (size_t)GR_STAGES * (GR_CH + 64) + (size_t)GR_WARPS * 2 * GR_LIST * 2 + (size_t)GR_WARPS * 48 + 256;
+    size_t fixed = (size_t)GR_STAGES * (GR_CH + 96) + (size_t)GR_WARPS * 2 * GR_LIST * 2 + (size_t)GR_WARPS * 48 + 256;
     size_t with_tbl = align_up((size_t)nb * 16, 128) + fixed;
     g->smem = with_tbl <= (size_t)maxsm;
     g->smem_bytes = g->smem ? with_tbl : fixed;
