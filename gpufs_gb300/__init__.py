@@ -11,6 +11,10 @@ import os
 
 import numpy as np
 
+# Enough hardware work queues that no host-worker stream shares one with the
+# stream of a running file-system kernel (must be set before CUDA starts).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 _HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(_HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libgpufs_gb300.so")

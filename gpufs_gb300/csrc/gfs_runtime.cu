@@ -365,6 +365,17 @@ static void worker_main(gfs_ctx* c, Worker* w) {
 
 static gfs_ctx* g_current = nullptr; /* session g_gfs points at */
 
+/* CUDA maps streams onto a fixed set of hardware work queues (8 unless
+ * CUDA_DEVICE_MAX_CONNECTIONS says otherwise).  A worker stream that shares
+ * a queue with the stream of a running file-system kernel has its copies
+ * ordered behind that kernel, which is waiting for them.  Ask for 32 queues
+ * before any context exists (the library is loaded before the first CUDA
+ * call in the programs and bindings that use it); host_workers is capped at
+ * GFS_MAX_WORKERS so a session's streams fit. */
+#define GFS_CONNECTIONS "32"
+#define GFS_MAX_WORKERS 24
+__attribute__((constructor)) static void gfs_set_connections() { setenv("CUDA_DEVICE_MAX_CONNECTIONS", GFS_CONNECTIONS, 0); }
+
 void gfs__preload_runtime();
 
 /* drop clean, unpinned, valid frames: first their index ways, then the frames */
@@ -423,7 +434,7 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
     *out = nullptr;
     if (cfg.log_page < 12 || cfg.log_page > 21) { delete c; return -GFS_EINVAL; }
     if (cfg.host_workers < 1) cfg.host_workers = 1;
-    if (cfg.host_workers > 64) cfg.host_workers = 64;
+    if (cfg.host_workers > GFS_MAX_WORKERS) cfg.host_workers = GFS_MAX_WORKERS;
     if (cfg.staging_depth < 2) cfg.staging_depth = 2;
     if (cfg.timeout_ns == 0) cfg.timeout_ns = 30ull * 1000000000ull;
     cfg.ring_slots = next_pow2(cfg.ring_slots < 64 ? 64 : cfg.ring_slots);

@@ -128,3 +128,18 @@ def test_one_shot_grep_text(sess, shm_dir):
     got = g.grep_text(sess, dpath, paths)
     want = oracle.grep_counts(open(dpath, "rb").read(), [open(p, "rb").read() for p in paths])
     assert np.array_equal(got, want)
+
+
+def test_many_sessions_in_one_process(built, shm_dir):
+    """Sessions created one after another in one process (each with its own
+    kernel and worker streams) keep serving cold reads while their kernel
+    occupies every SM."""
+    paths, dpath = datagen.grep_corpus(shm_dir, n_files=4, total_bytes=2 * (1 << 20) + 99, n_vocab=2000,
+                                       n_dict=500, seed=12)
+    want = oracle.grep_counts(open(dpath, "rb").read(), [open(p, "rb").read() for p in paths])
+    for i in range(12):
+        with g.Session(log_page=(12, 14, 16)[i % 3], pool_bytes=64 << 20, host_workers=8 + (i % 3) * 4,
+                       timeout_s=10) as s:
+            with g.Grep(s, dpath, paths) as gr:
+                gr.run(0)
+                assert np.array_equal(gr.counts(), want), i
