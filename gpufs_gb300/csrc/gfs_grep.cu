@@ -51,13 +51,16 @@
 #include "gfs_runtime.h"
 #include "gpufs_gb300.h"
 
-#define GR_CH 16384
-#define GR_STAGES 4
+#define GR_CONS 31                    /* consumer warps; warp 31 is the producer */
 #define GR_THREADS 1024
-#define GR_WARPS 32
-#define GR_SEG 512
-#define GR_LIST 256
-#define GR_WIN 32 /* pages pinned per window, including look-behind/ahead */
+#define GR_SEG 512                    /* bytes per consumer warp per chunk */
+#define GR_CH (GR_CONS * GR_SEG)      /* 15872-byte chunks */
+#define GR_LB 16                      /* look-behind bytes staged before a chunk */
+#define GR_LA 64                      /* look-ahead bytes staged after it */
+#define GR_STAGE (GR_LB + GR_CH + GR_LA + 32)
+#define GR_STAGES 4
+#define GR_LIST 258                   /* a segment holds up to 256 starts and 257 ends */
+#define GR_WIN 32                     /* pages per window, incl. look-behind/ahead */
 
 extern __device__ gfs_state* g_gfs;
 
@@ -66,17 +69,17 @@ struct GrepDev {
     int n_words;
     const int* fds;
     const uint64_t* sizes;
-    const uint64_t* chunk_prefix; /* n_files + 1 */
+    const uint64_t* chunk_prefix; /* n_files + 1, in GR_CH chunks */
     uint64_t total_chunks;
     uint32_t nb;                  /* buckets */
-    const uint32_t* table;        /* nb * 4 slot words: tag << 20 */
+    const uint32_t* table;        /* nb * 4 slot words: tag << 20 | long << 19 */
     const uint4* recs;            /* nb * 4 records of 32 bytes */
     const uint32_t* slot_word;    /* first record of each slot, ~0 if empty */
     const int32_t* next_dup;      /* next record with the same word, -1 */
     uint32_t* counts;             /* n_words x n_files */
     uint32_t* long_flags;         /* per file: a run of >= 33 letters was seen */
     uint32_t* status;             /* [0] error bits, [1] first failure: site << 16 | errno */
-    uint32_t win_data;            /* data pages per window (window = data + look-behind/ahead) */
+    uint32_t win_pages;           /* pages per window (two windows per CTA may be pinned) */
 };
 
 namespace {
@@ -91,6 +94,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -104,6 +110,7 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;" ::"r"(GR_CONS * 32) : "memory"); }
 
 /* ---------------- byte classification ---------------- */
 /* bit 7 of each byte of the result is set iff the byte is [A-Za-z_] */
@@ -120,51 +127,39 @@ __device__ __forceinline__ uint32_t nib4(uint32_t a) { return (a * 0x00204081u) 
 __device__ __forceinline__ uint32_t alpha16(uint4 v) {
     return nib4(alpha4(v.x)) | (nib4(alpha4(v.y)) << 4) | (nib4(alpha4(v.z)) << 8) | (nib4(alpha4(v.w)) << 12);
 }
-__device__ __forceinline__ bool is_alpha(uint32_t c) {
-    return (c - 65u < 26u) || (c - 97u < 26u) || c == 95u;
+__device__ __forceinline__ uint32_t is_alpha(uint32_t c) {
+    return ((c - 65u < 26u) || (c - 97u < 26u) || c == 95u) ? 1u : 0u;
 }
 
-/* zero-padded key words of `len` (1..32) bytes starting at byte `st` of an
- * smem buffer that is readable 4 bytes past st+len */
-__device__ __forceinline__ void key_from_smem(const uint8_t* base, uint32_t st, int len, uint32_t k[8]) {
+/* key of a token of len <= 16 at byte st of an 8-byte aligned smem buffer
+ * readable 24 bytes past (st & ~7): three 8-byte loads, funnel shifts, and
+ * a clamp mask per word (no branches) */
+__device__ __forceinline__ void key16(const uint8_t* base, uint32_t st, uint32_t len, uint32_t k[4]) {
+    const uint32_t o = st & 7u;
+    const uint2* q = (const uint2*)(base + (st - o));
+    const uint2 q0 = q[0], q1 = q[1], q2 = q[2];
+    const bool hi = o >= 4u;
+    const uint32_t y0 = hi ? q0.y : q0.x, y1 = hi ? q1.x : q0.y, y2 = hi ? q1.y : q1.x, y3 = hi ? q2.x : q1.y,
+                   y4 = hi ? q2.y : q2.x;
+    const uint32_t sh = (o & 3u) * 8u;
+    const int kb = (int)len * 8;
+    k[0] = __funnelshift_r(y0, y1, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb, 0));
+    k[1] = __funnelshift_r(y1, y2, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 32, 0));
+    k[2] = __funnelshift_r(y2, y3, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 64, 0));
+    k[3] = __funnelshift_r(y3, y4, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 96, 0));
+}
+
+/* key of any len <= 32 (slow path): 9 word loads */
+__device__ __forceinline__ void key32(const uint8_t* base, uint32_t st, uint32_t len, uint32_t k[8]) {
     const uint32_t* w = (const uint32_t*)(base + (st & ~3u));
     const uint32_t sh = (st & 3u) * 8u;
-    const int nw = (int)(((st & 3u) + (uint32_t)len + 3u) >> 2);
     uint32_t x[9];
 #pragma unroll
-    for (int i = 0; i < 9; i++) x[i] = (i < nw) ? w[i] : 0u;
+    for (int i = 0; i < 9; i++) x[i] = w[i];
+    const int kb = (int)len * 8;
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-        uint32_t v = __funnelshift_r(x[i], x[i + 1], sh);
-        int valid = len - 4 * i;
-        uint32_t m = valid >= 4 ? 0xFFFFFFFFu : (valid <= 0 ? 0u : ((1u << (8 * valid)) - 1u));
-        k[i] = v & m;
-    }
-}
-
-struct Ctx {
-    gfs_state* S;
-    GrepDev P;
-    uint32_t lp, pmask;
-};
-
-/* shared state of a CTA */
-struct Shared {
-    uint64_t mbar[GR_STAGES];
-    int win_frames[GR_WIN];
-    uint32_t win_lb;      /* first pinned page */
-    int win_n;            /* pinned pages */
-    int err;
-    uint32_t prev_alpha[2];
-};
-
-__device__ __forceinline__ uint32_t gbyte(const Ctx& C, const Shared& sh, uint64_t fsize, uint64_t q) {
-    if (q >= fsize) return 0u;
-    uint32_t pg = (uint32_t)(q >> C.lp);
-    int i = (int)(pg - sh.win_lb);
-    if (i < 0 || i >= sh.win_n) return 0u; /* not pinned: cannot happen within 33 bytes of a window */
-    const uint8_t* p = C.S->pool + ((size_t)sh.win_frames[i] << C.lp) + (q & C.pmask);
-    return (uint32_t)__ldcg(p);
+    for (int i = 0; i < 8; i++)
+        k[i] = __funnelshift_r(x[i], x[i + 1], sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 32 * i, 0));
 }
 
 __device__ __forceinline__ void flush_slot(const GrepDev& P, uint32_t slot, uint32_t n, int f) {
@@ -176,351 +171,453 @@ __device__ __forceinline__ void flush_slot(const GrepDev& P, uint32_t slot, uint
     }
 }
 
-/* Look a key up; on a verified match count it (smem counter or global). */
-template <bool SMEM>
-__device__ __forceinline__ void count_key(const GrepDev& P, uint32_t* tbl, const uint32_t k[8], int len, int f) {
-    uint64_t h = grep_hash(k, len);
-    uint32_t tag = grep_tag(h);
-    uint32_t bs[2] = {grep_b1(h, P.nb), grep_b2(h, P.nb)};
-#pragma unroll
-    for (int r = 0; r < 2; r++) {
-        uint4 q = SMEM ? *(const uint4*)(tbl + 4u * bs[r]) : __ldg((const uint4*)(P.table + 4u * bs[r]));
-        uint32_t s4[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
+/* Candidate slot of a key in the two buckets (first tag match), or ~0. */
+__device__ __forceinline__ uint32_t first_candidate(const uint32_t* tbl, uint32_t b1, uint32_t b2, uint32_t tag,
+                                                    uint32_t* word, bool global) {
+    const uint4 q1 = global ? __ldg((const uint4*)tbl + b1) : ((const uint4*)tbl)[b1];
+    const uint4 q2 = global ? __ldg((const uint4*)tbl + b2) : ((const uint4*)tbl)[b2];
+    const uint32_t tb = tag << GREP_TAG_SHIFT;
+    uint32_t slot = 0xFFFFFFFFu, w = 0;
+#define GR_PICK(val, s)                                                                                \
+    if ((((val) ^ tb) >> GREP_TAG_SHIFT) == 0u && slot == 0xFFFFFFFFu) { slot = (s); w = (val); }
+    GR_PICK(q1.x, 4u * b1) GR_PICK(q1.y, 4u * b1 + 1u) GR_PICK(q1.z, 4u * b1 + 2u) GR_PICK(q1.w, 4u * b1 + 3u)
+    GR_PICK(q2.x, 4u * b2) GR_PICK(q2.y, 4u * b2 + 1u) GR_PICK(q2.z, 4u * b2 + 2u) GR_PICK(q2.w, 4u * b2 + 3u)
+#undef GR_PICK
+    *word = w;
+    return slot;
+}
+
+__device__ __forceinline__ bool rec_equal(const GrepDev& P, uint32_t slot, uint32_t word, const uint32_t* k, uint32_t len) {
+    const bool rlong = (word & GREP_LONG_BIT) != 0u;
+    if (rlong != (len > 16u)) return false;
+    const uint4 a = __ldg(P.recs + 2u * slot);
+    bool eq = a.x == k[0] && a.y == k[1] && a.z == k[2] && a.w == k[3];
+    if (eq && rlong) {
+        const uint4 b = __ldg(P.recs + 2u * slot + 1u);
+        eq = b.x == k[4] && b.y == k[5] && b.z == k[6] && b.w == k[7];
+    }
+    return eq;
+}
+
+/* Slow, general lookup: every tag match in both buckets is verified. */
+__device__ void lookup_count(const GrepDev& P, uint32_t* tbl, bool smem, const uint32_t k[8], uint32_t len, int f) {
+    const uint32_t h1 = grep_h1(grep_mix(k, (int)len)), h2 = grep_h2(h1);
+    const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h2, b1, P.nb), tag = grep_tag(h1);
+    const uint32_t bs[2] = {b1, b2};
+    for (int r = 0; r < 2; r++)
         for (int i = 0; i < 4; i++) {
-            if ((s4[i] >> GREP_TAG_SHIFT) != tag) continue;
-            uint32_t slot = 4u * bs[r] + (uint32_t)i;
-            uint4 a = __ldg(P.recs + 2u * slot), b = __ldg(P.recs + 2u * slot + 1u);
-            if (a.x == k[0] && a.y == k[1] && a.z == k[2] && a.w == k[3] && b.x == k[4] && b.y == k[5] &&
-                b.z == k[6] && b.w == k[7]) {
-                if (SMEM) {
-                    uint32_t old = atomicAdd(&tbl[slot], 1u);
-                    if ((old & GREP_CNT_MASK) == 0x7FFFFu) { /* keep the 20-bit counter from overflowing */
-                        atomicSub(&tbl[slot], 0x80000u);
-                        flush_slot(P, slot, 0x80000u, f);
-                    }
-                } else {
-                    flush_slot(P, slot, 1u, f);
+            const uint32_t slot = 4u * bs[r] + (uint32_t)i;
+            const uint32_t w = smem ? tbl[slot] : __ldg(P.table + slot);
+            if ((w >> GREP_TAG_SHIFT) != tag) continue;
+            if (!rec_equal(P, slot, w, k, len)) continue;
+            if (smem) {
+                const uint32_t old = atomicAdd(&tbl[slot], 1u);
+                if ((old & GREP_CNT_MASK) == GREP_CNT_FLUSH - 1u) {
+                    atomicSub(&tbl[slot], GREP_CNT_FLUSH);
+                    flush_slot(P, slot, GREP_CNT_FLUSH, f);
                 }
-                return;
+            } else {
+                flush_slot(P, slot, 1u, f);
             }
+            return;
+        }
+}
+
+__device__ __forceinline__ void count_hit(const GrepDev& P, uint32_t* tbl, bool smem, uint32_t slot, int f) {
+    if (smem) {
+        const uint32_t old = atomicAdd(&tbl[slot], 1u);
+        if ((old & GREP_CNT_MASK) == GREP_CNT_FLUSH - 1u) {
+            atomicSub(&tbl[slot], GREP_CNT_FLUSH);
+            flush_slot(P, slot, GREP_CNT_FLUSH, f);
+        }
+    } else {
+        flush_slot(P, slot, 1u, f);
+    }
+}
+
+struct StageDesc {
+    uint64_t pos;   /* file offset of chunk byte 0 */
+    int f;          /* file */
+    uint32_t clen;  /* chunk bytes */
+    uint32_t avail; /* staged bytes from chunk byte 0 (chunk + look-ahead, to end of file) */
+    uint32_t pad;
+};
+
+struct Shared {
+    uint64_t full[GR_STAGES];
+    uint64_t empty[GR_STAGES];
+    StageDesc desc[GR_STAGES];
+    int frames[2][GR_WIN];
+    volatile int abort;
+    int err;
+    uint32_t win;
+};
+
+__device__ __forceinline__ void fail(Shared& sh, const GrepDev& P, int e, uint32_t site) {
+    sh.err = e;
+    sh.abort = 1;
+    atomicOr(P.status, e == -GFS_ETIMEDOUT ? GFS_ERRB_TIMEOUT : GFS_ERRB_IO);
+    atomicCAS(&P.status[1], 0u, (site << 16) | (uint32_t)(e < 0 ? -e : e));
+}
+
+/* Bounded wait on an mbarrier phase by one lane.  false: gave up (abort). */
+__device__ __forceinline__ bool wait_phase(Shared& sh, const GrepDev& P, uint64_t* bar, uint32_t parity, uint32_t site) {
+    uint32_t spins = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if (sh.abort) return false;
+        if (++spins > (1u << 24)) {
+            fail(sh, P, -GFS_ETIMEDOUT, site);
+            return false;
+        }
+        if (spins > 32) __nanosleep(spins > 4096 ? 2048 : 64);
+    }
+    return true;
+}
+
+__device__ __forceinline__ int file_of(const GrepDev& P, uint64_t c) {
+    int lo = 0, hi = P.n_files - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (P.chunk_prefix[mid] <= c) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+/* ---------------- consumer: one 512-byte segment ---------------- */
+template <bool SMEM>
+__device__ __forceinline__ void scan_segment(const GrepDev& P, uint32_t* tbl, const uint8_t* base, const StageDesc& d,
+                                             uint16_t* slist, uint16_t* elist, uint8_t* wscr) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t seg0 = (uint32_t)warp * GR_SEG;
+    const uint32_t clen = d.clen, avail = d.avail;
+    if (seg0 >= clen) return;
+    const uint32_t off = seg0 + 16u * (uint32_t)lane;
+    const uint4 v = *(const uint4*)(base + off);
+    uint32_t ax = alpha16(v);
+    ax &= off >= avail ? 0u : (avail - off >= 16u ? 0xFFFFu : ((1u << (avail - off)) - 1u));
+    const uint32_t a = ax & (off >= clen ? 0u : (clen - off >= 16u ? 0xFFFFu : ((1u << (clen - off)) - 1u)));
+    uint32_t pb = __shfl_up_sync(0xFFFFFFFFu, ax >> 15, 1);
+    if (lane == 0) pb = seg0 == 0 ? (d.pos > 0 ? is_alpha(base[-1]) : 0u) : is_alpha(base[seg0 - 1]);
+    uint32_t nx = __shfl_down_sync(0xFFFFFFFFu, ax & 1u, 1);
+    if (lane == 31) nx = seg0 + GR_SEG < avail ? is_alpha(base[seg0 + GR_SEG]) : 0u;
+    const uint32_t starts = a & ~((a << 1) | pb) & 0xFFFFu;
+    const uint32_t ends = a & ~((ax >> 1) | (nx << 15));
+    const uint32_t packed = (uint32_t)__popc(starts) | ((uint32_t)__popc(ends) << 16);
+    uint32_t incl = packed;
+#pragma unroll
+    for (int dd = 1; dd < 32; dd <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, dd);
+        if (lane >= dd) incl += t;
+    }
+    const uint32_t tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    const uint32_t n_s = tot & 0xFFFFu, n_e = tot >> 16;
+    uint32_t js = (incl - packed) & 0xFFFFu, je = (incl - packed) >> 16;
+    for (uint32_t m = starts; m; m &= m - 1u) slist[js++] = (uint16_t)(off + (uint32_t)(__ffs(m) - 1));
+    for (uint32_t m = ends; m; m &= m - 1u) elist[je++] = (uint16_t)(off + (uint32_t)(__ffs(m) - 1));
+    const uint32_t carry = __shfl_sync(0xFFFFFFFFu, a & pb & 1u, 0);
+    /* the last token may run past the segment: find its end in the staged
+     * bytes (chunk + look-ahead); 0xFFFF marks a run of 33+ letters */
+    if (lane == 0 && n_s + carry > n_e) {
+        const uint32_t st = 0; (void)st;
+        uint32_t q = seg0 + GR_SEG < clen ? seg0 + GR_SEG : clen;
+        const uint32_t cap = q + 33u;
+        while (q < avail && q < cap && is_alpha(base[q])) q++;
+        elist[n_e] = q >= cap ? (uint16_t)0xFFFFu : (uint16_t)(q - 1u);
+    }
+    __syncwarp();
+    for (uint32_t tb0 = 0; tb0 < n_s; tb0 += 64u) {
+        /* two tokens per lane: t0 and t1, straight-line so the two record
+         * loads are in flight together */
+        const uint32_t t0 = tb0 + (uint32_t)lane, t1 = t0 + 32u;
+        const bool v0 = t0 < n_s, v1 = t1 < n_s;
+        uint32_t st0 = 0, st1 = 0, len0 = 0, len1 = 0;
+        if (v0) {
+            st0 = slist[t0];
+            const uint32_t e = elist[t0 + carry];
+            len0 = e == 0xFFFFu ? 33u : e - st0 + 1u;
+        }
+        if (v1) {
+            st1 = slist[t1];
+            const uint32_t e = elist[t1 + carry];
+            len1 = e == 0xFFFFu ? 33u : e - st1 + 1u;
+        }
+        const bool f0 = v0 && len0 <= 16u, f1 = v1 && len1 <= 16u;
+        uint32_t k0[4], k1[4];
+        key16(base, f0 ? st0 : 0u, f0 ? len0 : 0u, k0);
+        key16(base, f1 ? st1 : 0u, f1 ? len1 : 0u, k1);
+        uint32_t ka0[8] = {k0[0], k0[1], k0[2], k0[3], 0u, 0u, 0u, 0u};
+        uint32_t ka1[8] = {k1[0], k1[1], k1[2], k1[3], 0u, 0u, 0u, 0u};
+        const uint32_t h10 = grep_h1(grep_mix(ka0, (int)len0)), h11 = grep_h1(grep_mix(ka1, (int)len1));
+        const uint32_t b10 = grep_bucket(h10, P.nb), b11 = grep_bucket(h11, P.nb);
+        const uint32_t b20 = grep_b2(grep_h2(h10), b10, P.nb), b21 = grep_b2(grep_h2(h11), b11, P.nb);
+        uint32_t w0 = 0, w1 = 0;
+        const uint32_t s0 = f0 ? first_candidate(tbl, b10, b20, grep_tag(h10), &w0, !SMEM) : 0xFFFFFFFFu;
+        const uint32_t s1 = f1 ? first_candidate(tbl, b11, b21, grep_tag(h11), &w1, !SMEM) : 0xFFFFFFFFu;
+        uint4 r0 = make_uint4(0, 0, 0, 0), r1 = make_uint4(0, 0, 0, 0);
+        if (s0 != 0xFFFFFFFFu) r0 = __ldg(P.recs + 2u * s0);
+        if (s1 != 0xFFFFFFFFu) r1 = __ldg(P.recs + 2u * s1);
+        const bool m0 = s0 != 0xFFFFFFFFu && !(w0 & GREP_LONG_BIT) && r0.x == k0[0] && r0.y == k0[1] &&
+                        r0.z == k0[2] && r0.w == k0[3];
+        const bool m1 = s1 != 0xFFFFFFFFu && !(w1 & GREP_LONG_BIT) && r1.x == k1[0] && r1.y == k1[1] &&
+                        r1.z == k1[2] && r1.w == k1[3];
+        if (m0) count_hit(P, tbl, SMEM, s0, d.f);
+        if (m1) count_hit(P, tbl, SMEM, s1, d.f);
+        /* rare: a tag match that was not the word (another candidate may be);
+         * tokens of 17..32 letters; runs of 33+ letters */
+        if (f0 && s0 != 0xFFFFFFFFu && !m0) lookup_count(P, tbl, SMEM, ka0, len0, d.f);
+        if (f1 && s1 != 0xFFFFFFFFu && !m1) lookup_count(P, tbl, SMEM, ka1, len1, d.f);
+        if (v0 && len0 > 16u) {
+            if (len0 > 32u) atomicOr(&P.long_flags[d.f], 1u);
+            else {
+                uint32_t kk[8];
+                key32(base, st0, len0, kk);
+                lookup_count(P, tbl, SMEM, kk, len0, d.f);
+            }
+        }
+        if (v1 && len1 > 16u) {
+            if (len1 > 32u) atomicOr(&P.long_flags[d.f], 1u);
+            else {
+                uint32_t kk[8];
+                key32(base, st1, len1, kk);
+                lookup_count(P, tbl, SMEM, kk, len1, d.f);
+            }
+        }
+    }
+    (void)wscr;
+}
+
+template <bool SMEM>
+__device__ void flush_counts(const GrepDev& P, uint32_t* tbl, int f) {
+    if (!SMEM) return;
+    const uint32_t nslots = 4u * P.nb;
+    for (uint32_t i = threadIdx.x; i < nslots; i += GR_CONS * 32) {
+        const uint32_t v = tbl[i];
+        const uint32_t n = v & GREP_CNT_MASK;
+        if (n) {
+            tbl[i] = v & ~GREP_CNT_MASK;
+            flush_slot(P, i, n, f);
         }
     }
 }
 
-/* Pin the window's pages (warp 0; one lane per page).  Returns 0, -GFS_ENOMEM
- * when the pool could not hold the whole window (nothing is left pinned;
- * the caller shrinks the window), or another -err. */
-__device__ int pin_window(const Ctx& C, Shared& sh, int fd, uint64_t fsize, uint32_t lb, int n) {
+/* ---------------- producer: pin windows, stream chunks ---------------- */
+struct Window {
+    uint32_t lb, n;   /* pinned pages [lb, lb + n) */
+    int buf;          /* sh.frames[buf] */
+    uint32_t last_g;  /* last chunk streamed from it */
+    bool live;
+};
+
+__device__ int pin_pages(gfs_state* S, Shared& sh, int buf, int fd, uint32_t lb, uint32_t n, bool soft) {
     const int lane = threadIdx.x & 31;
     int r = 0;
-    if (lane < n) {
-        PinFile pf = pin_file(C.S, fd);
+    if ((uint32_t)lane < n) {
+        PinFile pf = pin_file(S, fd);
         bool fresh;
-        r = pin_page(C.S, pf, lb + (uint32_t)lane, GFS_PIN_READ | (n > 1 ? GFS_PIN_NOALLOC : 0), &fresh);
-        if (r >= 0 && fresh) { /* beyond the host file: cannot happen below fsize */
-            publish_valid(C.S, (uint32_t)r);
-        }
-        sh.win_frames[lane] = r;
+        r = pin_page(S, pf, lb + (uint32_t)lane, GFS_PIN_READ | (soft ? GFS_PIN_NOALLOC : 0), &fresh);
+        if (r >= 0 && fresh) publish_valid(S, (uint32_t)r);
+        sh.frames[buf][lane] = r;
     }
-    unsigned bad = __ballot_sync(0xFFFFFFFFu, lane < n && r < 0 && r != -GFS_ENOMEM);
-    unsigned nomem = __ballot_sync(0xFFFFFFFFu, lane < n && r == -GFS_ENOMEM);
+    const unsigned bad = __ballot_sync(0xFFFFFFFFu, (uint32_t)lane < n && r < 0 && r != -GFS_ENOMEM);
+    const unsigned nomem = __ballot_sync(0xFFFFFFFFu, (uint32_t)lane < n && r == -GFS_ENOMEM);
     if (bad || nomem) {
-        if (lane < n && r >= 0) unpin(C.S, (uint32_t)r);
+        if ((uint32_t)lane < n && r >= 0) unpin(S, (uint32_t)r);
         return bad ? __shfl_sync(0xFFFFFFFFu, r, __ffs(bad) - 1) : -GFS_ENOMEM;
     }
     return 0;
 }
 
-__device__ void unpin_window(const Ctx& C, Shared& sh) {
+__device__ void unpin_window(gfs_state* S, Shared& sh, Window& w) {
     const int lane = threadIdx.x & 31;
-    if (lane < sh.win_n) unpin(C.S, (uint32_t)sh.win_frames[lane]);
+    if (w.live && (uint32_t)lane < w.n) unpin(S, (uint32_t)sh.frames[w.buf][lane]);
+    w.live = false;
 }
 
-/* Process one staged chunk.  base: the stage buffer (chunk byte 0),
- * clen: valid bytes, cpos: file offset of the chunk. */
-template <bool SMEM>
-__device__ __forceinline__ void scan_chunk(const Ctx& C, Shared& sh, uint32_t* tbl, const uint8_t* base, uint32_t clen,
-                                           uint32_t avail, uint64_t cpos, uint64_t fsize, int f, uint16_t* slist,
-                                           uint16_t* elist, uint8_t* wscratch, int parity) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t seg0 = (uint32_t)warp * GR_SEG;
-    const bool last_in_file = cpos + clen >= fsize;
-    if (seg0 < clen) {
-        const uint32_t off = seg0 + 16u * (uint32_t)lane;
-        uint4 v = *(const uint4*)(base + off);
-        uint32_t a = alpha16(v);
-        if (off >= clen) a = 0u;
-        else if (clen - off < 16u) a &= (1u << (clen - off)) - 1u;
-        /* previous byte's class */
-        uint32_t pb = __shfl_up_sync(0xFFFFFFFFu, a >> 15, 1);
-        if (lane == 0) pb = (seg0 == 0) ? sh.prev_alpha[parity] : (uint32_t)is_alpha(base[seg0 - 1]);
-        /* next byte's class; past the chunk end a token may continue (it is
-         * then left open and its end found by a scan), past the file end not */
-        uint32_t nxt = __shfl_down_sync(0xFFFFFFFFu, a & 1u, 1);
-        if (lane == 31) nxt = seg0 + GR_SEG < clen ? (uint32_t)is_alpha(base[seg0 + GR_SEG]) : 0u;
-        uint32_t na = (a >> 1) | (nxt << 15);
-        if (off < clen && clen - off <= 16u) {
-            const uint32_t j = clen - off - 1u;
-            na = (na & ~(1u << j)) | ((last_in_file ? 0u : 1u) << j);
+__device__ void producer(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* stages, uint64_t c0, uint64_t c1) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lp = S->log_page, page = S->page_size, pmask = page - 1u;
+    Window prev = {0, 0, 1, 0, false};
+    uint32_t g = 0;
+    /* pages one chunk with its look-behind and look-ahead can touch */
+    const uint32_t minwin = (uint32_t)((GR_LB + GR_CH + GR_LA + page - 1) / page) + 1u;
+    uint64_t c = c0;
+    while (c < c1) {
+        const int f = file_of(P, c);
+        const uint64_t fsize = P.sizes[f];
+        const uint64_t kend = (P.chunk_prefix[f + 1] < c1 ? P.chunk_prefix[f + 1] : c1) - P.chunk_prefix[f];
+        uint64_t k = c - P.chunk_prefix[f];
+        while (k < kend) {
+            /* window: chunks [k, kw) whose bytes, look-behind and look-ahead
+             * lie in at most sh.win pages */
+            const uint64_t lbpos = k * GR_CH >= GR_LB ? k * GR_CH - GR_LB : 0;
+            const uint32_t lb = (uint32_t)(lbpos >> lp);
+            uint64_t kw;
+            uint32_t n;
+            int buf = prev.buf ^ 1;
+            int e = 0;
+            bool hard = false;
+            for (;;) {
+                const uint64_t lim = ((uint64_t)lb + sh.win) << lp; /* first byte not covered */
+                kw = lim >= fsize + GR_LA ? kend : (lim > GR_LA ? (lim - GR_LA) / GR_CH : 0);
+                if (kw > kend) kw = kend;
+                if (kw <= k) kw = k + 1; /* a window always holds at least one chunk */
+                uint64_t endb = kw * GR_CH + GR_LA;
+                if (endb > fsize) endb = fsize;
+                n = (uint32_t)(((endb + pmask) >> lp) - lb);
+                if (n > GR_WIN) { kw = k + 1; endb = kw * GR_CH + GR_LA < fsize ? kw * GR_CH + GR_LA : fsize; n = (uint32_t)(((endb + pmask) >> lp) - lb); }
+                e = pin_pages(S, sh, buf, P.fds[f], lb, n, hard ? false : true);
+                if (e == -GFS_ENOMEM && !hard) {
+                    /* the pool is short: shrink the window; at the smallest
+                     * window drop the previous one first, then wait for frames */
+                    if (sh.win > minwin) {
+                        if (lane == 0) sh.win = sh.win / 2 > minwin ? sh.win / 2 : minwin;
+                    } else if (prev.live) {
+                        if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, 7);
+                        __syncwarp();
+                        unpin_window(S, sh, prev);
+                    } else {
+                        hard = true;
+                    }
+                    __syncwarp();
+                    continue;
+                }
+                break;
+            }
+            if (e) {
+                if (lane == 0) fail(sh, P, e, 2);
+                __syncwarp();
+                break;
+            }
+            /* the previous window's copies have all landed once its last
+             * chunk's full phase completed (its stage is not re-armed yet) */
+            if (prev.live) {
+                if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, 3);
+                __syncwarp();
+                unpin_window(S, sh, prev);
+            }
+            for (uint64_t kk = k; kk < kw; kk++, g++) {
+                const uint32_t s = g % GR_STAGES;
+                if (lane == 0) {
+                    bool ok = true;
+                    if (g >= GR_STAGES) ok = wait_phase(sh, P, &sh.empty[s], ((g / GR_STAGES) - 1u) & 1u, 4);
+                    const uint64_t pos = kk * GR_CH;
+                    const uint64_t rem = fsize - pos;
+                    StageDesc& dsc = sh.desc[s];
+                    dsc.pos = pos;
+                    dsc.f = f;
+                    dsc.clen = (uint32_t)(rem < GR_CH ? rem : GR_CH);
+                    dsc.avail = (uint32_t)(rem < (uint64_t)GR_CH + GR_LA ? rem : (uint64_t)GR_CH + GR_LA);
+                    uint8_t* dst = stages + (size_t)s * GR_STAGE;
+                    if (!ok || sh.abort) {
+                        mbar_arrive(&sh.full[s]); /* release the consumers; they see abort */
+                    } else {
+                        const uint32_t body = (dsc.avail + 15u) & ~15u;
+                        const uint32_t lbb = pos > 0 ? (uint32_t)GR_LB : 0u;
+                        fence_proxy_async();
+                        mbar_expect_tx(&sh.full[s], lbb + body);
+                        uint64_t from = pos - lbb;
+                        uint32_t done = 0, total = lbb + body;
+                        while (done < total) {
+                            const uint64_t q = from + done;
+                            const uint32_t pg = (uint32_t)(q >> lp);
+                            const uint32_t inpg = (uint32_t)(q & pmask);
+                            uint32_t piece = page - inpg;
+                            if (piece > total - done) piece = total - done;
+                            const uint8_t* src = S->pool + ((size_t)sh.frames[buf][pg - lb] << lp) + inpg;
+                            bulk_g2s(dst + (GR_LB - lbb) + done, src, piece, &sh.full[s]);
+                            done += piece;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+            prev.lb = lb;
+            prev.n = n;
+            prev.buf = buf;
+            prev.last_g = g - 1u;
+            prev.live = true;
+            k = kw;
         }
-        const uint32_t starts = a & ~((a << 1) | pb) & 0xFFFFu;
-        const uint32_t ends = a & ~na;
-        const uint32_t ns = (uint32_t)__popc(starts), ne = (uint32_t)__popc(ends);
-        uint32_t packed = ns | (ne << 16), incl = packed;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-            if (lane >= d) incl += t;
-        }
-        const uint32_t excl = incl - packed;
-        const uint32_t tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        const uint32_t n_s = tot & 0xFFFFu, n_e = tot >> 16;
-        uint32_t js = excl & 0xFFFFu, je = excl >> 16;
-        for (uint32_t m = starts; m; m &= m - 1u) slist[js++] = (uint16_t)(off + (uint32_t)(__ffs(m) - 1));
-        for (uint32_t m = ends; m; m &= m - 1u) elist[je++] = (uint16_t)(off + (uint32_t)(__ffs(m) - 1));
-        /* does the segment begin inside a token started earlier? */
-        const uint32_t carry = __shfl_sync(0xFFFFFFFFu, (a & 1u) & pb, 0);
+        if (sh.abort) break;
+        c = P.chunk_prefix[f] + kend;
+    }
+    if (prev.live) {
+        if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, 5);
         __syncwarp();
-        for (uint32_t t = (uint32_t)lane; t < n_s; t += 32u) {
-            const uint32_t st = slist[t];
-            const uint32_t ei = t + carry;
-            int len;
-            bool in_stage;
-            if (ei < n_e) {
-                len = (int)elist[ei] - (int)st + 1;
-                in_stage = true;
-            } else {
-                /* open at the segment end: scan forward through the staged
-                 * bytes (chunk + look-ahead); past `avail` lies end of file */
-                uint32_t p = st + 1u;
-                bool open = true;
-                while (open && p - st <= 32u) {
-                    uint32_t c = p < avail ? base[p] : (cpos + p >= fsize ? 0u : gbyte(C, sh, fsize, cpos + p));
-                    if (!is_alpha(c)) open = false;
-                    else p++;
-                }
-                len = (int)(p - st);
-                in_stage = p <= avail; /* always, given 64 bytes of look-ahead */
-                if (open) len = 33;
-            }
-            if (len > 32) {
-                if (len >= 33) atomicOr(&C.P.long_flags[f], 1u);
-                continue;
-            }
-            uint32_t k[8];
-            if (in_stage) {
-                key_from_smem(base, st, len, k);
-            } else {
-                /* crosses the chunk end: gather into this lane's scratch */
-                uint8_t* s = wscratch; /* one token per chunk crosses its end */
-                for (int i = 0; i < 40; i++) s[i] = 0;
-                for (int i = 0; i < len; i++) {
-                    uint32_t p = st + (uint32_t)i;
-                    s[i] = (uint8_t)(p < clen ? base[p] : gbyte(C, sh, fsize, cpos + p));
-                }
-                key_from_smem(s, 0, len, k);
-            }
-            count_key<SMEM>(C.P, tbl, k, len, f);
-        }
+        unpin_window(S, sh, prev);
     }
-    /* the last valid byte's class is the next chunk's look-behind */
-    if (threadIdx.x == 0) {
-        uint32_t lb = clen ? (uint32_t)is_alpha(base[clen - 1]) : sh.prev_alpha[parity];
-        sh.prev_alpha[parity ^ 1] = lb;
-    }
-}
-
-template <bool SMEM>
-__device__ void flush_counts(const Ctx& C, uint32_t* tbl, int f) {
-    if (!SMEM) return;
-    const uint32_t nslots = 4u * C.P.nb;
-    for (uint32_t i = threadIdx.x; i < nslots; i += blockDim.x) {
-        uint32_t v = tbl[i];
-        uint32_t n = v & GREP_CNT_MASK;
-        if (n) {
-            tbl[i] = v & ~GREP_CNT_MASK;
-            flush_slot(C.P, i, n, f);
+    /* chunks never produced after an abort: release their consumers */
+    if (sh.abort && lane == 0) {
+        uint64_t total = c1 - c0;
+        for (; g < total; g++) {
+            const uint32_t s = g % GR_STAGES;
+            if (g >= GR_STAGES && !wait_phase(sh, P, &sh.empty[s], ((g / GR_STAGES) - 1u) & 1u, 6)) {
+                /* consumers are gone too */
+            }
+            mbar_arrive(&sh.full[s]);
         }
     }
 }
 
 } // namespace
 
-/* One persistent CTA per SM; see the file comment. */
+/* One persistent 1024-thread CTA per SM: warp 31 pins pages and streams
+ * chunks (TMA), warps 0..30 scan them; see the file comment. */
 template <bool SMEM>
 __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepDev P) {
     extern __shared__ __align__(128) uint8_t dsm[];
     __shared__ Shared sh;
-    Ctx C;
-    C.S = S;
-    C.P = P;
-    C.lp = S->log_page;
-    C.pmask = S->page_size - 1u;
     const uint32_t tbl_bytes = SMEM ? 16u * P.nb : 0u;
     uint32_t* tbl = SMEM ? (uint32_t*)dsm : (uint32_t*)P.table;
     uint8_t* stages = dsm + ((tbl_bytes + 127u) & ~127u);
-    const uint32_t stage_bytes = GR_CH + 96u; /* chunk + 64 look-ahead + read slack */
-    uint16_t* lists = (uint16_t*)(stages + GR_STAGES * stage_bytes);
-    uint8_t* scratch = (uint8_t*)(lists + GR_WARPS * 2 * GR_LIST);
+    uint16_t* lists = (uint16_t*)(stages + GR_STAGES * GR_STAGE);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint16_t* slist = lists + warp * 2 * GR_LIST;
-    uint16_t* elist = slist + GR_LIST;
-    uint8_t* wscratch = scratch + warp * 48;
 
     if (SMEM)
         for (uint32_t i = threadIdx.x; i < P.nb; i += blockDim.x) ((uint4*)tbl)[i] = __ldg((const uint4*)P.table + i);
     if (threadIdx.x == 0) {
-        for (int s = 0; s < GR_STAGES; s++) mbar_init(&sh.mbar[s], 1u);
+        for (int s = 0; s < GR_STAGES; s++) {
+            mbar_init(&sh.full[s], 1u);
+            mbar_init(&sh.empty[s], GR_CONS);
+        }
         fence_mbar_init();
+        sh.abort = 0;
         sh.err = 0;
-        sh.prev_alpha[0] = sh.prev_alpha[1] = 0u;
+        uint32_t w = P.win_pages ? P.win_pages : GR_WIN;
+        const uint32_t mw = (uint32_t)((GR_LB + GR_CH + GR_LA + S->page_size - 1) / S->page_size) + 1u;
+        sh.win = w > GR_WIN ? GR_WIN : (w < mw ? mw : w);
     }
     __syncthreads();
 
     const uint64_t total = P.total_chunks;
     const uint64_t c0 = total * blockIdx.x / gridDim.x, c1 = total * (blockIdx.x + 1) / gridDim.x;
-    uint32_t gi = 0; /* chunks streamed by this CTA: stage = gi % STAGES, parity = (gi / STAGES) & 1 */
-    int parity = 0;   /* prev_alpha double buffer */
-    const uint32_t page = S->page_size;
-    const uint32_t chunks_per_page = page >= GR_CH ? page / GR_CH : 1u;
-    const uint32_t pages_per_chunk = page >= GR_CH ? 1u : GR_CH / page;
-    __shared__ uint32_t s_wdp; /* data pages per window; halved when the pool is short */
-    if (threadIdx.x == 0) {
-        uint32_t w = P.win_data ? P.win_data : (GR_WIN - 2);
-        if (w > GR_WIN - 2) w = GR_WIN - 2;
-        w = w / pages_per_chunk * pages_per_chunk;
-        s_wdp = w ? w : pages_per_chunk;
+    if (warp == GR_CONS) {
+        producer(S, P, sh, stages, c0, c1);
+        return;
     }
-    __syncthreads();
-
-    uint64_t cur = c0;
-    while (cur < c1 && !sh.err) {
-        /* file of chunk `cur` */
-        int lo = 0, hi = P.n_files - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (P.chunk_prefix[mid] <= cur) lo = mid; else hi = mid - 1;
-        }
-        const int f = lo;
+    uint16_t* slist = lists + warp * 2 * GR_LIST;
+    uint16_t* elist = slist + GR_LIST;
+    uint32_t g = 0;
+    uint64_t c = c0;
+    while (c < c1) {
+        const int f = file_of(P, c);
         const uint64_t fend = P.chunk_prefix[f + 1] < c1 ? P.chunk_prefix[f + 1] : c1;
-        const uint64_t fsize = P.sizes[f];
-        const int fd = P.fds[f];
-        const uint32_t fpages = (uint32_t)((fsize + page - 1) >> C.lp);
-        uint64_t k = cur - P.chunk_prefix[f];  /* chunk index within the file */
-        const uint64_t kend = fend - P.chunk_prefix[f];
-        bool first_window = true;
-        while (k < kend && !sh.err) {
-            /* window: data pages from the page of chunk k */
-            const uint32_t dp0 = (uint32_t)((k * GR_CH) >> C.lp);
-            uint32_t dp1 = dp0 + s_wdp;
-            const uint32_t need_end = (uint32_t)(((kend * GR_CH < fsize ? kend * GR_CH : fsize) + page - 1) >> C.lp);
-            if (dp1 > need_end) dp1 = need_end;
-            uint32_t lb = dp0;
-            if (first_window && k * GR_CH > 0) lb = (uint32_t)((k * GR_CH - 1) >> C.lp);
-            uint32_t ub = dp1 + 1u < fpages ? dp1 + 1u : fpages; /* look-ahead page */
-            if (ub < dp1) ub = dp1;
-            const uint64_t kw_end_pos = (uint64_t)dp1 << C.lp;
-            uint64_t kw_end = (kw_end_pos + GR_CH - 1) / GR_CH;
-            if (kw_end > kend) kw_end = kend;
-            if (warp == 0) {
-                if (lane == 0) {
-                    sh.win_lb = lb;
-                    sh.win_n = (int)(ub - lb);
-                }
-                __syncwarp();
-                int e = pin_window(C, sh, fd, fsize, lb, (int)(ub - lb));
-                if (lane == 0 && e) {
-                    if (e == -GFS_ENOMEM && s_wdp > pages_per_chunk) {
-                        s_wdp = (s_wdp / 2 + pages_per_chunk - 1) / pages_per_chunk * pages_per_chunk;
-                        sh.err = 1; /* retry this window smaller */
-                    } else {
-                        sh.err = e;
-                        atomicCAS(&P.status[1], 0u, (2u << 16) | (uint32_t)(-e));
-                    }
-                }
+        for (; c < fend; c++, g++) {
+            const uint32_t s = g % GR_STAGES;
+            bool ok = true;
+            if (lane == 0) ok = wait_phase(sh, P, &sh.full[s], (g / GR_STAGES) & 1u, 1);
+            ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
+            if (ok && !sh.abort) {
+                const StageDesc d = sh.desc[s];
+                scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, slist, elist, nullptr);
             }
-            __syncthreads();
-            if (sh.err == 1) {
-                __syncthreads();
-                if (threadIdx.x == 0) sh.err = 0;
-                __syncthreads();
-                continue;
-            }
-            if (sh.err) break;
-            if (threadIdx.x == 0 && first_window) {
-                sh.prev_alpha[parity] = k == 0 ? 0u : (uint32_t)is_alpha(gbyte(C, sh, fsize, k * GR_CH - 1));
-            }
-            first_window = false;
-            /* stream chunks [k, kw_end) through the stage ring */
-            const uint32_t n = (uint32_t)(kw_end - k);
-            auto issue = [&](uint32_t i) {
-                const uint64_t kk = k + i;
-                const uint32_t g = gi + i;
-                uint8_t* dst = stages + (g % GR_STAGES) * stage_bytes;
-                uint64_t pos = kk * GR_CH;
-                /* the chunk plus 64 bytes of look-ahead (tokens that start in the
-                 * chunk end at most 33 bytes past it), rounded to 16 bytes */
-                uint64_t cov = fsize - pos < (uint64_t)GR_CH + 64u ? fsize - pos : (uint64_t)GR_CH + 64u;
-                uint32_t clen16 = ((uint32_t)cov + 15u) & ~15u;
-                mbar_expect_tx(&sh.mbar[g % GR_STAGES], clen16);
-                uint32_t done = 0;
-                while (done < clen16) {
-                    uint64_t q = pos + done;
-                    uint32_t pg = (uint32_t)(q >> C.lp);
-                    uint32_t in_pg = (uint32_t)(q & C.pmask);
-                    uint32_t piece = page - in_pg;
-                    if (piece > clen16 - done) piece = clen16 - done;
-                    const uint8_t* src = S->pool + ((size_t)sh.win_frames[pg - sh.win_lb] << C.lp) + in_pg;
-                    bulk_g2s(dst + done, src, piece, &sh.mbar[g % GR_STAGES]);
-                    done += piece;
-                }
-            };
-            if (threadIdx.x == 0) {
-                fence_proxy_async();
-                for (uint32_t i = 0; i < n && i < GR_STAGES - 1; i++) issue(i);
-            }
-            for (uint32_t i = 0; i < n; i++) {
-                const uint32_t g = gi + i;
-                if (threadIdx.x == 0 && i + GR_STAGES - 1 < n) {
-                    fence_proxy_async();
-                    issue(i + GR_STAGES - 1);
-                }
-                /* wait for chunk i (bounded) */
-                {
-                    uint32_t spins = 0;
-                    while (!mbar_try_wait(&sh.mbar[g % GR_STAGES], (g / GR_STAGES) & 1u)) {
-                        if (++spins > (1u << 26)) {
-                            if (threadIdx.x == 0) {
-                                sh.err = -GFS_ETIMEDOUT;
-                                atomicOr(P.status, GFS_ERRB_TIMEOUT);
-                                atomicCAS(&P.status[1], 0u, (1u << 16) | (uint32_t)(g & 0xFFFFu));
-                            }
-                            break;
-                        }
-                        if (spins > 64) __nanosleep(64);
-                    }
-                }
-                const uint64_t kk = k + i;
-                const uint64_t pos = kk * GR_CH;
-                const uint32_t clen = (uint32_t)(fsize - pos < GR_CH ? fsize - pos : GR_CH);
-                const uint32_t avail = (uint32_t)(fsize - pos < (uint64_t)GR_CH + 64u ? fsize - pos : (uint64_t)GR_CH + 64u);
-                const uint8_t* base = stages + (g % GR_STAGES) * stage_bytes;
-                scan_chunk<SMEM>(C, sh, tbl, base, clen, avail, pos, fsize, f, slist, elist, wscratch, parity);
-                parity ^= 1;
-                __syncthreads();
-            }
-            gi += n;
-            if (warp == 0) unpin_window(C, sh);
-            __syncthreads();
-            k = kw_end;
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sh.empty[s]);
         }
-        flush_counts<SMEM>(C, tbl, f);
-        __syncthreads();
-        cur = fend;
+        consumers_sync();
+        if (!sh.abort) flush_counts<SMEM>(P, tbl, f);
+        consumers_sync();
     }
-    if (threadIdx.x == 0 && sh.err) atomicOr(P.status, sh.err == -GFS_ETIMEDOUT ? GFS_ERRB_TIMEOUT : GFS_ERRB_IO);
-    (void)chunks_per_page;
 }
 
 /* ------------------------------------------------------------------ */
@@ -562,7 +659,7 @@ __device__ void count_piece(const GrepDev& P, PageCursor& pc, uint64_t a, uint64
     for (int i = 0; i < 8; i++)
         k[i] = (uint32_t)buf[4 * i] | ((uint32_t)buf[4 * i + 1] << 8) | ((uint32_t)buf[4 * i + 2] << 16) |
                ((uint32_t)buf[4 * i + 3] << 24);
-    count_key<false>(P, nullptr, k, len, f);
+    lookup_count(P, nullptr, false, k, (uint32_t)len, f);
 }
 } // namespace
 
@@ -690,8 +787,9 @@ bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
                 uint32_t k[8];
                 int len;
                 rec_key(dict + (size_t)cur * 32, k, &len);
-                uint64_t h = grep_hash(k, len);
-                uint32_t b[2] = {grep_b1(h, nb), grep_b2(h, nb)};
+                const uint32_t h1 = grep_h1(grep_mix(k, len));
+                const uint32_t b1 = grep_bucket(h1, nb);
+                uint32_t b[2] = {b1, grep_b2(grep_h2(h1), b1, nb)};
                 int placed = -1;
                 for (int r = 0; r < 2 && placed < 0; r++)
                     for (int i = 0; i < GREP_WAYS; i++)
@@ -720,8 +818,8 @@ bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
             uint32_t k[8];
             int len;
             rec_key(dict + (size_t)w * 32, k, &len);
-            uint64_t h = grep_hash(k, len);
-            T.tbl[s] = grep_tag(h) << GREP_TAG_SHIFT;
+            const uint32_t h1 = grep_h1(grep_mix(k, len));
+            T.tbl[s] = (grep_tag(h1) << GREP_TAG_SHIFT) | (len > 16 ? GREP_LONG_BIT : 0u);
             memcpy(&T.recs[(size_t)s * 8], k, 32);
             T.slot_word[s] = (uint32_t)w;
         }
@@ -745,12 +843,12 @@ struct gfs_grep {
     uint32_t last_status[2] = {0, 0};
 };
 
-/* Data pages per window so that all CTAs' windows fit in half the pool. */
+/* Pages per window so that all CTAs' pinned windows (two each) fit in half
+ * the pool; the kernel halves it further if frames still run short. */
 static void set_window(gfs_grep* g, int n_ctas) {
     uint32_t frames = gfs_num_frames(g->ctx);
     uint64_t per = (uint64_t)frames / 2u / (uint64_t)(n_ctas > 0 ? n_ctas : 1);
-    uint32_t w = per > 2u ? (uint32_t)(per - 2u) : 1u;
-    g->dev.win_data = w > GR_WIN - 2 ? GR_WIN - 2 : w;
+    g->dev.win_pages = per > GR_WIN ? GR_WIN : (uint32_t)(per ? per : 1u); /* the kernel raises it to one chunk */
 }
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -844,7 +942,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     g->sms = sms;
-    size_t fixed = (size_t)GR_STAGES * (GR_CH + 96) + (size_t)GR_WARPS * 2 * GR_LIST * 2 + (size_t)GR_WARPS * 48 + 256;
+    size_t fixed = (size_t)GR_STAGES * GR_STAGE + (size_t)GR_CONS * 2 * GR_LIST * 2 + 256;
     size_t with_tbl = align_up((size_t)nb * 16, 128) + fixed;
     g->smem = with_tbl <= (size_t)maxsm;
     g->smem_bytes = g->smem ? with_tbl : fixed;

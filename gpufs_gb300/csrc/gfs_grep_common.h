@@ -6,6 +6,10 @@
  * its key is the token bytes zero-padded to 32 bytes, i.e. exactly a
  * normalised 32-byte dictionary record (grep_text_gpu.cu:221: records are
  * 32 bytes, NUL padded), as 8 little-endian 32-bit words.
+ *
+ * The hash is 32-bit integer arithmetic only (a multiply-add over the key
+ * words, then two xor-shift-multiply rounds): a handful of instructions per
+ * token on the GPU, where the scan is instruction-bound.
  */
 #ifndef GFS_GREP_COMMON_H
 #define GFS_GREP_COMMON_H
@@ -18,42 +22,29 @@
 #define GFS_HD static inline
 #endif
 
-#define GREP_WAYS 4       /* slots per bucket (16 bytes) */
-#define GREP_TAG_SHIFT 20 /* slot word: tag:12 << 20 | count:20 */
-#define GREP_CNT_MASK 0xFFFFFu
+#define GREP_WAYS 4        /* slots per bucket (16 bytes) */
+#define GREP_TAG_SHIFT 20  /* slot word: tag:12 << 20 | long:1 << 19 | count:19 */
+#define GREP_LONG_BIT 0x80000u
+#define GREP_CNT_MASK 0x7FFFFu
+#define GREP_CNT_FLUSH 0x40000u /* a counter is flushed to global memory at 2^18 */
 
-GFS_HD uint64_t grep_hash(const uint32_t k[8], int len) {
-    const uint64_t K0 = 0x9E3779B97F4A7C15ULL, K1 = 0xD6E8FEB86659FD93ULL, K2 = 0xFF51AFD7ED558CCDULL;
-    uint64_t h = (uint64_t)len * K0;
-    h = (h ^ ((uint64_t)k[0] | ((uint64_t)k[1] << 32))) * K1;
-    h ^= h >> 29;
-    if (len > 8) {
-        h = (h ^ ((uint64_t)k[2] | ((uint64_t)k[3] << 32))) * K1;
-        h ^= h >> 29;
-    }
-    if (len > 16) {
-        h = (h ^ ((uint64_t)k[4] | ((uint64_t)k[5] << 32))) * K1;
-        h ^= h >> 29;
-    }
-    if (len > 24) {
-        h = (h ^ ((uint64_t)k[6] | ((uint64_t)k[7] << 32))) * K1;
-        h ^= h >> 29;
-    }
-    h ^= h >> 32;
-    h *= K2;
-    h ^= h >> 29;
-    return h;
+/* key words k[0..7], len in 1..32 */
+GFS_HD uint32_t grep_mix(const uint32_t k[8], int len) {
+    uint32_t a = (uint32_t)len * 0x9E3779B1u + k[0] * 0x85EBCA77u + k[1] * 0xC2B2AE3Du + k[2] * 0x27D4EB2Fu +
+                 k[3] * 0x165667B1u;
+    if (len > 16) a += k[4] * 0xD3A2646Du + k[5] * 0xFD7046C5u + k[6] * 0xB55A4F09u + k[7] * 0x8DA6B343u;
+    return a;
 }
-
-GFS_HD uint32_t grep_tag(uint64_t h) {
-    uint32_t t = (uint32_t)(h >> 20) & 0xFFFu;
+GFS_HD uint32_t grep_h1(uint32_t a) { return (a ^ (a >> 15)) * 0x2C1B3C6Du; }
+GFS_HD uint32_t grep_h2(uint32_t h1) { return (h1 ^ (h1 >> 13)) * 0x297A2D39u; }
+GFS_HD uint32_t grep_tag(uint32_t h1) {
+    uint32_t t = h1 & 0xFFFu;
     return t ? t : 1u;
 }
-GFS_HD uint32_t grep_b1(uint64_t h, uint32_t nb) { return (uint32_t)(((uint64_t)(uint32_t)h * nb) >> 32); }
-GFS_HD uint32_t grep_b2(uint64_t h, uint32_t nb) {
-    uint32_t b = (uint32_t)(((h >> 32) * (uint64_t)nb) >> 32);
-    uint32_t a = grep_b1(h, nb);
-    return b == a ? (a + 1u == nb ? 0u : a + 1u) : b;
+GFS_HD uint32_t grep_bucket(uint32_t h, uint32_t nb) { return (uint32_t)(((uint64_t)h * nb) >> 32); }
+GFS_HD uint32_t grep_b2(uint32_t h2, uint32_t b1, uint32_t nb) {
+    uint32_t b = grep_bucket(h2, nb);
+    return b == b1 ? (b1 + 1u == nb ? 0u : b1 + 1u) : b;
 }
 
 #endif
