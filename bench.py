@@ -22,6 +22,7 @@ a time, all host threads) on a bounded sample of the same corpus.
 """
 import argparse
 import json
+import re
 import os
 import statistics
 import subprocess
@@ -149,14 +150,13 @@ def peaks():
 
 
 def traffic_per_byte():
-    """DRAM bytes per corpus byte of the scan kernel, from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "grep_scan_traffic.json")
-    if os.path.exists(p):
-        try:
-            return float(json.load(open(p))["dram_bytes_per_corpus_byte"])
-        except (KeyError, ValueError):
-            return None
-    return None
+    """DRAM bytes per corpus byte of the scan kernel, read from the committed
+    ncu summary (the `dram_bytes_per_corpus_byte` row)."""
+    p = os.path.join(ROOT, "profiles", "k_grep_scan_grep_text_256MiB.md")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"dram_bytes_per_corpus_byte\*\*\s*\|\s*\*\*([0-9.]+)", open(p).read())
+    return float(m.group(1)) if m else None
 
 
 def cpu_threads():
