@@ -35,6 +35,7 @@ STAT_NAMES = ["hits", "misses", "evictions", "writebacks", "read_rpcs", "bytes_r
               "host_writes", "host_write_bytes", "host_opens", "host_errors", "err_site", "rpc_submitted"]
 
 ERR_TIMEOUT, ERR_IO, ERR_NOMEM, ERR_TABLE, ERR_ARG = 1, 2, 4, 8, 16
+XXH64_NOALLOC_MAX_FILES = 1024  # GFS_XXH64_NOALLOC_MAX_FILES
 
 
 class Config(ctypes.Structure):
@@ -87,6 +88,7 @@ _SIGS = {
     "gfs_bigmatrix": (_int, [_c_p, _c_s, _c_s, _c_s, _int, _int, ctypes.POINTER(ctypes.c_float)]),
     "gfs_xxh64_files": (_int, [_c_p, ctypes.POINTER(_c_s), _int, ctypes.POINTER(ctypes.c_ulonglong),
                                ctypes.POINTER(ctypes.c_float)]),
+    "gfs_xxh64_files_noalloc": (_int, [_c_p, ctypes.POINTER(_c_s), _int, ctypes.POINTER(ctypes.c_ulonglong)]),
     "gfs_measure_link": (_int, [_u64, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
 }
 
@@ -225,6 +227,14 @@ class Session:
         _check(self.L.gfs_xxh64_files(self._h, _paths(paths), len(paths), out, ctypes.byref(ms)),
                "gfs_xxh64_files")
         return [int(v) for v in out], ms.value
+
+    def xxh64_files_noalloc(self, paths):
+        """gfs_xxh64_files without any allocation (at most XXH64_NOALLOC_MAX_FILES
+        files; calls on one device must not overlap)."""
+        out = (ctypes.c_ulonglong * max(len(paths), 1))()
+        _check(self.L.gfs_xxh64_files_noalloc(self._h, _paths(paths), len(paths), out),
+               "gfs_xxh64_files_noalloc")
+        return [int(v) for v in out[:len(paths)]]
 
     # -- introspection / fault injection --
     def stats(self):

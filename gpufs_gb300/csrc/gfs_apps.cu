@@ -21,6 +21,7 @@
 #include <string.h>
 #include <sys/stat.h>
 
+#include <mutex>
 #include <vector>
 
 #include "fs_calls.cu.h"
@@ -438,3 +439,105 @@ int gfs_xxh64_files(gfs_ctx* ctx, const char* const* paths, int n, unsigned long
 }
 
 } /* extern "C" */
+
+/* ---- allocation-free XXH64 over files ----
+ * The same three kernels as gfs_xxh64_files, with every per-call buffer
+ * (names, sizes, hashes, descriptors, close codes, error word) carved from
+ * one file-scope device array of fixed size instead of cudaMalloc.  Its
+ * device address is looked up once per device with cudaGetSymbolAddress, so
+ * the first call on a device does that set-up (and should come before any
+ * stream capture); later calls make no allocation of any kind, on the device
+ * or on the host.  All callers on a device share the array: overlapping calls
+ * on one device race and must be serialised by the caller. */
+namespace {
+
+constexpr size_t XN_NAMES = (size_t)GFS_XXH64_NOALLOC_MAX_FILES * GFS_NAME_MAX;
+constexpr size_t XN_SIZES = XN_NAMES;
+constexpr size_t XN_OUT = XN_SIZES + 8u * GFS_XXH64_NOALLOC_MAX_FILES;
+constexpr size_t XN_FDS = XN_OUT + 8u * GFS_XXH64_NOALLOC_MAX_FILES;
+constexpr size_t XN_RCS = XN_FDS + 4u * GFS_XXH64_NOALLOC_MAX_FILES;
+constexpr size_t XN_ERR = XN_RCS + 4u * GFS_XXH64_NOALLOC_MAX_FILES;
+constexpr size_t XN_BYTES = XN_ERR + 256u;
+constexpr int XN_MAX_DEVICES = 64;
+
+static __device__ __align__(256) unsigned char g_xxh64_scratch[XN_BYTES];
+
+unsigned char* g_xxh64_scratch_addr[XN_MAX_DEVICES];
+std::mutex g_xxh64_scratch_mu;
+
+/* device address of g_xxh64_scratch on the current device (set-up on first use) */
+int xxh64_scratch(unsigned char** out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= XN_MAX_DEVICES) return -GFS_EIO;
+    std::lock_guard<std::mutex> lk(g_xxh64_scratch_mu);
+    if (!g_xxh64_scratch_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_xxh64_scratch);
+        if (e != cudaSuccess || !p) {
+            fprintf(stderr, "gpufs_gb300: gfs_xxh64_files_noalloc: cudaGetSymbolAddress failed: %s\n",
+                    cudaGetErrorString(e));
+            return -GFS_EIO;
+        }
+        g_xxh64_scratch_addr[dev] = (unsigned char*)p;
+    }
+    *out = g_xxh64_scratch_addr[dev];
+    return 0;
+}
+
+} /* namespace */
+
+extern "C" int gfs_xxh64_files_noalloc(gfs_ctx* ctx, const char* const* paths, int n, unsigned long long* host_out) {
+    if (n < 1 || !paths || !host_out) return -GFS_EINVAL;
+    if (n > GFS_XXH64_NOALLOC_MAX_FILES) {
+        fprintf(stderr, "gpufs_gb300: gfs_xxh64_files_noalloc: %d files exceed the static scratch limit of %d\n", n,
+                GFS_XXH64_NOALLOC_MAX_FILES);
+        return -GFS_E2BIG;
+    }
+    for (int i = 0; i < n; i++)
+        if (!paths[i] || strlen(paths[i]) >= GFS_NAME_MAX) return -GFS_EINVAL;
+    if (gfs__activate(ctx)) return -GFS_EIO;
+    unsigned char* base = nullptr;
+    int rc = xxh64_scratch(&base);
+    if (rc) return rc;
+    char* names = (char*)base;
+    uint64_t* sizes = (uint64_t*)(base + XN_SIZES);
+    unsigned long long* out = (unsigned long long*)(base + XN_OUT);
+    int* fds = (int*)(base + XN_FDS);
+    int* rcs = (int*)(base + XN_RCS);
+    int* err = (int*)(base + XN_ERR);
+    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
+    /* names go up in chunks through a stack buffer: a pageable-to-device
+     * cudaMemcpyAsync has consumed its source when it returns */
+    constexpr int CH = 32;
+    char hn[CH * GFS_NAME_MAX];
+    cudaError_t e = cudaSuccess;
+    for (int i0 = 0; i0 < n && e == cudaSuccess; i0 += CH) {
+        const int m = n - i0 < CH ? n - i0 : CH;
+        memset(hn, 0, sizeof hn);
+        for (int j = 0; j < m; j++) memcpy(hn + (size_t)j * GFS_NAME_MAX, paths[i0 + j], strlen(paths[i0 + j]));
+        e = cudaMemcpyAsync(names + (size_t)i0 * GFS_NAME_MAX, hn, (size_t)m * GFS_NAME_MAX, cudaMemcpyHostToDevice,
+                            s);
+    }
+    /* the error word is the only state that must start at zero */
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, 4, s);
+    if (e != cudaSuccess) return -GFS_EIO;
+    k_open_many<<<n, 64, 0, s>>>(names, n, O_GRDONLY, fds, sizes);
+    const int warps = 8;
+    k_xxh64<<<(n + warps - 1) / warps, warps * 32, 0, s>>>(fds, sizes, n, out, err);
+    k_close_many<<<n, 64, 0, s>>>(fds, n, rcs);
+    e = cudaGetLastError();
+    cudaError_t es = cudaStreamSynchronize(s); /* kernels first, then copies back */
+    if (e == cudaSuccess) e = es;
+    int herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(host_out, out, sizeof(unsigned long long) * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost);
+    int hf[256];
+    for (int i0 = 0; i0 < n && e == cudaSuccess; i0 += 256) {
+        const int m = n - i0 < 256 ? n - i0 : 256;
+        e = cudaMemcpy(hf, fds + i0, 4 * (size_t)m, cudaMemcpyDeviceToHost);
+        for (int j = 0; j < m && e == cudaSuccess; j++)
+            if (hf[j] < 0) return hf[j];
+    }
+    if (e != cudaSuccess) return -GFS_EIO;
+    return herr;
+}

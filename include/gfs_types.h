@@ -79,6 +79,7 @@ extern "C" {
 #define GFS_OK 0
 #define GFS_ENOENT 2
 #define GFS_EIO 5
+#define GFS_E2BIG 7
 #define GFS_EBADF 9
 #define GFS_ENOMEM 12
 #define GFS_EINVAL 22

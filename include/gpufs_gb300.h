@@ -126,6 +126,17 @@ int gfs_bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, cons
 /* XXH64 (seed 0) of each file, read through the buffer cache; one warp per file */
 int gfs_xxh64_files(gfs_ctx* ctx, const char* const* paths, int n, unsigned long long* host_out, float* kernel_ms);
 
+/* Allocation-free form of gfs_xxh64_files (no reference counterpart: the
+ * reference has no checksum and allocates per call).  Same results; every
+ * per-call buffer lives in a fixed file-scope device array, so a call makes
+ * no cudaMalloc/cudaFree or other allocation.  At most
+ * GFS_XXH64_NOALLOC_MAX_FILES files per call, else -GFS_E2BIG.  The first
+ * call on a device looks the array's address up (cudaGetSymbolAddress): make
+ * it before any stream capture.  The array is shared by all callers on a
+ * device, so overlapping calls on one device race: serialise them. */
+#define GFS_XXH64_NOALLOC_MAX_FILES 1024
+int gfs_xxh64_files_noalloc(gfs_ctx* ctx, const char* const* paths, int n, unsigned long long* host_out);
+
 /* ---- grep_text (samples/grep_text/grep_text_gpu.cu:193-387) ----
  * Whole-word occurrence counts of every record of a dictionary file (32-byte
  * NUL-padded records, the reference's dict.gpu format) in every corpus file,
