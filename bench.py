@@ -21,6 +21,7 @@ match_string driven through its 16 KiB window walk, one dictionary word at
 a time, all host threads) on a bounded sample of the same corpus.
 """
 import argparse
+import atexit
 import json
 import re
 import os
@@ -91,11 +92,24 @@ class Clocks:
         self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
 
     def start(self):
+        # the sampler never outlives the bench: a time limit of its own, and
+        # a stop at interpreter exit whatever way the bench ends
         try:
-            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
-                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            self.p = subprocess.Popen(["timeout", "900", "nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+        if self.p is not None:
+            atexit.register(self._kill)
+
+    def _kill(self):
+        if self.p is not None and self.p.poll() is None:
+            self.p.kill()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                pass
 
     def stop(self):
         if self.p is None:

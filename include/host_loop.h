@@ -6,7 +6,20 @@
 #ifndef HOST_LOOP_CPP
 #define HOST_LOOP_CPP
 
+/* system headers the reference's host_loop.h brings in, which the samples
+ * use without including them (stat, open, pthreads, iostream) */
+#include <assert.h>
+#include <fcntl.h>
+#include <pthread.h>
 #include <stdio.h>
+#include <string.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <sys/types.h>
+#include <unistd.h>
+#include <iomanip>
+#include <iostream>
+
 #include "fs_initializer.cu.h"
 
 static inline void run_gpufs_handler(volatile GPUGlobals* gpuGlobals, int gpuid) {
