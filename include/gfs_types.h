@@ -20,8 +20,9 @@
  *              status, slot incarnation and open count for CAS transitions.
  *   ring[]     MPMC request ring in mapped pinned host memory (Vyukov
  *              sequence protocol): device blocks produce, host workers
- *              consume; completions come back as a 32-bit word written into
- *              device memory by the stream that moved the data.
+ *              consume; completions come back as a 32-bit word in mapped
+ *              host memory (hdone), stored by the host worker once the copy
+ *              that moved the data has completed.
  */
 #ifndef GFS_TYPES_H
 #define GFS_TYPES_H
@@ -143,7 +144,7 @@ typedef struct gfs_req {
     int32_t oflags;
     uint32_t pad[5];
     char name[GFS_NAME_MAX];
-} gfs_req; /* 128 bytes */
+} gfs_req; /* 136 bytes */
 
 typedef struct gfs_stats {
     unsigned long long hits;
@@ -192,5 +193,8 @@ typedef struct gfs_state {
 
 #ifdef __cplusplus
 }
+static_assert(sizeof(gfs_req) == 136, "gfs_req layout");
+static_assert(sizeof(gfs_frame) == 32, "gfs_frame layout");
+static_assert(sizeof(gfs_open_reply) == 24, "gfs_open_reply layout");
 #endif
 #endif
