@@ -97,11 +97,15 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
 }
+/* try_wait with a suspend-time hint: the thread sleeps in hardware until the
+ * phase completes or GR_SUSPEND_NS pass, instead of spinning on the issue
+ * slots the scanning warps need */
+#define GR_SUSPEND_NS 20000u
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
     uint32_t ok;
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok) : "r"(smem_u32(b)), "r"(parity) : "memory");
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok) : "r"(smem_u32(b)), "r"(parity), "n"(GR_SUSPEND_NS) : "memory");
     return ok != 0;
 }
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
@@ -251,6 +255,8 @@ struct Shared {
     volatile int abort;
     int err;
     uint32_t win;
+    uint32_t next_item; /* consumers take (chunk, segment) items in order */
+    uint64_t wait_ns;   /* bound on every mbarrier wait (session timeout) */
 };
 
 __device__ __forceinline__ void fail(Shared& sh, const GrepDev& P, int e, uint32_t site) {
@@ -260,16 +266,22 @@ __device__ __forceinline__ void fail(Shared& sh, const GrepDev& P, int e, uint32
     atomicCAS(&P.status[1], 0u, (site << 16) | (uint32_t)(e < 0 ? -e : e));
 }
 
-/* Bounded wait on an mbarrier phase by one lane.  false: gave up (abort). */
+/* Bounded wait on an mbarrier phase by one lane.  false: gave up (abort).
+ * Each try suspends for up to GR_SUSPEND_NS; every 16 tries the abort flag
+ * and the session's wait limit (%globaltimer) are checked. */
 __device__ __forceinline__ bool wait_phase(Shared& sh, const GrepDev& P, uint64_t* bar, uint32_t parity, uint32_t site) {
     uint32_t spins = 0;
+    uint64_t t0 = 0;
     while (!mbar_try_wait(bar, parity)) {
-        if (sh.abort) return false;
-        if (++spins > (1u << 24)) {
-            fail(sh, P, -GFS_ETIMEDOUT, site);
-            return false;
+        if ((++spins & 15u) == 0u) {
+            if (sh.abort) return false;
+            const uint64_t now = gtimer();
+            if (t0 == 0) t0 = now;
+            else if (now - t0 > sh.wait_ns) {
+                fail(sh, P, -GFS_ETIMEDOUT, site);
+                return false;
+            }
         }
-        if (spins > 32) __nanosleep(spins > 4096 ? 2048 : 64);
     }
     return true;
 }
@@ -286,9 +298,9 @@ __device__ __forceinline__ int file_of(const GrepDev& P, uint64_t c) {
 /* ---------------- consumer: one 512-byte segment ---------------- */
 template <bool SMEM>
 __device__ __forceinline__ void scan_segment(const GrepDev& P, uint32_t* tbl, const uint8_t* base, const StageDesc& d,
-                                             uint16_t* slist, uint16_t* elist, uint8_t* wscr) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t seg0 = (uint32_t)warp * GR_SEG;
+                                             uint32_t segi, uint16_t* slist, uint16_t* elist) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t seg0 = segi * GR_SEG;
     const uint32_t clen = d.clen, avail = d.avail;
     if (seg0 >= clen) return;
     const uint32_t off = seg0 + 16u * (uint32_t)lane;
@@ -383,7 +395,6 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, uint32_t* tbl, co
             }
         }
     }
-    (void)wscr;
 }
 
 template <bool SMEM>
@@ -583,6 +594,8 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
         fence_mbar_init();
         sh.abort = 0;
         sh.err = 0;
+        sh.next_item = 0;
+        sh.wait_ns = S->timeout_ns;
         uint32_t w = P.win_pages ? P.win_pages : GR_WIN;
         const uint32_t mw = (uint32_t)((GR_LB + GR_CH + GR_LA + S->page_size - 1) / S->page_size) + 1u;
         sh.win = w > GR_WIN ? GR_WIN : (w < mw ? mw : w);
@@ -597,26 +610,42 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
     }
     uint16_t* slist = lists + warp * 2 * GR_LIST;
     uint16_t* elist = slist + GR_LIST;
-    uint32_t g = 0;
-    uint64_t c = c0;
-    while (c < c1) {
-        const int f = file_of(P, c);
-        const uint64_t fend = P.chunk_prefix[f + 1] < c1 ? P.chunk_prefix[f + 1] : c1;
-        for (; c < fend; c++, g++) {
-            const uint32_t s = g % GR_STAGES;
-            bool ok = true;
-            if (lane == 0) ok = wait_phase(sh, P, &sh.full[s], (g / GR_STAGES) & 1u, 1);
-            ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
-            if (ok && !sh.abort) {
-                const StageDesc d = sh.desc[s];
-                scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, slist, elist, nullptr);
-            }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&sh.empty[s]);
+    /* Items (chunk, segment) are taken in order from a shared counter, so a
+     * warp that finishes early takes the next segment instead of idling
+     * behind the slowest warp of its chunk.  A chunk has exactly GR_CONS
+     * items, one per consumer warp: a chunk's items cannot all be finished
+     * before it has landed, so no warp can take an item of the chunk four
+     * stages later while its stage still holds an earlier phase (the parity
+     * waits stay unambiguous).  Counts are flushed per file: a warp whose
+     * item lies beyond the current file waits at the consumers' barrier,
+     * which every warp passes once per file in the same order. */
+    const uint32_t nchunks = (uint32_t)(c1 - c0), n_items = nchunks * GR_CONS;
+    if (nchunks == 0) return;
+    int f = file_of(P, c0);
+    uint32_t fend = (uint32_t)((P.chunk_prefix[f + 1] < c1 ? P.chunk_prefix[f + 1] : c1) - c0);
+    for (;;) {
+        uint32_t it = 0;
+        if (lane == 0) it = atomicAdd(&sh.next_item, 1u);
+        it = __shfl_sync(0xFFFFFFFFu, it, 0);
+        const uint32_t g = it < n_items ? it / GR_CONS : nchunks;
+        while (g >= fend) {
+            consumers_sync();
+            if (!sh.abort) flush_counts<SMEM>(P, tbl, f);
+            consumers_sync();
+            if (fend >= nchunks) return;
+            f = file_of(P, c0 + fend);
+            fend = (uint32_t)((P.chunk_prefix[f + 1] < c1 ? P.chunk_prefix[f + 1] : c1) - c0);
         }
-        consumers_sync();
-        if (!sh.abort) flush_counts<SMEM>(P, tbl, f);
-        consumers_sync();
+        const uint32_t s = g % GR_STAGES;
+        bool ok = true;
+        if (lane == 0) ok = wait_phase(sh, P, &sh.full[s], (g / GR_STAGES) & 1u, 1);
+        ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
+        if (ok && !sh.abort) {
+            const StageDesc d = sh.desc[s];
+            scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % GR_CONS, slist, elist);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sh.empty[s]);
     }
 }
 
