@@ -59,7 +59,6 @@
 #define GR_LA 64                      /* look-ahead bytes staged after it */
 #define GR_STAGE (GR_LB + GR_CH + GR_LA + 32)
 #define GR_STAGES 4
-#define GR_LIST 258                   /* a segment holds up to 256 starts and 257 ends */
 #define GR_WIN 32                     /* pages per window, incl. look-behind/ahead */
 
 extern __device__ gfs_state* g_gfs;
@@ -73,7 +72,9 @@ struct GrepDev {
     uint64_t total_chunks;
     uint32_t nb;                  /* buckets */
     const uint32_t* table;        /* nb * 4 slot words: tag << 20 | long << 19 */
-    const uint4* recs;            /* nb * 4 records of 32 bytes */
+    const uint4* rec_lo;          /* nb * 4: bytes 0..15 of each slot's record */
+    const uint4* rec_hi;          /* nb * 4: bytes 16..31 (separate, so the short-word
+                                     probes touch half the bytes) */
     const uint32_t* slot_word;    /* first record of each slot, ~0 if empty */
     const int32_t* next_dup;      /* next record with the same word, -1 */
     uint32_t* counts;             /* n_words x n_files */
@@ -135,22 +136,18 @@ __device__ __forceinline__ uint32_t is_alpha(uint32_t c) {
     return ((c - 65u < 26u) || (c - 97u < 26u) || c == 95u) ? 1u : 0u;
 }
 
-/* key of a token of len <= 16 at byte st of an 8-byte aligned smem buffer
- * readable 24 bytes past (st & ~7): three 8-byte loads, funnel shifts, and
- * a clamp mask per word (no branches) */
+/* key of a token of len <= 16 at byte st of a 4-byte aligned smem buffer
+ * readable 20 bytes past (st & ~3): five word loads, funnel shifts, and a
+ * clamp mask per word (no branches) */
 __device__ __forceinline__ void key16(const uint8_t* base, uint32_t st, uint32_t len, uint32_t k[4]) {
-    const uint32_t o = st & 7u;
-    const uint2* q = (const uint2*)(base + (st - o));
-    const uint2 q0 = q[0], q1 = q[1], q2 = q[2];
-    const bool hi = o >= 4u;
-    const uint32_t y0 = hi ? q0.y : q0.x, y1 = hi ? q1.x : q0.y, y2 = hi ? q1.y : q1.x, y3 = hi ? q2.x : q1.y,
-                   y4 = hi ? q2.y : q2.x;
-    const uint32_t sh = (o & 3u) * 8u;
+    const uint32_t* w = (const uint32_t*)(base + (st & ~3u));
+    const uint32_t sh = (st & 3u) * 8u;
+    const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], x3 = w[3], x4 = w[4];
     const int kb = (int)len * 8;
-    k[0] = __funnelshift_r(y0, y1, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb, 0));
-    k[1] = __funnelshift_r(y1, y2, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 32, 0));
-    k[2] = __funnelshift_r(y2, y3, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 64, 0));
-    k[3] = __funnelshift_r(y3, y4, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 96, 0));
+    k[0] = __funnelshift_r(x0, x1, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb, 0));
+    k[1] = __funnelshift_r(x1, x2, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 32, 0));
+    k[2] = __funnelshift_r(x2, x3, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 64, 0));
+    k[3] = __funnelshift_r(x3, x4, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 96, 0));
 }
 
 /* key of any len <= 32 (slow path): 9 word loads */
@@ -175,29 +172,13 @@ __device__ __forceinline__ void flush_slot(const GrepDev& P, uint32_t slot, uint
     }
 }
 
-/* Candidate slot of a key in the two buckets (first tag match), or ~0. */
-__device__ __forceinline__ uint32_t first_candidate(const uint32_t* tbl, uint32_t b1, uint32_t b2, uint32_t tag,
-                                                    uint32_t* word, bool global) {
-    const uint4 q1 = global ? __ldg((const uint4*)tbl + b1) : ((const uint4*)tbl)[b1];
-    const uint4 q2 = global ? __ldg((const uint4*)tbl + b2) : ((const uint4*)tbl)[b2];
-    const uint32_t tb = tag << GREP_TAG_SHIFT;
-    uint32_t slot = 0xFFFFFFFFu, w = 0;
-#define GR_PICK(val, s)                                                                                \
-    if ((((val) ^ tb) >> GREP_TAG_SHIFT) == 0u && slot == 0xFFFFFFFFu) { slot = (s); w = (val); }
-    GR_PICK(q1.x, 4u * b1) GR_PICK(q1.y, 4u * b1 + 1u) GR_PICK(q1.z, 4u * b1 + 2u) GR_PICK(q1.w, 4u * b1 + 3u)
-    GR_PICK(q2.x, 4u * b2) GR_PICK(q2.y, 4u * b2 + 1u) GR_PICK(q2.z, 4u * b2 + 2u) GR_PICK(q2.w, 4u * b2 + 3u)
-#undef GR_PICK
-    *word = w;
-    return slot;
-}
-
 __device__ __forceinline__ bool rec_equal(const GrepDev& P, uint32_t slot, uint32_t word, const uint32_t* k, uint32_t len) {
     const bool rlong = (word & GREP_LONG_BIT) != 0u;
     if (rlong != (len > 16u)) return false;
-    const uint4 a = __ldg(P.recs + 2u * slot);
+    const uint4 a = __ldg(P.rec_lo + slot);
     bool eq = a.x == k[0] && a.y == k[1] && a.z == k[2] && a.w == k[3];
     if (eq && rlong) {
-        const uint4 b = __ldg(P.recs + 2u * slot + 1u);
+        const uint4 b = __ldg(P.rec_hi + slot);
         eq = b.x == k[4] && b.y == k[5] && b.z == k[6] && b.w == k[7];
     }
     return eq;
@@ -205,10 +186,10 @@ __device__ __forceinline__ bool rec_equal(const GrepDev& P, uint32_t slot, uint3
 
 /* Slow, general lookup: every tag match in both buckets is verified. */
 __device__ void lookup_count(const GrepDev& P, uint32_t* tbl, bool smem, const uint32_t k[8], uint32_t len, int f) {
-    const uint32_t h1 = grep_h1(grep_mix(k, (int)len)), h2 = grep_h2(h1);
-    const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h2, b1, P.nb), tag = grep_tag(h1);
+    const uint32_t h1 = grep_h1(grep_mix(k, (int)len));
+    const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h1, P.nb), tag = grep_tag(h1, (int)len);
     const uint32_t bs[2] = {b1, b2};
-    for (int r = 0; r < 2; r++)
+    for (int r = 0; r < (b2 == b1 ? 1 : 2); r++)
         for (int i = 0; i < 4; i++) {
             const uint32_t slot = 4u * bs[r] + (uint32_t)i;
             const uint32_t w = smem ? tbl[slot] : __ldg(P.table + slot);
@@ -296,89 +277,130 @@ __device__ __forceinline__ int file_of(const GrepDev& P, uint64_t c) {
 }
 
 /* ---------------- consumer: one 512-byte segment ---------------- */
+/* Per-warp scratch: the segment's alpha bitmap (bits 0..511, then the 32
+ * bytes after the segment, then a zero word) and the list of token starts. */
+#define GR_BM_WORDS 18
+#define GR_WSCR (GR_BM_WORDS * 4 + GR_SEG) /* bytes per warp: bitmap + 256 u16 starts */
+
+/* 4-bit mask of the slots of a bucket whose 12-bit tag equals tb's */
+__device__ __forceinline__ uint32_t match4(const uint4 q, uint32_t tb) {
+    const uint32_t lim = 1u << GREP_TAG_SHIFT;
+    return ((q.x ^ tb) < lim ? 1u : 0u) | ((q.y ^ tb) < lim ? 2u : 0u) | ((q.z ^ tb) < lim ? 4u : 0u) |
+           ((q.w ^ tb) < lim ? 8u : 0u);
+}
+
+/* letters from bit r of the bitmap on: 1..32, or 33 for a run of 33+ */
+__device__ __forceinline__ uint32_t run_len(const uint32_t* bm, uint32_t r) {
+    const uint32_t w = r >> 5, b = r & 31u;
+    const uint32_t x = __funnelshift_r(bm[w], bm[w + 1], b);
+    if (x != 0xFFFFFFFFu) return (uint32_t)__popc(x & ~(x + 1u)); /* trailing ones */
+    return 32u + (__funnelshift_r(bm[w + 1], bm[w + 2], b) & 1u);
+}
+
+/* Tag candidates of a token of at most 16 letters, key k[0..3] zero padded:
+ * bit i < 4 is slot i of bucket b1, bit 4 + i slot i of bucket b2. */
+template <bool SMEM>
+__device__ __forceinline__ uint32_t cands16(const GrepDev& P, const uint32_t* tbl, const uint32_t k[4], uint32_t len,
+                                            uint32_t* b1o, uint32_t* b2o) {
+    const uint32_t a = len * 0x9E3779B1u + k[0] * 0x85EBCA77u + k[1] * 0xC2B2AE3Du + k[2] * 0x27D4EB2Fu +
+                       k[3] * 0x165667B1u; /* grep_mix for len <= 16 */
+    const uint32_t h1 = grep_h1(a);
+    const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h1, P.nb);
+    const uint32_t tb = grep_tag(h1, (int)len) << GREP_TAG_SHIFT;
+    const uint4 q1 = SMEM ? ((const uint4*)tbl)[b1] : __ldg((const uint4*)P.table + b1);
+    const uint4 q2 = SMEM ? ((const uint4*)tbl)[b2] : __ldg((const uint4*)P.table + b2);
+    *b1o = b1;
+    *b2o = b2;
+    return match4(q1, tb) | (b2 != b1 ? match4(q2, tb) << 4 : 0u);
+}
+__device__ __forceinline__ uint32_t cand_slot(uint32_t m, uint32_t b1, uint32_t b2) {
+    const uint32_t i = (uint32_t)(__ffs(m) - 1);
+    return i < 4u ? 4u * b1 + i : 4u * b2 + (i - 4u);
+}
+__device__ __forceinline__ bool key_eq(const uint4 r, const uint32_t k[4]) {
+    return r.x == k[0] && r.y == k[1] && r.z == k[2] && r.w == k[3];
+}
+
+/* a short token whose first candidate was another word: try the others
+ * (a short token's candidates are short words, so equal first 16 bytes
+ * mean equal words); returns the slot or ~0 */
+template <bool SMEM>
+__device__ __forceinline__ uint32_t other_cands16(const GrepDev& P, const uint32_t* tbl, const uint32_t* k, uint32_t len) {
+    uint32_t b1, b2;
+    const uint32_t kk[4] = {k[0], k[1], k[2], k[3]};
+    uint32_t m = cands16<SMEM>(P, tbl, kk, len, &b1, &b2);
+    for (m &= m - 1u; m; m &= m - 1u) {
+        const uint32_t c = cand_slot(m, b1, b2);
+        if (key_eq(__ldg(P.rec_lo + c), kk)) return c;
+    }
+    return 0xFFFFFFFFu;
+}
+
 template <bool SMEM>
 __device__ __forceinline__ void scan_segment(const GrepDev& P, uint32_t* tbl, const uint8_t* base, const StageDesc& d,
-                                             uint32_t segi, uint16_t* slist, uint16_t* elist) {
+                                             uint32_t segi, uint8_t* wscr) {
     const int lane = threadIdx.x & 31;
+    uint32_t* bm = (uint32_t*)wscr;
+    uint16_t* slist = (uint16_t*)(wscr + GR_BM_WORDS * 4);
     const uint32_t seg0 = segi * GR_SEG;
     const uint32_t clen = d.clen, avail = d.avail;
     if (seg0 >= clen) return;
     const uint32_t off = seg0 + 16u * (uint32_t)lane;
     const uint4 v = *(const uint4*)(base + off);
+    /* letters among the staged bytes of this file (< avail); token starts
+     * only among the chunk's own bytes (< clen) */
     uint32_t ax = alpha16(v);
     ax &= off >= avail ? 0u : (avail - off >= 16u ? 0xFFFFu : ((1u << (avail - off)) - 1u));
     const uint32_t a = ax & (off >= clen ? 0u : (clen - off >= 16u ? 0xFFFFu : ((1u << (clen - off)) - 1u)));
+    /* byte before the segment (the look-behind when seg0 == 0; nothing before
+     * the file's first byte) and the 32 bytes after it, one per lane */
+    const uint32_t before = (seg0 == 0u && d.pos == 0u) ? 0u : is_alpha(base[(int)seg0 - 1]);
     uint32_t pb = __shfl_up_sync(0xFFFFFFFFu, ax >> 15, 1);
-    if (lane == 0) pb = seg0 == 0 ? (d.pos > 0 ? is_alpha(base[-1]) : 0u) : is_alpha(base[seg0 - 1]);
-    uint32_t nx = __shfl_down_sync(0xFFFFFFFFu, ax & 1u, 1);
-    if (lane == 31) nx = seg0 + GR_SEG < avail ? is_alpha(base[seg0 + GR_SEG]) : 0u;
+    if (lane == 0) pb = before;
+    const uint32_t q = seg0 + GR_SEG + (uint32_t)lane;
+    const uint32_t cont = __ballot_sync(0xFFFFFFFFu, q < avail && is_alpha(base[q]));
+    ((uint16_t*)bm)[lane] = (uint16_t)ax;
+    if (lane == 0) {
+        bm[16] = cont;
+        bm[17] = 0u;
+    }
+    /* compact the token starts into the list */
     const uint32_t starts = a & ~((a << 1) | pb) & 0xFFFFu;
-    const uint32_t ends = a & ~((ax >> 1) | (nx << 15));
-    const uint32_t packed = (uint32_t)__popc(starts) | ((uint32_t)__popc(ends) << 16);
-    uint32_t incl = packed;
+    const uint32_t cnt = (uint32_t)__popc(starts);
+    uint32_t incl = cnt;
 #pragma unroll
     for (int dd = 1; dd < 32; dd <<= 1) {
         const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, dd);
         if (lane >= dd) incl += t;
     }
-    const uint32_t tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    const uint32_t n_s = tot & 0xFFFFu, n_e = tot >> 16;
-    uint32_t js = (incl - packed) & 0xFFFFu, je = (incl - packed) >> 16;
+    const uint32_t n_s = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    uint32_t js = incl - cnt;
     for (uint32_t m = starts; m; m &= m - 1u) slist[js++] = (uint16_t)(off + (uint32_t)(__ffs(m) - 1));
-    for (uint32_t m = ends; m; m &= m - 1u) elist[je++] = (uint16_t)(off + (uint32_t)(__ffs(m) - 1));
-    const uint32_t carry = __shfl_sync(0xFFFFFFFFu, a & pb & 1u, 0);
-    /* the last token may run past the segment: find its end in the staged
-     * bytes (chunk + look-ahead); 0xFFFF marks a run of 33+ letters */
-    if (lane == 0 && n_s + carry > n_e) {
-        const uint32_t st = 0; (void)st;
-        uint32_t q = seg0 + GR_SEG < clen ? seg0 + GR_SEG : clen;
-        const uint32_t cap = q + 33u;
-        while (q < avail && q < cap && is_alpha(base[q])) q++;
-        elist[n_e] = q >= cap ? (uint16_t)0xFFFFu : (uint16_t)(q - 1u);
-    }
     __syncwarp();
     for (uint32_t tb0 = 0; tb0 < n_s; tb0 += 64u) {
-        /* two tokens per lane: t0 and t1, straight-line so the two record
-         * loads are in flight together */
+        /* two tokens per lane, straight-line so their loads overlap */
         const uint32_t t0 = tb0 + (uint32_t)lane, t1 = t0 + 32u;
         const bool v0 = t0 < n_s, v1 = t1 < n_s;
-        uint32_t st0 = 0, st1 = 0, len0 = 0, len1 = 0;
-        if (v0) {
-            st0 = slist[t0];
-            const uint32_t e = elist[t0 + carry];
-            len0 = e == 0xFFFFu ? 33u : e - st0 + 1u;
-        }
-        if (v1) {
-            st1 = slist[t1];
-            const uint32_t e = elist[t1 + carry];
-            len1 = e == 0xFFFFu ? 33u : e - st1 + 1u;
-        }
+        const uint32_t st0 = v0 ? slist[t0] : seg0, st1 = v1 ? slist[t1] : seg0;
+        const uint32_t len0 = v0 ? run_len(bm, st0 - seg0) : 0u, len1 = v1 ? run_len(bm, st1 - seg0) : 0u;
         const bool f0 = v0 && len0 <= 16u, f1 = v1 && len1 <= 16u;
         uint32_t k0[4], k1[4];
-        key16(base, f0 ? st0 : 0u, f0 ? len0 : 0u, k0);
-        key16(base, f1 ? st1 : 0u, f1 ? len1 : 0u, k1);
-        uint32_t ka0[8] = {k0[0], k0[1], k0[2], k0[3], 0u, 0u, 0u, 0u};
-        uint32_t ka1[8] = {k1[0], k1[1], k1[2], k1[3], 0u, 0u, 0u, 0u};
-        const uint32_t h10 = grep_h1(grep_mix(ka0, (int)len0)), h11 = grep_h1(grep_mix(ka1, (int)len1));
-        const uint32_t b10 = grep_bucket(h10, P.nb), b11 = grep_bucket(h11, P.nb);
-        const uint32_t b20 = grep_b2(grep_h2(h10), b10, P.nb), b21 = grep_b2(grep_h2(h11), b11, P.nb);
-        uint32_t w0 = 0, w1 = 0;
-        const uint32_t s0 = f0 ? first_candidate(tbl, b10, b20, grep_tag(h10), &w0, !SMEM) : 0xFFFFFFFFu;
-        const uint32_t s1 = f1 ? first_candidate(tbl, b11, b21, grep_tag(h11), &w1, !SMEM) : 0xFFFFFFFFu;
-        uint4 r0 = make_uint4(0, 0, 0, 0), r1 = make_uint4(0, 0, 0, 0);
-        if (s0 != 0xFFFFFFFFu) r0 = __ldg(P.recs + 2u * s0);
-        if (s1 != 0xFFFFFFFFu) r1 = __ldg(P.recs + 2u * s1);
-        const bool m0 = s0 != 0xFFFFFFFFu && !(w0 & GREP_LONG_BIT) && r0.x == k0[0] && r0.y == k0[1] &&
-                        r0.z == k0[2] && r0.w == k0[3];
-        const bool m1 = s1 != 0xFFFFFFFFu && !(w1 & GREP_LONG_BIT) && r1.x == k1[0] && r1.y == k1[1] &&
-                        r1.z == k1[2] && r1.w == k1[3];
-        if (m0) count_hit(P, tbl, SMEM, s0, d.f);
-        if (m1) count_hit(P, tbl, SMEM, s1, d.f);
-        /* rare: a tag match that was not the word (another candidate may be);
-         * tokens of 17..32 letters; runs of 33+ letters */
-        if (f0 && s0 != 0xFFFFFFFFu && !m0) lookup_count(P, tbl, SMEM, ka0, len0, d.f);
-        if (f1 && s1 != 0xFFFFFFFFu && !m1) lookup_count(P, tbl, SMEM, ka1, len1, d.f);
-        if (v0 && len0 > 16u) {
+        key16(base, st0, f0 ? len0 : 0u, k0);
+        key16(base, st1, f1 ? len1 : 0u, k1);
+        uint32_t b10, b20, b11, b21;
+        const uint32_t m0 = f0 ? cands16<SMEM>(P, tbl, k0, len0, &b10, &b20) : 0u;
+        const uint32_t m1 = f1 ? cands16<SMEM>(P, tbl, k1, len1, &b11, &b21) : 0u;
+        uint32_t s0 = m0 ? cand_slot(m0, b10, b20) : 0xFFFFFFFFu, s1 = m1 ? cand_slot(m1, b11, b21) : 0xFFFFFFFFu;
+        const uint4 r0 = m0 ? __ldg(P.rec_lo + s0) : make_uint4(0, 0, 0, 0);
+        const uint4 r1 = m1 ? __ldg(P.rec_lo + s1) : make_uint4(0, 0, 0, 0);
+        if (m0 && !key_eq(r0, k0)) s0 = other_cands16<SMEM>(P, tbl, k0, len0);
+        if (m1 && !key_eq(r1, k1)) s1 = other_cands16<SMEM>(P, tbl, k1, len1);
+        if (s0 != 0xFFFFFFFFu) count_hit(P, tbl, SMEM, s0, d.f);
+        if (s1 != 0xFFFFFFFFu) count_hit(P, tbl, SMEM, s1, d.f);
+        const bool slow0 = v0 && len0 > 16u, slow1 = v1 && len1 > 16u;
+        /* rare: tokens of 17..32 letters take the general lookup; a run of 33+
+         * letters flags the file for the fix-up kernel */
+        if (slow0) {
             if (len0 > 32u) atomicOr(&P.long_flags[d.f], 1u);
             else {
                 uint32_t kk[8];
@@ -386,7 +408,7 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, uint32_t* tbl, co
                 lookup_count(P, tbl, SMEM, kk, len0, d.f);
             }
         }
-        if (v1 && len1 > 16u) {
+        if (slow1) {
             if (len1 > 32u) atomicOr(&P.long_flags[d.f], 1u);
             else {
                 uint32_t kk[8];
@@ -581,7 +603,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
     const uint32_t tbl_bytes = SMEM ? 16u * P.nb : 0u;
     uint32_t* tbl = SMEM ? (uint32_t*)dsm : (uint32_t*)P.table;
     uint8_t* stages = dsm + ((tbl_bytes + 127u) & ~127u);
-    uint16_t* lists = (uint16_t*)(stages + GR_STAGES * GR_STAGE);
+    uint8_t* wscr = stages + GR_STAGES * GR_STAGE + (size_t)(threadIdx.x >> 5) * GR_WSCR;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (SMEM)
@@ -608,8 +630,6 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
         producer(S, P, sh, stages, c0, c1);
         return;
     }
-    uint16_t* slist = lists + warp * 2 * GR_LIST;
-    uint16_t* elist = slist + GR_LIST;
     /* Items (chunk, segment) are taken in order from a shared counter, so a
      * warp that finishes early takes the next segment instead of idling
      * behind the slowest warp of its chunk.  A chunk has exactly GR_CONS
@@ -642,7 +662,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
         ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
         if (ok && !sh.abort) {
             const StageDesc d = sh.desc[s];
-            scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % GR_CONS, slist, elist);
+            scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % GR_CONS, wscr);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&sh.empty[s]);
@@ -782,6 +802,9 @@ void rec_key(const uint8_t* rec, uint32_t k[8], int* len) {
     *len = l;
 }
 
+/* Load 0.85: a larger table in shared memory leaves less of the SM's
+ * combined L1/shared storage to L1, which caches the records the scan
+ * verifies candidates against -- measured slower at load 0.62. */
 bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
     std::unordered_map<std::string, int> first;
     std::vector<int> uniq;
@@ -818,7 +841,7 @@ bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
                 rec_key(dict + (size_t)cur * 32, k, &len);
                 const uint32_t h1 = grep_h1(grep_mix(k, len));
                 const uint32_t b1 = grep_bucket(h1, nb);
-                uint32_t b[2] = {b1, grep_b2(grep_h2(h1), b1, nb)};
+                uint32_t b[2] = {b1, grep_b2(h1, nb)};
                 int placed = -1;
                 for (int r = 0; r < 2 && placed < 0; r++)
                     for (int i = 0; i < GREP_WAYS; i++)
@@ -848,7 +871,7 @@ bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
             int len;
             rec_key(dict + (size_t)w * 32, k, &len);
             const uint32_t h1 = grep_h1(grep_mix(k, len));
-            T.tbl[s] = (grep_tag(h1) << GREP_TAG_SHIFT) | (len > 16 ? GREP_LONG_BIT : 0u);
+            T.tbl[s] = (grep_tag(h1, len) << GREP_TAG_SHIFT) | (len > 16 ? GREP_LONG_BIT : 0u);
             memcpy(&T.recs[(size_t)s * 8], k, 32);
             T.slot_word[s] = (uint32_t)w;
         }
@@ -915,6 +938,11 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     g->ctx = ctx;
     g->n_files = n_files;
     g->n_words = (int)(st.st_size / 32); /* grep_text_gpu.cu:221 */
+    int dev = 0, sms = 0, maxsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t fixed = (size_t)GR_STAGES * GR_STAGE + (size_t)GR_CONS * GR_WSCR + 256;
     if (!build_table(dict.data(), g->n_words, g->T)) { delete g; return -GFS_ENOMEM; }
     const uint32_t nb = g->T.nb;
     /* device layout */
@@ -928,7 +956,15 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     uint8_t* b = (uint8_t*)g->dmem;
     cudaMemset(b, 0, total);
     cudaMemcpy(b + o_tbl, g->T.tbl.data(), (size_t)nb * 16, cudaMemcpyHostToDevice);
-    cudaMemcpy(b + o_recs, g->T.recs.data(), (size_t)nb * 4 * 32, cudaMemcpyHostToDevice);
+    {
+        const size_t ns = (size_t)nb * 4;
+        std::vector<uint32_t> lohi(ns * 8);
+        for (size_t i = 0; i < ns; i++) {
+            memcpy(&lohi[i * 4], &g->T.recs[i * 8], 16);
+            memcpy(&lohi[(ns + i) * 4], &g->T.recs[i * 8 + 4], 16);
+        }
+        cudaMemcpy(b + o_recs, lohi.data(), ns * 32, cudaMemcpyHostToDevice);
+    }
     cudaMemcpy(b + o_sw, g->T.slot_word.data(), (size_t)nb * 16, cudaMemcpyHostToDevice);
     if (g->n_words) cudaMemcpy(b + o_nd, g->T.next_dup.data(), (size_t)g->n_words * 4, cudaMemcpyHostToDevice);
     std::vector<char> names((size_t)n_files * GFS_NAME_MAX, 0);
@@ -942,7 +978,8 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     d.chunk_prefix = (const uint64_t*)(b + o_pf);
     d.nb = nb;
     d.table = (const uint32_t*)(b + o_tbl);
-    d.recs = (const uint4*)(b + o_recs);
+    d.rec_lo = (const uint4*)(b + o_recs);
+    d.rec_hi = d.rec_lo + (size_t)nb * 4;
     d.slot_word = (const uint32_t*)(b + o_sw);
     d.next_dup = (const int32_t*)(b + o_nd);
     d.counts = (uint32_t*)(b + o_cnt);
@@ -966,12 +1003,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     cudaMemcpy((void*)d.chunk_prefix, pf.data(), pf.size() * 8, cudaMemcpyHostToDevice);
     d.total_chunks = pf[(size_t)n_files];
     /* shared memory: table (if it fits) + stages + token lists + scratch */
-    int dev = 0, sms = 0, maxsm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     g->sms = sms;
-    size_t fixed = (size_t)GR_STAGES * GR_STAGE + (size_t)GR_CONS * 2 * GR_LIST * 2 + 256;
     size_t with_tbl = align_up((size_t)nb * 16, 128) + fixed;
     g->smem = with_tbl <= (size_t)maxsm;
     g->smem_bytes = g->smem ? with_tbl : fixed;

@@ -8,8 +8,9 @@
  * 32 bytes, NUL padded), as 8 little-endian 32-bit words.
  *
  * The hash is 32-bit integer arithmetic only (a multiply-add over the key
- * words, then two xor-shift-multiply rounds): a handful of instructions per
- * token on the GPU, where the scan is instruction-bound.
+ * words, one xor-shift-multiply round, and one more multiply for the second
+ * bucket): a handful of instructions per token on the GPU, where the scan is
+ * instruction-bound.
  */
 #ifndef GFS_GREP_COMMON_H
 #define GFS_GREP_COMMON_H
@@ -36,15 +37,15 @@ GFS_HD uint32_t grep_mix(const uint32_t k[8], int len) {
     return a;
 }
 GFS_HD uint32_t grep_h1(uint32_t a) { return (a ^ (a >> 15)) * 0x2C1B3C6Du; }
-GFS_HD uint32_t grep_h2(uint32_t h1) { return (h1 ^ (h1 >> 13)) * 0x297A2D39u; }
-GFS_HD uint32_t grep_tag(uint32_t h1) {
-    uint32_t t = h1 & 0xFFFu;
+/* 12-bit tag: 11 hash bits, and the top bit set for words of 17..32 letters,
+ * so a token of at most 16 letters never meets a longer word's slot */
+GFS_HD uint32_t grep_tag(uint32_t h1, int len) {
+    uint32_t t = (h1 & 0x7FFu) | (len > 16 ? 0x800u : 0u);
     return t ? t : 1u;
 }
 GFS_HD uint32_t grep_bucket(uint32_t h, uint32_t nb) { return (uint32_t)(((uint64_t)h * nb) >> 32); }
-GFS_HD uint32_t grep_b2(uint32_t h2, uint32_t b1, uint32_t nb) {
-    uint32_t b = grep_bucket(h2, nb);
-    return b == b1 ? (b1 + 1u == nb ? 0u : b1 + 1u) : b;
-}
+/* second bucket: the top bits of another multiple of h1 (it may equal the
+ * first; the table builder then has only one bucket for the word) */
+GFS_HD uint32_t grep_b2(uint32_t h1, uint32_t nb) { return grep_bucket(h1 * 0x85EBCA6Bu, nb); }
 
 #endif
