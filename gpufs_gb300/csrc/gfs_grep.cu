@@ -58,7 +58,7 @@
 #define GR_LB 16                      /* look-behind bytes staged before a chunk */
 #define GR_LA 64                      /* look-ahead bytes staged after it */
 #define GR_STAGE (GR_LB + GR_CH + GR_LA + 32)
-#define GR_STAGES 4
+#define GR_STAGES 3
 #define GR_WIN 32                     /* pages per window, incl. look-behind/ahead */
 
 extern __device__ gfs_state* g_gfs;
@@ -71,7 +71,7 @@ struct GrepDev {
     const uint64_t* chunk_prefix; /* n_files + 1, in GR_CH chunks */
     uint64_t total_chunks;
     uint32_t nb;                  /* buckets */
-    const uint32_t* table;        /* nb * 4 slot words: tag << 20 | long << 19 */
+    const uint16_t* tags;         /* nb * 4 slot tags (grep_tag), 0 = empty */
     const uint4* rec_lo;          /* nb * 4: bytes 0..15 of each slot's record */
     const uint4* rec_hi;          /* nb * 4: bytes 16..31 (separate, so the short-word
                                      probes touch half the bytes) */
@@ -172,8 +172,7 @@ __device__ __forceinline__ void flush_slot(const GrepDev& P, uint32_t slot, uint
     }
 }
 
-__device__ __forceinline__ bool rec_equal(const GrepDev& P, uint32_t slot, uint32_t word, const uint32_t* k, uint32_t len) {
-    const bool rlong = (word & GREP_LONG_BIT) != 0u;
+__device__ __forceinline__ bool rec_equal(const GrepDev& P, uint32_t slot, bool rlong, const uint32_t* k, uint32_t len) {
     if (rlong != (len > 16u)) return false;
     const uint4 a = __ldg(P.rec_lo + slot);
     bool eq = a.x == k[0] && a.y == k[1] && a.z == k[2] && a.w == k[3];
@@ -184,40 +183,35 @@ __device__ __forceinline__ bool rec_equal(const GrepDev& P, uint32_t slot, uint3
     return eq;
 }
 
+/* The dictionary table a scan works with: slot tags, and (table in shared
+ * memory) one 32-bit counter per slot for the current file.  Without shared
+ * memory counts go straight to the global count matrix. */
+struct Tbl {
+    const uint16_t* tags;
+    uint32_t* cnt;
+};
+
+/* A slot counter holds one CTA's count of one word in one file, which the
+ * uint32 count matrix bounds anyway: a plain add, no overflow check. */
+__device__ __forceinline__ void count_hit(const GrepDev& P, const Tbl& t, bool smem, uint32_t slot, int f) {
+    if (smem) atomicAdd(&t.cnt[slot], 1u);
+    else flush_slot(P, slot, 1u, f);
+}
+
 /* Slow, general lookup: every tag match in both buckets is verified. */
-__device__ void lookup_count(const GrepDev& P, uint32_t* tbl, bool smem, const uint32_t k[8], uint32_t len, int f) {
+__device__ void lookup_count(const GrepDev& P, const Tbl& t, bool smem, const uint32_t k[8], uint32_t len, int f) {
     const uint32_t h1 = grep_h1(grep_mix(k, (int)len));
     const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h1, P.nb), tag = grep_tag(h1, (int)len);
     const uint32_t bs[2] = {b1, b2};
     for (int r = 0; r < (b2 == b1 ? 1 : 2); r++)
         for (int i = 0; i < 4; i++) {
             const uint32_t slot = 4u * bs[r] + (uint32_t)i;
-            const uint32_t w = smem ? tbl[slot] : __ldg(P.table + slot);
-            if ((w >> GREP_TAG_SHIFT) != tag) continue;
-            if (!rec_equal(P, slot, w, k, len)) continue;
-            if (smem) {
-                const uint32_t old = atomicAdd(&tbl[slot], 1u);
-                if ((old & GREP_CNT_MASK) == GREP_CNT_FLUSH - 1u) {
-                    atomicSub(&tbl[slot], GREP_CNT_FLUSH);
-                    flush_slot(P, slot, GREP_CNT_FLUSH, f);
-                }
-            } else {
-                flush_slot(P, slot, 1u, f);
-            }
+            const uint32_t tg = t.tags[slot];
+            if (tg != tag) continue;
+            if (!rec_equal(P, slot, (tg & GREP_TAG_LONG) != 0u, k, len)) continue;
+            count_hit(P, t, smem, slot, f);
             return;
         }
-}
-
-__device__ __forceinline__ void count_hit(const GrepDev& P, uint32_t* tbl, bool smem, uint32_t slot, int f) {
-    if (smem) {
-        const uint32_t old = atomicAdd(&tbl[slot], 1u);
-        if ((old & GREP_CNT_MASK) == GREP_CNT_FLUSH - 1u) {
-            atomicSub(&tbl[slot], GREP_CNT_FLUSH);
-            flush_slot(P, slot, GREP_CNT_FLUSH, f);
-        }
-    } else {
-        flush_slot(P, slot, 1u, f);
-    }
 }
 
 struct StageDesc {
@@ -282,11 +276,13 @@ __device__ __forceinline__ int file_of(const GrepDev& P, uint64_t c) {
 #define GR_BM_WORDS 18
 #define GR_WSCR (GR_BM_WORDS * 4 + GR_SEG) /* bytes per warp: bitmap + 256 u16 starts */
 
-/* 4-bit mask of the slots of a bucket whose 12-bit tag equals tb's */
-__device__ __forceinline__ uint32_t match4(const uint4 q, uint32_t tb) {
-    const uint32_t lim = 1u << GREP_TAG_SHIFT;
-    return ((q.x ^ tb) < lim ? 1u : 0u) | ((q.y ^ tb) < lim ? 2u : 0u) | ((q.z ^ tb) < lim ? 4u : 0u) |
-           ((q.w ^ tb) < lim ? 8u : 0u);
+/* Bit 15 / bit 31 set where the low / high 16-bit tag of w equals the
+ * token's (tt = tag in both halves).  Exact for the low half; the high half
+ * can read as a match when the low half matches too, which the record check
+ * and the exact candidate loop absorb. */
+__device__ __forceinline__ uint32_t z16(uint32_t w, uint32_t tt) {
+    const uint32_t x = w ^ tt;
+    return (x - 0x00010001u) & ~x & 0x80008000u;
 }
 
 /* letters from bit r of the bitmap on: 1..32, or 33 for a run of 33+ */
@@ -298,46 +294,50 @@ __device__ __forceinline__ uint32_t run_len(const uint32_t* bm, uint32_t r) {
 }
 
 /* Tag candidates of a token of at most 16 letters, key k[0..3] zero padded:
- * bit i < 4 is slot i of bucket b1, bit 4 + i slot i of bucket b2. */
-template <bool SMEM>
-__device__ __forceinline__ uint32_t cands16(const GrepDev& P, const uint32_t* tbl, const uint32_t k[4], uint32_t len,
+ * a mask with bits 31/15 (bucket b1 slots 1/0), 30/14 (b1 slots 3/2),
+ * 29/13 (b2 slots 1/0) and 28/12 (b2 slots 3/2). */
+__device__ __forceinline__ uint32_t cands16(const GrepDev& P, const Tbl& t, const uint32_t k[4], uint32_t len,
                                             uint32_t* b1o, uint32_t* b2o) {
     const uint32_t a = len * 0x9E3779B1u + k[0] * 0x85EBCA77u + k[1] * 0xC2B2AE3Du + k[2] * 0x27D4EB2Fu +
                        k[3] * 0x165667B1u; /* grep_mix for len <= 16 */
     const uint32_t h1 = grep_h1(a);
     const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h1, P.nb);
-    const uint32_t tb = grep_tag(h1, (int)len) << GREP_TAG_SHIFT;
-    const uint4 q1 = SMEM ? ((const uint4*)tbl)[b1] : __ldg((const uint4*)P.table + b1);
-    const uint4 q2 = SMEM ? ((const uint4*)tbl)[b2] : __ldg((const uint4*)P.table + b2);
+    const uint32_t tt = grep_tag(h1, (int)len) * 0x00010001u;
+    const uint2 q1 = ((const uint2*)t.tags)[b1];
+    const uint2 q2 = ((const uint2*)t.tags)[b2];
     *b1o = b1;
     *b2o = b2;
-    return match4(q1, tb) | (b2 != b1 ? match4(q2, tb) << 4 : 0u);
+    uint32_t m = z16(q1.x, tt) | (z16(q1.y, tt) >> 1);
+    if (b2 != b1) m |= (z16(q2.x, tt) >> 2) | (z16(q2.y, tt) >> 3);
+    return m;
 }
+/* slot of the candidate at the highest set bit of m */
 __device__ __forceinline__ uint32_t cand_slot(uint32_t m, uint32_t b1, uint32_t b2) {
-    const uint32_t i = (uint32_t)(__ffs(m) - 1);
-    return i < 4u ? 4u * b1 + i : 4u * b2 + (i - 4u);
+    const uint32_t p = 31u - (uint32_t)__clz(m);
+    const uint32_t w = (15u - (p & 15u)) & 3u;
+    return 4u * (w < 2u ? b1 : b2) + ((w & 1u) << 1) + (p >> 4);
 }
 __device__ __forceinline__ bool key_eq(const uint4 r, const uint32_t k[4]) {
     return r.x == k[0] && r.y == k[1] && r.z == k[2] && r.w == k[3];
 }
 
-/* a short token whose first candidate was another word: try the others
- * (a short token's candidates are short words, so equal first 16 bytes
- * mean equal words); returns the slot or ~0 */
-template <bool SMEM>
-__device__ __forceinline__ uint32_t other_cands16(const GrepDev& P, const uint32_t* tbl, const uint32_t* k, uint32_t len) {
-    uint32_t b1, b2;
+/* a short token whose first candidate was not the word: check every slot
+ * of both buckets exactly (a short token's candidates are short words, so
+ * equal first 16 bytes mean equal words); returns the slot or ~0 */
+__device__ __forceinline__ uint32_t other_cands16(const GrepDev& P, const Tbl& t, const uint32_t* k, uint32_t len) {
     const uint32_t kk[4] = {k[0], k[1], k[2], k[3]};
-    uint32_t m = cands16<SMEM>(P, tbl, kk, len, &b1, &b2);
-    for (m &= m - 1u; m; m &= m - 1u) {
-        const uint32_t c = cand_slot(m, b1, b2);
-        if (key_eq(__ldg(P.rec_lo + c), kk)) return c;
+    const uint32_t h1 = grep_h1(len * 0x9E3779B1u + kk[0] * 0x85EBCA77u + kk[1] * 0xC2B2AE3Du +
+                                kk[2] * 0x27D4EB2Fu + kk[3] * 0x165667B1u);
+    const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h1, P.nb), tag = grep_tag(h1, (int)len);
+    for (uint32_t j = 0; j < 8u; j++) {
+        const uint32_t c = 4u * (j < 4u ? b1 : b2) + (j & 3u);
+        if (t.tags[c] == tag && key_eq(__ldg(P.rec_lo + c), kk)) return c;
     }
     return 0xFFFFFFFFu;
 }
 
 template <bool SMEM>
-__device__ __forceinline__ void scan_segment(const GrepDev& P, uint32_t* tbl, const uint8_t* base, const StageDesc& d,
+__device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, const uint8_t* base, const StageDesc& d,
                                              uint32_t segi, uint8_t* wscr) {
     const int lane = threadIdx.x & 31;
     uint32_t* bm = (uint32_t*)wscr;
@@ -388,13 +388,13 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, uint32_t* tbl, co
         key16(base, st0, f0 ? len0 : 0u, k0);
         key16(base, st1, f1 ? len1 : 0u, k1);
         uint32_t b10, b20, b11, b21;
-        const uint32_t m0 = f0 ? cands16<SMEM>(P, tbl, k0, len0, &b10, &b20) : 0u;
-        const uint32_t m1 = f1 ? cands16<SMEM>(P, tbl, k1, len1, &b11, &b21) : 0u;
+        const uint32_t m0 = f0 ? cands16(P, tbl, k0, len0, &b10, &b20) : 0u;
+        const uint32_t m1 = f1 ? cands16(P, tbl, k1, len1, &b11, &b21) : 0u;
         uint32_t s0 = m0 ? cand_slot(m0, b10, b20) : 0xFFFFFFFFu, s1 = m1 ? cand_slot(m1, b11, b21) : 0xFFFFFFFFu;
         const uint4 r0 = m0 ? __ldg(P.rec_lo + s0) : make_uint4(0, 0, 0, 0);
         const uint4 r1 = m1 ? __ldg(P.rec_lo + s1) : make_uint4(0, 0, 0, 0);
-        if (m0 && !key_eq(r0, k0)) s0 = other_cands16<SMEM>(P, tbl, k0, len0);
-        if (m1 && !key_eq(r1, k1)) s1 = other_cands16<SMEM>(P, tbl, k1, len1);
+        if (m0 && !key_eq(r0, k0)) s0 = other_cands16(P, tbl, k0, len0);
+        if (m1 && !key_eq(r1, k1)) s1 = other_cands16(P, tbl, k1, len1);
         if (s0 != 0xFFFFFFFFu) count_hit(P, tbl, SMEM, s0, d.f);
         if (s1 != 0xFFFFFFFFu) count_hit(P, tbl, SMEM, s1, d.f);
         const bool slow0 = v0 && len0 > 16u, slow1 = v1 && len1 > 16u;
@@ -420,14 +420,13 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, uint32_t* tbl, co
 }
 
 template <bool SMEM>
-__device__ void flush_counts(const GrepDev& P, uint32_t* tbl, int f) {
+__device__ void flush_counts(const GrepDev& P, const Tbl& t, int f) {
     if (!SMEM) return;
     const uint32_t nslots = 4u * P.nb;
     for (uint32_t i = threadIdx.x; i < nslots; i += GR_CONS * 32) {
-        const uint32_t v = tbl[i];
-        const uint32_t n = v & GREP_CNT_MASK;
+        const uint32_t n = t.cnt[i];
         if (n) {
-            tbl[i] = v & ~GREP_CNT_MASK;
+            t.cnt[i] = 0u;
             flush_slot(P, i, n, f);
         }
     }
@@ -600,14 +599,22 @@ template <bool SMEM>
 __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepDev P) {
     extern __shared__ __align__(128) uint8_t dsm[];
     __shared__ Shared sh;
-    const uint32_t tbl_bytes = SMEM ? 16u * P.nb : 0u;
-    uint32_t* tbl = SMEM ? (uint32_t*)dsm : (uint32_t*)P.table;
-    uint8_t* stages = dsm + ((tbl_bytes + 127u) & ~127u);
+    /* shared memory: slot tags (8 B per bucket), slot counters (16 B per
+     * bucket), the stage ring, per-warp scratch */
+    const uint32_t tag_bytes = SMEM ? (8u * P.nb + 127u) & ~127u : 0u;
+    const uint32_t tbl_bytes = SMEM ? tag_bytes + ((16u * P.nb + 127u) & ~127u) : 0u;
+    Tbl tbl;
+    tbl.tags = SMEM ? (const uint16_t*)dsm : P.tags;
+    tbl.cnt = SMEM ? (uint32_t*)(dsm + tag_bytes) : nullptr;
+    uint8_t* stages = dsm + tbl_bytes;
     uint8_t* wscr = stages + GR_STAGES * GR_STAGE + (size_t)(threadIdx.x >> 5) * GR_WSCR;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (SMEM)
-        for (uint32_t i = threadIdx.x; i < P.nb; i += blockDim.x) ((uint4*)tbl)[i] = __ldg((const uint4*)P.table + i);
+        for (uint32_t i = threadIdx.x; i < P.nb; i += blockDim.x) {
+            ((uint2*)dsm)[i] = __ldg((const uint2*)P.tags + i);
+            ((uint4*)tbl.cnt)[i] = make_uint4(0u, 0u, 0u, 0u);
+        }
     if (threadIdx.x == 0) {
         for (int s = 0; s < GR_STAGES; s++) {
             mbar_init(&sh.full[s], 1u);
@@ -708,7 +715,10 @@ __device__ void count_piece(const GrepDev& P, PageCursor& pc, uint64_t a, uint64
     for (int i = 0; i < 8; i++)
         k[i] = (uint32_t)buf[4 * i] | ((uint32_t)buf[4 * i + 1] << 8) | ((uint32_t)buf[4 * i + 2] << 16) |
                ((uint32_t)buf[4 * i + 3] << 24);
-    lookup_count(P, nullptr, false, k, (uint32_t)len, f);
+    Tbl t;
+    t.tags = P.tags;
+    t.cnt = nullptr;
+    lookup_count(P, t, false, k, (uint32_t)len, f);
 }
 } // namespace
 
@@ -785,7 +795,7 @@ namespace {
 
 struct HostTable {
     uint32_t nb = 0;
-    std::vector<uint32_t> tbl;       /* nb*4 */
+    std::vector<uint16_t> tags;      /* nb*4 slot tags */
     std::vector<uint32_t> recs;      /* nb*4*8 */
     std::vector<uint32_t> slot_word; /* nb*4 */
     std::vector<int32_t> next_dup;   /* n_words */
@@ -802,9 +812,10 @@ void rec_key(const uint8_t* rec, uint32_t k[8], int* len) {
     *len = l;
 }
 
-/* Load 0.85: a larger table in shared memory leaves less of the SM's
- * combined L1/shared storage to L1, which caches the records the scan
- * verifies candidates against -- measured slower at load 0.62. */
+/* Load 0.92: the table lives in shared memory, and the less of the SM's
+ * combined L1/shared storage it takes, the more L1 is left to cache the
+ * records the scan verifies candidates against (measured: lower loads were
+ * slower).  16-bit tags keep false candidates rare at this load. */
 bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
     std::unordered_map<std::string, int> first;
     std::vector<int> uniq;
@@ -827,7 +838,7 @@ bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
             last[(size_t)h] = w;
         }
     }
-    uint32_t nb = (uint32_t)((double)uniq.size() / (GREP_WAYS * 0.85)) + 16u;
+    uint32_t nb = (uint32_t)((double)uniq.size() / (GREP_WAYS * 0.92)) + 16u;
     for (int attempt = 0; attempt < 20; attempt++, nb = nb + nb / 8u + 1u) {
         std::vector<int> slot_of(nb * GREP_WAYS, -1);
         uint64_t rng = 0x243F6A8885A308D3ULL ^ nb;
@@ -861,7 +872,7 @@ bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
         }
         if (!ok) continue;
         T.nb = nb;
-        T.tbl.assign(nb * GREP_WAYS, 0u);
+        T.tags.assign(nb * GREP_WAYS, 0u);
         T.recs.assign((size_t)nb * GREP_WAYS * 8, 0u);
         T.slot_word.assign(nb * GREP_WAYS, 0xFFFFFFFFu);
         for (uint32_t s = 0; s < nb * GREP_WAYS; s++) {
@@ -871,7 +882,7 @@ bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
             int len;
             rec_key(dict + (size_t)w * 32, k, &len);
             const uint32_t h1 = grep_h1(grep_mix(k, len));
-            T.tbl[s] = (grep_tag(h1, len) << GREP_TAG_SHIFT) | (len > 16 ? GREP_LONG_BIT : 0u);
+            T.tags[s] = (uint16_t)grep_tag(h1, len);
             memcpy(&T.recs[(size_t)s * 8], k, 32);
             T.slot_word[s] = (uint32_t)w;
         }
@@ -946,7 +957,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     if (!build_table(dict.data(), g->n_words, g->T)) { delete g; return -GFS_ENOMEM; }
     const uint32_t nb = g->T.nb;
     /* device layout */
-    size_t o_tbl = 0, o_recs = align_up(o_tbl + (size_t)nb * 16, 256), o_sw = align_up(o_recs + (size_t)nb * 4 * 32, 256),
+    size_t o_tbl = 0, o_recs = align_up(o_tbl + (size_t)nb * 8, 256), o_sw = align_up(o_recs + (size_t)nb * 4 * 32, 256),
            o_nd = align_up(o_sw + (size_t)nb * 16, 256), o_cnt = align_up(o_nd + (size_t)g->n_words * 4 + 4, 256),
            o_fds = align_up(o_cnt + (size_t)g->n_words * n_files * 4 + 4, 256), o_sz = align_up(o_fds + (size_t)n_files * 4, 256),
            o_pf = align_up(o_sz + (size_t)n_files * 8, 256), o_fl = align_up(o_pf + (size_t)(n_files + 1) * 8, 256),
@@ -955,7 +966,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     if (cudaMalloc(&g->dmem, total) != cudaSuccess) { delete g; return -GFS_ENOMEM; }
     uint8_t* b = (uint8_t*)g->dmem;
     cudaMemset(b, 0, total);
-    cudaMemcpy(b + o_tbl, g->T.tbl.data(), (size_t)nb * 16, cudaMemcpyHostToDevice);
+    cudaMemcpy(b + o_tbl, g->T.tags.data(), (size_t)nb * 8, cudaMemcpyHostToDevice);
     {
         const size_t ns = (size_t)nb * 4;
         std::vector<uint32_t> lohi(ns * 8);
@@ -977,7 +988,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     d.sizes = (const uint64_t*)(b + o_sz);
     d.chunk_prefix = (const uint64_t*)(b + o_pf);
     d.nb = nb;
-    d.table = (const uint32_t*)(b + o_tbl);
+    d.tags = (const uint16_t*)(b + o_tbl);
     d.rec_lo = (const uint4*)(b + o_recs);
     d.rec_hi = d.rec_lo + (size_t)nb * 4;
     d.slot_word = (const uint32_t*)(b + o_sw);
@@ -1004,7 +1015,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     d.total_chunks = pf[(size_t)n_files];
     /* shared memory: table (if it fits) + stages + token lists + scratch */
     g->sms = sms;
-    size_t with_tbl = align_up((size_t)nb * 16, 128) + fixed;
+    size_t with_tbl = align_up((size_t)nb * 8, 128) + align_up((size_t)nb * 16, 128) + fixed;
     g->smem = with_tbl <= (size_t)maxsm;
     g->smem_bytes = g->smem ? with_tbl : fixed;
     cudaFuncSetAttribute(k_grep_scan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);

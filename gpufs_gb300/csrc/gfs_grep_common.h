@@ -23,11 +23,8 @@
 #define GFS_HD static inline
 #endif
 
-#define GREP_WAYS 4        /* slots per bucket (16 bytes) */
-#define GREP_TAG_SHIFT 20  /* slot word: tag:12 << 20 | long:1 << 19 | count:19 */
-#define GREP_LONG_BIT 0x80000u
-#define GREP_CNT_MASK 0x7FFFFu
-#define GREP_CNT_FLUSH 0x40000u /* a counter is flushed to global memory at 2^18 */
+#define GREP_WAYS 4         /* slots per bucket */
+#define GREP_TAG_LONG 0x8000u /* tag bit: the word has 17..32 letters */
 
 /* key words k[0..7], len in 1..32 */
 GFS_HD uint32_t grep_mix(const uint32_t k[8], int len) {
@@ -37,10 +34,11 @@ GFS_HD uint32_t grep_mix(const uint32_t k[8], int len) {
     return a;
 }
 GFS_HD uint32_t grep_h1(uint32_t a) { return (a ^ (a >> 15)) * 0x2C1B3C6Du; }
-/* 12-bit tag: 11 hash bits, and the top bit set for words of 17..32 letters,
- * so a token of at most 16 letters never meets a longer word's slot */
+/* 16-bit slot tag, never 0 (0 marks an empty slot): 15 hash bits, and the
+ * top bit set for words of 17..32 letters, so a token of at most 16 letters
+ * never meets a longer word's slot */
 GFS_HD uint32_t grep_tag(uint32_t h1, int len) {
-    uint32_t t = (h1 & 0x7FFu) | (len > 16 ? 0x800u : 0u);
+    uint32_t t = (h1 & 0x7FFFu) | (len > 16 ? GREP_TAG_LONG : 0u);
     return t ? t : 1u;
 }
 GFS_HD uint32_t grep_bucket(uint32_t h, uint32_t nb) { return (uint32_t)(((uint64_t)h * nb) >> 32); }
