@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-extra", action="store_true", help="skip the link-bandwidth measurement")
     ap.add_argument("--corpus-mb", type=int, default=TOTAL_BYTES >> 20,
                     help="smaller corpora are for profiling only; the benchmark is 1024")
+    ap.add_argument("--workload", default="grep_text", choices=["grep_text", "gread", "memcopy", "bigmatrix"],
+                    help="grep_text is the benchmark line; the others measure the other configurations")
     return ap.parse_args()
 
 
@@ -228,6 +230,9 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, ws, td, data_dir)
         return
+    if args.workload != "grep_text":
+        run_workload(args, rank, ws, local, td, data_dir)
+        return
     import __graft_entry__
     total_bytes = args.corpus_mb << 20
     if rank == 0:
@@ -331,6 +336,274 @@ def main():
         "extra": dict(extra, **{"cache_stats": {k: st[k] for k in ("misses", "evictions", "host_read_bytes")}}),
     }
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# the other configurations: gread, memcopy, bigmatrix_mmap
+# ---------------------------------------------------------------------------
+def _stamped(d, name, want, make):
+    """Generate an input once per data directory (seeded, so reruns agree)."""
+    os.makedirs(d, exist_ok=True)
+    path = os.path.join(d, name)
+    stamp = path + ".stamp"
+    if not (os.path.exists(path) and os.path.exists(stamp) and open(stamp).read() == want):
+        make(path)
+        with open(stamp, "w") as f:
+            f.write(want)
+    return path
+
+
+def _cpu_pread_gbs(path, chunk, nt, reps=2):
+    """All-threads host pread of a whole file in `chunk` pieces (GB/s, best of reps)."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    size = os.path.getsize(path)
+    buf = np.empty(size, dtype=np.uint8)
+    mv = memoryview(buf)
+
+    def part(i):
+        fd = os.open(path, os.O_RDONLY)
+        try:
+            for off in range(i * chunk, size, nt * chunk):
+                n = min(chunk, size - off)
+                os.preadv(fd, [mv[off:off + n]], off)
+        finally:
+            os.close(fd)
+    best = None
+    with ThreadPoolExecutor(nt) as ex:
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            list(ex.map(part, range(nt)))
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+    return size / best / 1e9
+
+
+def _cpu_copy_gbs(src, dst, chunk, nt):
+    """All-threads host pread/pwrite copy of src to a new dst (GB/s of file)."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    size = os.path.getsize(src)
+    if os.path.exists(dst):
+        os.unlink(dst)
+    fd_out = os.open(dst, os.O_WRONLY | os.O_CREAT, 0o644)
+    os.ftruncate(fd_out, size)
+
+    def part(i):
+        fd = os.open(src, os.O_RDONLY)
+        b = np.empty(chunk, dtype=np.uint8)
+        try:
+            for off in range(i * chunk, size, nt * chunk):
+                n = os.preadv(fd, [memoryview(b)[:min(chunk, size - off)]], off)
+                os.pwrite(fd_out, memoryview(b)[:n], off)
+        finally:
+            os.close(fd)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(nt) as ex:
+        list(ex.map(part, range(nt)))
+    dt = time.perf_counter() - t0
+    os.close(fd_out)
+    os.unlink(dst)
+    return size / dt / 1e9
+
+
+def run_workload(args, rank, ws, local, td, data_dir):
+    import __graft_entry__
+    if rank == 0:
+        __graft_entry__.build()
+    barrier(td)
+    if rank != 0:
+        __graft_entry__.build()
+    import numpy as np
+    import gpufs_gb300 as g
+    from gpufs_gb300 import datagen
+    nt = cpu_threads()
+    workers = max(4, min(32, nt))
+    hbm, how = peaks()
+    d = data_dir + "_" + args.workload
+    steps, warm = args.steps, max(3, args.warmup)
+    extra = {}
+    link = None
+    if not args.no_extra:
+        link = g.measure_link(1 << 30, 5)
+        extra["link_h2d_gbs"], extra["link_d2h_gbs"] = link
+    clk = Clocks(local)
+    if args.workload == "gread":
+        size = 1 << 30
+        src = _stamped(d, "f.bin", "uniform %d 7" % size, lambda p: datagen.uniform_bytes(p, size, seed=7))
+        page = 1 << args.log_page
+        sess = g.Session(log_page=args.log_page, pool_bytes=size + (256 << 20), max_files=64, host_workers=workers,
+                         staging_depth=4, timeout_s=60, device=local)
+        import torch
+        dev = torch.empty(size, dtype=torch.uint8, device="cuda:%d" % local)
+        nblocks, nthreads = size // page if size // page <= 4096 else 4096, 1024
+        clk.start()
+        sess.pread_dev(src, 0, size, dev.data_ptr(), nblocks, nthreads)  # loads the cache
+        for _ in range(warm):
+            sess.pread_dev(src, 0, size, dev.data_ptr(), nblocks, nthreads)
+        ks = [sess.pread_dev(src, 0, size, dev.data_ptr(), nblocks, nthreads)[1] for _ in range(steps)]
+        kms = allmax(td, sum(ks) / len(ks))
+        want = oracle_xxh64_file(src)
+        ok = bool(oracle_xxh64_bytes(dev.cpu().numpy()) == want)
+        host = np.empty(size, dtype=np.uint8)
+        e2e = []
+        for i in range(warm + max(2, min(steps, 5))):
+            sess.drop_cache()
+            t0 = time.perf_counter()
+            n = sess.L.gfs_pread(sess.handle, src.encode(), 0, size, host.ctypes.data, nblocks, nthreads)
+            dt = time.perf_counter() - t0
+            if n != size:
+                raise RuntimeError("gfs_pread returned %d" % n)
+            if i >= warm:
+                e2e.append(dt)
+        ok = ok and bool(oracle_xxh64_bytes(host) == want)
+        e2e_t = allmax(td, sum(e2e) / len(e2e))
+        clocks = clk.stop()
+        sess.close()
+        cpu = {"value": _cpu_pread_gbs(src, page, nt), "unit": "GB/s", "cores": nt, "kind": "port",
+               "sample": "host pread of the whole 1 GiB file in page-sized pieces, all threads, best of 2"} \
+            if rank == 0 and not args.no_cpu else None
+        achieved = 2 * size / (kms * 1e-3) / 1e9
+        line = {"metric": METRIC, "value": ws * size / (kms * 1e-3) / 1e9, "unit": "GB/s", "n_gpus": ws,
+                "steps": steps, "warmup": warm, "ms_per_step": kms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u8", "data": "synthetic: seeded uniform random bytes",
+                "config": {"workload": "gread: one 1 GiB file read into a device buffer through gopen/gread/gclose",
+                           "page_bytes": page, "blocks": nblocks, "threads": nthreads,
+                           "l2": "1 GiB > 129 MB L2 (no flush needed)"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                             "frac": achieved / hbm, "peak_source": how, "traffic": None, "kernel": "k_pread",
+                             "algorithmic_bytes_per_launch": 2 * size, "mean_launch_ms": kms},
+                "cpu_baseline": cpu,
+                "e2e": {"value": ws * size / e2e_t / 1e9, "unit": "GB/s", "h2d_bytes_per_step": size,
+                        "d2h_bytes_per_step": size, "ms_per_step": e2e_t * 1e3,
+                        "call": "gfs_pread into a host buffer, cold buffer cache",
+                        "over_link_h2d": (size / e2e_t / 1e9) / link[0] if link else None},
+                "gpu_launches": steps, "clocks": clocks, "parity": {"bytes_equal_file": ok}, "extra": extra}
+    elif args.workload == "memcopy":
+        size = 512 << 20
+        src = _stamped(d, "src.bin", "uniform %d 0x6770756673" % size,
+                       lambda p: datagen.uniform_bytes(p, size, seed=0x6770756673))
+        dst = os.path.join(d, "dst.bin")
+        sess = g.Session(log_page=16, pool_bytes=(2 * size) + (256 << 20), max_files=64, host_workers=workers,
+                         staging_depth=4, timeout_s=60, device=local)
+        clk.start()
+        want = oracle_xxh64_file(src)
+
+        def once(mode):
+            if os.path.exists(dst):
+                os.unlink(dst)
+            t0 = time.perf_counter()
+            ms = sess.memcopy(src, dst, 112, 256, mode)
+            return ms, time.perf_counter() - t0
+        for _ in range(warm):
+            once(0)
+        ks = [once(0)[0] for _ in range(steps)]
+        kms = allmax(td, sum(ks) / len(ks))
+        ok = oracle_xxh64_file(dst) == want
+        k1 = [once(1)[0] for _ in range(steps)]
+        ok = ok and oracle_xxh64_file(dst) == want
+        e2e = []
+        for i in range(1 + max(2, min(steps, 5))):
+            sess.drop_cache()
+            ms, dt = once(0)
+            if i >= 1:
+                e2e.append(dt)
+        ok = ok and oracle_xxh64_file(dst) == want
+        e2e_t = allmax(td, sum(e2e) / len(e2e))
+        clocks = clk.stop()
+        sess.close()
+        cpu = {"value": _cpu_copy_gbs(src, dst, 64 << 10, nt), "unit": "GB/s", "cores": nt, "kind": "port",
+               "sample": "host pread/pwrite copy of the 512 MiB file in 64 KiB pieces to a new file, all threads"} \
+            if rank == 0 and not args.no_cpu else None
+        achieved = size / (kms * 1e-3) / 1e9
+        extra["mode1_gmmap_ms"] = sum(k1) / len(k1)
+        line = {"metric": METRIC, "value": ws * size / (kms * 1e-3) / 1e9, "unit": "GB/s", "n_gpus": ws,
+                "steps": steps, "warmup": warm, "ms_per_step": kms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u8", "data": "synthetic: seeded uniform random bytes",
+                "config": {"workload": "memcopy: one 512 MiB file copied to a new file by 112 blocks x 256 threads "
+                                       "with gread/gwrite in 64 KiB pages (source resident in the buffer cache; the "
+                                       "copy is written back to the host file at gclose)", "page_bytes": 65536},
+                "roofline": {"bound": "link", "achieved": achieved, "peak": link[1] if link else None,
+                             "unit": "GB/s", "frac": achieved / link[1] if link else None,
+                             "peak_source": "measured pinned D2H", "traffic": None, "kernel": "k_memcopy",
+                             "algorithmic_bytes_per_launch": size, "mean_launch_ms": kms},
+                "cpu_baseline": cpu,
+                "e2e": {"value": ws * size / e2e_t / 1e9, "unit": "GB/s", "h2d_bytes_per_step": size,
+                        "d2h_bytes_per_step": size, "ms_per_step": e2e_t * 1e3,
+                        "call": "gfs_memcopy, cold buffer cache, new destination file"},
+                "gpu_launches": steps, "clocks": clocks, "parity": {"xxh64_equal": bool(ok)}, "extra": extra}
+    else:  # bigmatrix
+        rows, cols = 16384, 65536
+        vp = _stamped(d, "vec.f32", "n %d 11" % cols, lambda p: datagen.normal_f32(p, cols, seed=11))
+        mp = _stamped(d, "mat.f32", "n %d 12" % (rows * cols), lambda p: datagen.normal_f32(p, rows * cols, seed=12))
+        op = os.path.join(d, "out.f32")
+        mbytes = rows * cols * 4
+        sess = g.Session(log_page=21, pool_bytes=mbytes + (512 << 20), max_files=64, host_workers=workers,
+                         staging_depth=4, timeout_s=120, device=local)
+        nblocks, nthreads = 152, 1024  # one wave: every block holds the files open for the whole launch
+        clk.start()
+        for _ in range(warm):
+            sess.bigmatrix(vp, mp, op, nblocks, nthreads)
+        ks = [sess.bigmatrix(vp, mp, op, nblocks, nthreads) for _ in range(steps)]
+        kms = allmax(td, sum(ks) / len(ks))
+        y = np.fromfile(op, dtype=np.float32)
+        e2e = []
+        for i in range(1 + 2):
+            sess.drop_cache()
+            t0 = time.perf_counter()
+            sess.bigmatrix(vp, mp, op, nblocks, nthreads)
+            if i >= 1:
+                e2e.append(time.perf_counter() - t0)
+        e2e_t = allmax(td, sum(e2e) / len(e2e))
+        clocks = clk.stop()
+        sess.close()
+        parity = cpu = None
+        if rank == 0 and not args.no_cpu:
+            from oracle import oracle
+            A = np.memmap(mp, dtype=np.float32, mode="r", shape=(rows, cols))
+            x = np.fromfile(vp, dtype=np.float32)
+            sel = np.random.default_rng(0).choice(rows, 512, replace=False)
+            y64, ay = oracle.gemv_f64(np.ascontiguousarray(A[sel]), x)
+            parity = {"rows_checked": 512,
+                      "normwise": float(np.linalg.norm(y[sel] - y64) / np.linalg.norm(y64)),
+                      "within_1e-5": bool(np.all(np.abs(y[sel] - y64) <= 1e-5 * ay)),
+                      "bytes_equal_e2e": bool(np.array_equal(np.fromfile(op, dtype=np.float32), y))}
+            t0 = time.perf_counter()
+            yc = np.empty(rows, dtype=np.float32)
+            for r0 in range(0, rows, 1024):
+                yc[r0:r0 + 1024] = np.fromfile(mp, dtype=np.float32, count=1024 * cols,
+                                               offset=r0 * cols * 4).reshape(-1, cols) @ x
+            cpu_t = time.perf_counter() - t0
+            cpu = {"value": mbytes / cpu_t / 1e9, "unit": "GB/s", "cores": nt, "kind": "port",
+                   "sample": "host read of the whole 4 GiB matrix + FP32 matrix-vector product (numpy), once"}
+        achieved = (mbytes + cols * 4 + rows * 4) / (kms * 1e-3) / 1e9
+        line = {"metric": METRIC, "value": ws * mbytes / (kms * 1e-3) / 1e9, "unit": "GB/s", "n_gpus": ws,
+                "steps": steps, "warmup": warm, "ms_per_step": kms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded N(0,1) FP32",
+                "config": {"workload": "bigmatrix_mmap: y = A x, A 16384 x 65536 FP32 (4 GiB) read through gmmap "
+                                       "in 2 MiB pages, x 65536 FP32, y written through gmmap", "page_bytes": 1 << 21,
+                           "blocks": nblocks, "threads": nthreads, "l2": "4 GiB > 129 MB L2 (no flush needed)"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                             "frac": achieved / hbm, "peak_source": how, "traffic": None, "kernel": "k_bigmatrix",
+                             "algorithmic_bytes_per_launch": mbytes + cols * 4 + rows * 4, "mean_launch_ms": kms},
+                "cpu_baseline": cpu,
+                "e2e": {"value": ws * mbytes / e2e_t / 1e9, "unit": "GB/s", "h2d_bytes_per_step": mbytes + cols * 4,
+                        "d2h_bytes_per_step": rows * 4, "ms_per_step": e2e_t * 1e3,
+                        "call": "gfs_bigmatrix, cold buffer cache",
+                        "over_link_h2d": (mbytes / e2e_t / 1e9) / link[0] if link else None},
+                "gpu_launches": steps, "clocks": clocks, "parity": parity, "extra": extra}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def oracle_xxh64_file(path):
+    import numpy as np
+    return oracle_xxh64_bytes(np.fromfile(path, dtype=np.uint8))
+
+
+def oracle_xxh64_bytes(b):
+    from oracle import oracle
+    return oracle.xxh64(b)
 
 
 if __name__ == "__main__":

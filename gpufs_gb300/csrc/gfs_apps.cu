@@ -58,8 +58,18 @@ __device__ float dot_part(const float* a, const float* b, uint32_t n) {
     const uint32_t n4 = ((((uintptr_t)a | (uintptr_t)b) & 15u) == 0u) ? n / 4u : 0u;
     const float4* a4 = (const float4*)a;
     const float4* b4 = (const float4*)b;
-    for (uint32_t i = threadIdx.x; i < n4; i += blockDim.x) {
-        float4 p = __ldcg(a4 + i), q = __ldg(b4 + i);
+    const uint32_t bd = blockDim.x;
+    uint32_t i = threadIdx.x;
+    /* two independent 16-byte row loads in flight per thread (four spilled
+     * under the 64-register cap of this translation unit) */
+    for (; i + bd < n4; i += 2u * bd) {
+        const float4 p0 = __ldcg(a4 + i), p1 = __ldcg(a4 + i + bd);
+        const float4 q0 = __ldg(b4 + i), q1 = __ldg(b4 + i + bd);
+        s0 = fmaf(p0.x, q0.x, s0); s1 = fmaf(p0.y, q0.y, s1); s2 = fmaf(p0.z, q0.z, s2); s3 = fmaf(p0.w, q0.w, s3);
+        s0 = fmaf(p1.x, q1.x, s0); s1 = fmaf(p1.y, q1.y, s1); s2 = fmaf(p1.z, q1.z, s2); s3 = fmaf(p1.w, q1.w, s3);
+    }
+    for (; i < n4; i += bd) {
+        const float4 p = __ldcg(a4 + i), q = __ldg(b4 + i);
         s0 = fmaf(p.x, q.x, s0);
         s1 = fmaf(p.y, q.y, s1);
         s2 = fmaf(p.z, q.z, s2);

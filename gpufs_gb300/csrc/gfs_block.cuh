@@ -469,16 +469,15 @@ __device__ __noinline__ int st_fsync(gfs_state* S, int fd) {
 
 /* gunlink: remove the host file; a cached closed copy is invalidated. */
 __device__ __noinline__ int st_unlink(gfs_state* S, const char* name) {
-    int len = 0;
-    while (len < GFS_NAME_MAX && name[len]) len++;
-    if (len == 0 || len >= GFS_NAME_MAX) return -GFS_EINVAL;
-    uint64_t h = name_hash(name);
-    int slot = file_find(S, name, h);
+    Name nm;
+    name_load(name, nm);
+    if (nm.len == 0 || nm.len >= GFS_NAME_MAX) return -GFS_EINVAL;
+    int slot = file_find(S, nm);
     Waiter w(S->timeout_ns);
     if (slot < 0) {
         if (!spin_lock(&S->table_lock, w)) return -GFS_ETIMEDOUT;
-        slot = file_find(S, name, h);
-        if (slot < 0) slot = file_claim(S, name, h);
+        slot = file_find(S, nm);
+        if (slot < 0) slot = file_claim(S, nm);
         spin_unlock(&S->table_lock);
         if (slot < 0) return -GFS_EMFILE;
     }

@@ -626,37 +626,71 @@ __device__ __noinline__ int flush_frame(gfs_state* S, uint32_t fr, uint32_t slot
 /* ------------------------------------------------------------------ */
 /* open-file table                                                     */
 /* ------------------------------------------------------------------ */
-__device__ __forceinline__ uint64_t name_hash(const char* n) {
-    uint64_t h = 1469598103934665603ULL;
-    for (int i = 0; i < GFS_NAME_MAX && n[i]; i++) { h ^= (uint8_t)n[i]; h *= 1099511628211ULL; }
-    return h | 1ULL;
-}
-__device__ __forceinline__ bool name_eq(const char* a, const char* b) {
-    for (int i = 0; i < GFS_NAME_MAX; i++) {
-        char x = a[i], y = ((volatile const char*)b)[i];
-        if (x != y) return false;
-        if (!x) return true;
+/* A file name as 16 little-endian words, zero padded: read once with
+ * independent byte loads (no early exit), so a lookup costs one memory
+ * latency instead of one per character. */
+struct Name {
+    uint32_t w[GFS_NAME_MAX / 4];
+    int len;
+    uint64_t h;
+};
+__device__ __forceinline__ void name_load(const char* n, Name& nm) {
+#pragma unroll
+    for (int i = 0; i < GFS_NAME_MAX / 4; i++)
+        nm.w[i] = (uint32_t)(uint8_t)n[4 * i] | ((uint32_t)(uint8_t)n[4 * i + 1] << 8) |
+                  ((uint32_t)(uint8_t)n[4 * i + 2] << 16) | ((uint32_t)(uint8_t)n[4 * i + 3] << 24);
+    int len = GFS_NAME_MAX;
+#pragma unroll
+    for (int i = GFS_NAME_MAX / 4 - 1; i >= 0; i--) {
+        const uint32_t z = (nm.w[i] - 0x01010101u) & ~nm.w[i] & 0x80808080u; /* lowest set bit: first NUL */
+        if (z) len = 4 * i + ((__ffs(z) - 1) >> 3);
     }
-    return true;
+    uint64_t h = 1469598103934665603ULL;
+#pragma unroll
+    for (int i = 0; i < GFS_NAME_MAX / 4; i++) {
+        const int keep = len - 4 * i; /* bytes of this word inside the name */
+        nm.w[i] &= keep >= 4 ? 0xFFFFFFFFu : (keep <= 0 ? 0u : (1u << (8 * keep)) - 1u);
+        for (int k = 0; k < 4 && k < keep; k++) {
+            h ^= (nm.w[i] >> (8 * k)) & 0xFFu;
+            h *= 1099511628211ULL;
+        }
+    }
+    nm.len = len;
+    nm.h = h | 1ULL;
+}
+/* the slot's stored name (written under the table lock, published by the
+ * release store of its state word) against nm, 16 bytes at a time */
+__device__ __forceinline__ bool name_eq(const Name& nm, const char* slot_name) {
+    const uint4* q = (const uint4*)slot_name;
+    bool eq = true;
+#pragma unroll
+    for (int i = 0; i < GFS_NAME_MAX / 16; i++) {
+        uint4 v;
+        asm volatile("ld.relaxed.gpu.global.v4.u32 {%0,%1,%2,%3}, [%4];"
+                     : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(q + i) : "memory");
+        eq = eq && v.x == nm.w[4 * i] && v.y == nm.w[4 * i + 1] && v.z == nm.w[4 * i + 2] && v.w == nm.w[4 * i + 3];
+    }
+    return eq;
 }
 
-__device__ __forceinline__ int file_find(gfs_state* S, const char* name, uint64_t h) {
+__device__ __forceinline__ int file_find(gfs_state* S, const Name& nm) {
     uint32_t mask = S->n_files - 1;
     for (uint32_t p = 0; p < S->n_files; p++) {
-        uint32_t i = (uint32_t)(h + p) & mask;
+        uint32_t i = (uint32_t)(nm.h + p) & mask;
         gfs_file* fe = &S->files[i];
         uint32_t st = ld_acq(&fe->st);
         uint32_t s = sstatus(st);
         if (s == GFS_SS_EMPTY) return -1;
         if (s == GFS_SS_CLAIMING) continue;
-        if (ld_rlx64(&fe->hash) == h && name_eq(name, fe->name)) return (int)i;
+        if (ld_rlx64(&fe->hash) == nm.h && name_eq(nm, fe->name)) return (int)i;
     }
     return -1;
 }
 
 /* Caller holds the table lock.  Binds `name` to the first empty slot on its
  * probe path, or re-binds a closed, unused, clean slot. */
-__device__ __forceinline__ int file_claim(gfs_state* S, const char* name, uint64_t h) {
+__device__ __forceinline__ int file_claim(gfs_state* S, const Name& nm) {
+    const uint64_t h = nm.h;
     uint32_t mask = S->n_files - 1;
     for (uint32_t p = 0; p < S->n_files; p++) {
         uint32_t i = (uint32_t)(h + p) & mask;
@@ -668,11 +702,8 @@ __device__ __forceinline__ int file_claim(gfs_state* S, const char* name, uint64
         uint32_t inc = ((st >> GFS_S_INC_SHIFT) + 1u) & 0xFFu;
         uint32_t claiming = (GFS_SS_CLAIMING << GFS_S_SHIFT) | (inc << GFS_S_INC_SHIFT);
         if (atomicCAS(&fe->st, st, claiming) != st) continue;
-        for (int k = 0; k < GFS_NAME_MAX; k++) {
-            char c = name[k];
-            ((volatile char*)fe->name)[k] = c;
-            if (!c) { for (int z = k + 1; z < GFS_NAME_MAX; z++) ((volatile char*)fe->name)[z] = 0; break; }
-        }
+#pragma unroll
+        for (int k = 0; k < GFS_NAME_MAX / 4; k++) ((volatile uint32_t*)fe->name)[k] = nm.w[k];
         st_rlx64(&fe->hash, h);
         st_rlx((uint32_t*)&fe->host_fd, (uint32_t)-1);
         st_rlx64(&fe->cached_ctime, 0ULL);
@@ -687,28 +718,32 @@ __device__ __forceinline__ int file_claim(gfs_state* S, const char* name, uint64
 
 /* gopen body (single thread): returns the slot (fd) or -error. */
 __device__ __noinline__ int file_open(gfs_state* S, const char* name, int oflags) {
-    int len = 0;
-    while (len < GFS_NAME_MAX && name[len]) len++;
-    if (len == 0 || len >= GFS_NAME_MAX) { set_error(S, GFS_ERRB_ARG); return -GFS_EINVAL; }
-    uint64_t h = name_hash(name);
+    Name nm;
+    name_load(name, nm);
+    if (nm.len == 0 || nm.len >= GFS_NAME_MAX) { set_error(S, GFS_ERRB_ARG); return -GFS_EINVAL; }
+    const uint64_t h = nm.h;
     Waiter w(S->timeout_ns);
     for (;;) {
-        int slot = file_find(S, name, h);
+        int slot = file_find(S, nm);
         if (slot < 0) {
             if (!spin_lock(&S->table_lock, w)) { set_error(S, GFS_ERRB_TIMEOUT); return -GFS_ETIMEDOUT; }
-            slot = file_find(S, name, h);
-            if (slot < 0) slot = file_claim(S, name, h);
+            slot = file_find(S, nm);
+            if (slot < 0) slot = file_claim(S, nm);
             spin_unlock(&S->table_lock);
             if (slot < 0) { set_error(S, GFS_ERRB_TABLE); return -GFS_EMFILE; }
         }
         gfs_file* fe = &S->files[slot];
         for (;;) {
             uint32_t st = ld_acq(&fe->st);
-            if (ld_rlx64(&fe->hash) != h || !name_eq(name, fe->name)) break; /* re-bound: find again */
+            if (ld_rlx64(&fe->hash) != h || !name_eq(nm, fe->name)) break; /* re-bound: find again */
             uint32_t s = sstatus(st), cnt = st & GFS_S_CNT;
             uint32_t inc_bits = st & GFS_S_INC_MASK;
             if (s == GFS_SS_OPEN) {
-                if (atomicCAS(&fe->st, st, st + 1u) == st) return slot;
+                /* fetch-and-add (never retried under contention); it holds if
+                 * status and incarnation were unchanged, else it is undone */
+                const uint32_t old = atomicAdd(&fe->st, 1u);
+                if ((old & ~GFS_S_CNT) == (st & ~GFS_S_CNT)) return slot;
+                atomicSub(&fe->st, 1u);
                 continue;
             }
             if (s == GFS_SS_CLOSED && cnt == 0u) {
@@ -780,17 +815,17 @@ __device__ __noinline__ int file_open(gfs_state* S, const char* name, int oflags
 __device__ __forceinline__ int file_close_begin(gfs_state* S, int fd) {
     if (fd < 0 || (uint32_t)fd >= S->n_files) return -GFS_EBADF;
     gfs_file* fe = &S->files[fd];
-    for (int spins = 0; spins < 1000000; spins++) {
-        uint32_t st = ld_acq(&fe->st);
-        if (sstatus(st) != GFS_SS_OPEN || (st & GFS_S_CNT) == 0u) return -GFS_EBADF;
-        if ((st & GFS_S_CNT) > 1u) {
-            if (atomicCAS(&fe->st, st, st - 1u) == st) return 0;
-        } else {
-            uint32_t closing = (GFS_SS_CLOSING << GFS_S_SHIFT) | (st & GFS_S_INC_MASK);
-            if (atomicCAS(&fe->st, st, closing) == st) return 1;
-        }
-    }
-    return -GFS_ETIMEDOUT;
+    const uint32_t st = ld_acq(&fe->st);
+    if (sstatus(st) != GFS_SS_OPEN || (st & GFS_S_CNT) == 0u) return -GFS_EBADF; /* not open */
+    /* The caller holds one count, so the slot stays OPEN until it drops it:
+     * fetch-and-subtract; the closer that takes the count to zero then moves
+     * the slot to CLOSING, unless an opener came in first (that opener then
+     * holds the file and will close it). */
+    const uint32_t old = atomicSub(&fe->st, 1u);
+    if ((old & GFS_S_CNT) > 1u) return 0;
+    const uint32_t zero = old - 1u;
+    const uint32_t closing = (GFS_SS_CLOSING << GFS_S_SHIFT) | (zero & GFS_S_INC_MASK);
+    return atomicCAS(&fe->st, zero, closing) == zero ? 1 : 0;
 }
 
 __device__ __forceinline__ int file_close_finish(gfs_state* S, int fd) {
