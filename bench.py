@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--data-dir", default=None)
-    ap.add_argument("--log-page", type=int, default=20)
+    ap.add_argument("--log-page", type=int, default=21)
     ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true")

@@ -32,16 +32,18 @@ O_GWRONCE = O_CREAT | O_WRONLY
 
 STAT_NAMES = ["hits", "misses", "evictions", "writebacks", "read_rpcs", "bytes_read_rpc", "opens", "closes",
               "timeouts", "errors", "conflict_evictions", "host_requests", "host_reads", "host_read_bytes",
-              "host_writes", "host_write_bytes", "host_opens", "host_errors", "err_site", "rpc_submitted"]
+              "host_writes", "host_write_bytes", "host_opens", "host_errors", "err_site", "rpc_submitted",
+              "host_map_reads"]
 
 ERR_TIMEOUT, ERR_IO, ERR_NOMEM, ERR_TABLE, ERR_ARG = 1, 2, 4, 8, 16
 XXH64_NOALLOC_MAX_FILES = 1024  # GFS_XXH64_NOALLOC_MAX_FILES
+CFG_NO_FILE_MAP = 1  # GFS_CFG_NO_FILE_MAP
 
 
 class Config(ctypes.Structure):
     _fields_ = [("log_page", ctypes.c_uint32), ("max_files", ctypes.c_uint32), ("pool_bytes", ctypes.c_uint64),
                 ("ring_slots", ctypes.c_uint32), ("host_workers", ctypes.c_uint32),
-                ("staging_depth", ctypes.c_uint32), ("pad0", ctypes.c_uint32), ("timeout_ns", ctypes.c_uint64),
+                ("staging_depth", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("timeout_ns", ctypes.c_uint64),
                 ("device", ctypes.c_int32), ("pad1", ctypes.c_uint32)]
 
 
@@ -131,7 +133,7 @@ class Session:
     """One file-system session on one GPU (initializer() .. delete GPUGlobals)."""
 
     def __init__(self, log_page=16, pool_bytes=2 << 30, max_files=1024, ring_slots=4096, host_workers=8,
-                 staging_depth=8, timeout_s=30.0, device=0):
+                 staging_depth=8, timeout_s=30.0, device=0, file_map=True):
         L = lib()
         c = Config()
         L.gfs_default_config(ctypes.byref(c))
@@ -141,6 +143,7 @@ class Session:
         c.ring_slots = ring_slots
         c.host_workers = host_workers
         c.staging_depth = staging_depth
+        c.flags = 0 if file_map else CFG_NO_FILE_MAP
         c.timeout_ns = int(timeout_s * 1e9)
         c.device = device
         h = ctypes.c_void_p()

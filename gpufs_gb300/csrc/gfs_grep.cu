@@ -817,54 +817,76 @@ void rec_key(const uint8_t* rec, uint32_t k[8], int* len) {
  * records the scan verifies candidates against (measured: lower loads were
  * slower).  16-bit tags keep false candidates rare at this load. */
 bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
-    std::unordered_map<std::string, int> first;
-    std::vector<int> uniq;
-    T.next_dup.assign((size_t)(n_words > 0 ? n_words : 1), -1);
-    std::vector<int> last((size_t)(n_words > 0 ? n_words : 1), -1);
-    for (int w = 0; w < n_words; w++) {
+    const size_t nw = n_words > 0 ? (size_t)n_words : 1u;
+    struct Key {
         uint32_t k[8];
+        uint32_t h1;
         int len;
-        rec_key(dict + (size_t)w * 32, k, &len);
-        if (len == 0) continue;
-        std::string key((const char*)dict + (size_t)w * 32, (size_t)len);
-        auto it = first.find(key);
-        if (it == first.end()) {
-            first.emplace(key, w);
-            uniq.push_back(w);
-            last[(size_t)w] = w;
-        } else {
-            int h = it->second;
-            T.next_dup[(size_t)last[(size_t)h]] = w;
-            last[(size_t)h] = w;
+    };
+    std::vector<Key> key(nw);
+    std::vector<int> uniq, last(nw, -1);
+    uniq.reserve(nw);
+    T.next_dup.assign(nw, -1);
+    /* duplicates: open addressing on the word hash, exact key compare */
+    size_t cap = 16;
+    while (cap < 2 * nw) cap <<= 1;
+    std::vector<int> seen(cap, -1);
+    for (int w = 0; w < n_words; w++) {
+        Key& kw = key[(size_t)w];
+        rec_key(dict + (size_t)w * 32, kw.k, &kw.len);
+        if (kw.len == 0) continue;
+        kw.h1 = grep_h1(grep_mix(kw.k, kw.len));
+        for (size_t i = kw.h1 & (cap - 1);; i = (i + 1) & (cap - 1)) {
+            const int u = seen[i];
+            if (u < 0) {
+                seen[i] = w;
+                uniq.push_back(w);
+                last[(size_t)w] = w;
+                break;
+            }
+            const Key& ku = key[(size_t)u];
+            if (ku.h1 == kw.h1 && ku.len == kw.len && memcmp(ku.k, kw.k, sizeof kw.k) == 0) {
+                T.next_dup[(size_t)last[(size_t)u]] = w;
+                last[(size_t)u] = w;
+                break;
+            }
         }
     }
+    /* bucketised cuckoo placement (2 choices x 4 slots), random-walk kicks */
+    std::vector<uint32_t> ba(nw), bb(nw);
     uint32_t nb = (uint32_t)((double)uniq.size() / (GREP_WAYS * 0.92)) + 16u;
     for (int attempt = 0; attempt < 20; attempt++, nb = nb + nb / 8u + 1u) {
-        std::vector<int> slot_of(nb * GREP_WAYS, -1);
+        for (int w : uniq) {
+            ba[(size_t)w] = grep_bucket(key[(size_t)w].h1, nb);
+            bb[(size_t)w] = grep_b2(key[(size_t)w].h1, nb);
+        }
+        std::vector<int> slot_of((size_t)nb * GREP_WAYS, -1);
         uint64_t rng = 0x243F6A8885A308D3ULL ^ nb;
         bool ok = true;
         for (int w : uniq) {
             int cur = w;
             int kicks = 0;
             for (;;) {
-                uint32_t k[8];
-                int len;
-                rec_key(dict + (size_t)cur * 32, k, &len);
-                const uint32_t h1 = grep_h1(grep_mix(k, len));
-                const uint32_t b1 = grep_bucket(h1, nb);
-                uint32_t b[2] = {b1, grep_b2(h1, nb)};
-                int placed = -1;
-                for (int r = 0; r < 2 && placed < 0; r++)
+                const uint32_t b[2] = {ba[(size_t)cur], bb[(size_t)cur]};
+                /* the emptier of the two buckets (fewer kicks near full load) */
+                int placed = -1, best_free = 0;
+                for (int r = 0; r < 2; r++) {
+                    int nfree = 0, first = -1;
                     for (int i = 0; i < GREP_WAYS; i++)
-                        if (slot_of[b[r] * GREP_WAYS + (uint32_t)i] < 0) { placed = (int)(b[r] * GREP_WAYS + (uint32_t)i); break; }
+                        if (slot_of[b[r] * GREP_WAYS + (uint32_t)i] < 0) {
+                            nfree++;
+                            if (first < 0) first = (int)(b[r] * GREP_WAYS + (uint32_t)i);
+                        }
+                    if (nfree > best_free) { best_free = nfree; placed = first; }
+                }
                 if (placed >= 0) {
                     slot_of[(size_t)placed] = cur;
                     break;
                 }
                 if (++kicks > 2000) { ok = false; break; }
                 rng ^= rng << 13; rng ^= rng >> 7; rng ^= rng << 17;
-                uint32_t victim = b[rng & 1u] * GREP_WAYS + (uint32_t)((rng >> 8) & 3u);
-                int ev = slot_of[victim];
+                const uint32_t victim = b[rng & 1u] * GREP_WAYS + (uint32_t)((rng >> 8) & 3u);
+                const int ev = slot_of[victim];
                 slot_of[victim] = cur;
                 cur = ev;
             }
@@ -872,19 +894,16 @@ bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
         }
         if (!ok) continue;
         T.nb = nb;
-        T.tags.assign(nb * GREP_WAYS, 0u);
+        T.tags.assign((size_t)nb * GREP_WAYS, 0u);
         T.recs.assign((size_t)nb * GREP_WAYS * 8, 0u);
-        T.slot_word.assign(nb * GREP_WAYS, 0xFFFFFFFFu);
-        for (uint32_t s = 0; s < nb * GREP_WAYS; s++) {
-            int w = slot_of[s];
+        T.slot_word.assign((size_t)nb * GREP_WAYS, 0xFFFFFFFFu);
+        for (uint32_t sl = 0; sl < nb * GREP_WAYS; sl++) {
+            const int w = slot_of[sl];
             if (w < 0) continue;
-            uint32_t k[8];
-            int len;
-            rec_key(dict + (size_t)w * 32, k, &len);
-            const uint32_t h1 = grep_h1(grep_mix(k, len));
-            T.tags[s] = (uint16_t)grep_tag(h1, len);
-            memcpy(&T.recs[(size_t)s * 8], k, 32);
-            T.slot_word[s] = (uint32_t)w;
+            const Key& kw = key[(size_t)w];
+            T.tags[sl] = (uint16_t)grep_tag(kw.h1, kw.len);
+            memcpy(&T.recs[(size_t)sl * 8], kw.k, 32);
+            T.slot_word[sl] = (uint32_t)w;
         }
         return true;
     }

@@ -35,12 +35,16 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <sys/mman.h>
+#include <sys/resource.h>
 #include <sys/stat.h>
 #include <sys/time.h>
 #include <time.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -120,6 +124,18 @@ ssize_t pwrite_full(int fd, const uint8_t* buf, size_t len, off_t off) {
 
 } // namespace
 
+/* A read-only file's bytes, mapped from the host page cache and registered
+ * with CUDA, so page misses are copy-engine DMA from it (no pread, no
+ * staging copy).  Keyed by the file's identity and version. */
+struct FileMap {
+    uint64_t dev = 0, ino = 0, size = 0;
+    int64_t ctime_ns = 0;
+    uint8_t* base = nullptr;
+    size_t len = 0;
+    int refs = 0;      /* open host fds using it */
+    uint64_t last = 0; /* LRU stamp */
+};
+
 struct gfs_ctx {
     gfs_config cfg{};
     gfs_state hs{};
@@ -143,6 +159,13 @@ struct gfs_ctx {
     size_t reply_off = 0;
     std::atomic<int> logged{0};
     size_t d_scratch_cap = 0;
+    /* registered file mappings */
+    std::mutex map_mu;
+    std::vector<FileMap*> maps;
+    std::vector<std::atomic<FileMap*>> fd_map; /* host fd -> mapping, read lock-free by workers */
+    size_t mapped_bytes = 0, map_cap = 0;
+    uint64_t map_clock = 0;
+    std::atomic<unsigned long long> h_map_reads{0};
 };
 
 static uint32_t* host_word(gfs_ctx* c, uint64_t dev_addr) {
@@ -191,6 +214,72 @@ static int slot_take(gfs_ctx* c, Worker* w) {
     return k;
 }
 
+static void map_release(FileMap* m) {
+    cudaHostUnregister(m->base);
+    munmap(m->base, m->len);
+    delete m;
+}
+
+/* Mapping for a file just opened read-only (host fd `fd`, stat `st`), made
+ * on first use and kept while unchanged; nullptr when it cannot be made. */
+static void map_attach(gfs_ctx* c, int fd, const struct stat& st) {
+    if ((c->cfg.flags & GFS_CFG_NO_FILE_MAP) || !S_ISREG(st.st_mode) || st.st_size < (off_t)(64 << 10)) return;
+    if (fd < 0 || (size_t)fd >= c->fd_map.size()) return;
+    const int64_t ct = (int64_t)st.st_ctim.tv_sec * 1000000000LL + st.st_ctim.tv_nsec;
+    const size_t len = (size_t)st.st_size;
+    {
+        std::lock_guard<std::mutex> lk(c->map_mu);
+        for (FileMap* m : c->maps)
+            if (m->dev == (uint64_t)st.st_dev && m->ino == (uint64_t)st.st_ino && m->size == (uint64_t)len &&
+                m->ctime_ns == ct) {
+                m->refs++;
+                m->last = ++c->map_clock;
+                c->fd_map[(size_t)fd].store(m, std::memory_order_release);
+                return;
+            }
+        if (c->mapped_bytes + len > c->map_cap) {
+            /* evict unused mappings, least recently used first */
+            std::sort(c->maps.begin(), c->maps.end(), [](FileMap* a, FileMap* b) { return a->last < b->last; });
+            for (size_t i = 0; i < c->maps.size() && c->mapped_bytes + len > c->map_cap;) {
+                FileMap* m = c->maps[i];
+                if (m->refs) { i++; continue; }
+                c->mapped_bytes -= m->len;
+                c->maps.erase(c->maps.begin() + (long)i);
+                map_release(m);
+            }
+            if (c->mapped_bytes + len > c->map_cap) return;
+        }
+    }
+    void* p = mmap(nullptr, len, PROT_READ, MAP_SHARED | MAP_POPULATE, fd, 0);
+    if (p == MAP_FAILED) return;
+    if (cudaHostRegister(p, len, cudaHostRegisterDefault) != cudaSuccess) {
+        cudaGetLastError();
+        munmap(p, len);
+        return;
+    }
+    FileMap* m = new FileMap();
+    m->dev = (uint64_t)st.st_dev;
+    m->ino = (uint64_t)st.st_ino;
+    m->size = (uint64_t)len;
+    m->ctime_ns = ct;
+    m->base = (uint8_t*)p;
+    m->len = len;
+    m->refs = 1;
+    std::lock_guard<std::mutex> lk(c->map_mu);
+    m->last = ++c->map_clock;
+    c->maps.push_back(m);
+    c->mapped_bytes += len;
+    c->fd_map[(size_t)fd].store(m, std::memory_order_release);
+}
+
+static void map_detach(gfs_ctx* c, int fd) {
+    if (fd < 0 || (size_t)fd >= c->fd_map.size()) return;
+    FileMap* m = c->fd_map[(size_t)fd].exchange(nullptr, std::memory_order_acq_rel);
+    if (!m) return;
+    std::lock_guard<std::mutex> lk(c->map_mu);
+    m->refs--;
+}
+
 static int host_open_flags(int oflags) {
     /* the reference turns write-once into O_RDWR|O_CREAT (host_loop.h:169-173);
      * write-only files are opened read-write as well so partial-page writes
@@ -218,6 +307,7 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
             if (fstat(fd, &st) == 0) {
                 rep.size = (uint64_t)st.st_size;
                 rep.ctime_ns = (int64_t)st.st_ctim.tv_sec * 1000000000LL + st.st_ctim.tv_nsec;
+                if ((host_open_flags(r.oflags) & O_ACCMODE) == O_RDONLY) map_attach(c, fd, st);
             }
         }
         if (r.file < c->hs.n_files) {
@@ -230,6 +320,7 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         break;
     }
     case GFS_OP_CLOSE: {
+        map_detach(c, r.host_fd);
         int rc = r.host_fd >= 0 ? close(r.host_fd) : 0;
         set_done(c, done, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno));
         break;
@@ -242,6 +333,33 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         size_t len = (size_t)r.length;
         if (len > w->slot_bytes) len = w->slot_bytes;
         int k = slot_take(c, w);
+        FileMap* fm = (r.host_fd >= 0 && (size_t)r.host_fd < c->fd_map.size())
+                          ? c->fd_map[(size_t)r.host_fd].load(std::memory_order_acquire)
+                          : nullptr;
+        if (fm && r.offset < fm->len) {
+            /* DMA straight from the registered page-cache mapping */
+            const size_t n = len < fm->len - (size_t)r.offset ? len : fm->len - (size_t)r.offset;
+            size_t cp = (n + 4095u) & ~(size_t)4095u;
+            if (cp > w->slot_bytes) cp = w->slot_bytes;
+            cudaError_t e = cudaMemcpyAsync((void*)(uintptr_t)r.dev_addr, fm->base + r.offset, n,
+                                            cudaMemcpyHostToDevice, w->stream);
+            if (e == cudaSuccess && cp > n)
+                e = cudaMemsetAsync((void*)(uintptr_t)(r.dev_addr + n), 0, cp - n, w->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(w->ev[(size_t)k], w->stream);
+            if (e != cudaSuccess) {
+                log_failure(c, r, EIO);
+                set_done(c, done, GFS_DONE_ERR | (uint32_t)EIO);
+                break;
+            }
+            c->h_reads++;
+            c->h_map_reads++;
+            c->h_read_bytes += (unsigned long long)n;
+            w->pend[(size_t)k] = Pending{done, 1u + (uint32_t)n};
+            w->busy[(size_t)k] = 1;
+            w->nbusy++;
+            drain(c, w, false);
+            break;
+        }
         uint8_t* buf = w->staging + (size_t)k * w->slot_bytes;
         ssize_t n = pread_full(r.host_fd, buf, len, (off_t)r.offset);
         if (n < 0) {
@@ -441,6 +559,18 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
     cfg.max_files = next_pow2(cfg.max_files < 64 ? 64 : cfg.max_files);
     if (cfg.max_files > (1u << 20)) { delete c; return -GFS_EINVAL; }
     {
+        /* registered file mappings: one slot per possible host fd, at most
+         * half the host memory mapped */
+        struct rlimit rl;
+        size_t nfd = 1u << 16;
+        if (getrlimit(RLIMIT_NOFILE, &rl) == 0 && rl.rlim_cur != RLIM_INFINITY && rl.rlim_cur < (1u << 20))
+            nfd = (size_t)rl.rlim_cur;
+        c->fd_map = std::vector<std::atomic<FileMap*>>(nfd);
+        for (auto& a : c->fd_map) a.store(nullptr);
+        const long pages = sysconf(_SC_PHYS_PAGES), psz = sysconf(_SC_PAGESIZE);
+        c->map_cap = pages > 0 && psz > 0 ? (size_t)pages * (size_t)psz / 2 : (size_t)8 << 30;
+    }
+    {
         uint64_t page = 1ull << cfg.log_page;
         uint64_t nf = cfg.pool_bytes / page;
         if (nf < 64) nf = 64;
@@ -532,6 +662,8 @@ int gfs_destroy(gfs_ctx* c) {
         delete w;
     }
     c->workers.clear();
+    for (FileMap* m : c->maps) map_release(m);
+    c->maps.clear();
     gfs_state& s = c->hs;
     gfs_state* none = nullptr;
     if (c->ds && g_current == c) {
@@ -582,7 +714,7 @@ int gfs_get_stats(gfs_ctx* c, unsigned long long* out, int n) {
         st.hits, st.misses, st.evictions, st.writebacks, st.read_rpcs, st.bytes_read_rpc, st.opens, st.closes,
         st.timeouts, st.errors, st.conflict_evictions, c->h_requests.load(), c->h_reads.load(),
         c->h_read_bytes.load(), c->h_writes.load(), c->h_write_bytes.load(), c->h_opens.load(), c->h_errors.load(),
-        st.err_site, st.rpc_submitted};
+        st.err_site, st.rpc_submitted, c->h_map_reads.load()};
     int k = n < GFS_NSTATS ? n : GFS_NSTATS;
     for (int i = 0; i < k; i++) out[i] = v[i];
     return k;
@@ -599,6 +731,7 @@ int gfs_reset_stats(gfs_ctx* c) {
     c->h_write_bytes = 0;
     c->h_opens = 0;
     c->h_errors = 0;
+    c->h_map_reads = 0;
     return 0;
 }
 

@@ -34,23 +34,34 @@ typedef struct gfs_config {
     uint32_t ring_slots;    /* host request ring slots, 2^k (RW_IPC_SIZE) */
     uint32_t host_workers;  /* host I/O threads (RW_HOST_WORKERS) */
     uint32_t staging_depth; /* pinned staging pages per worker (RW_SCRATCH_PER_WORKER) */
-    uint32_t pad0;
+    uint32_t flags;         /* GFS_CFG_* */
     uint64_t timeout_ns;    /* bound on every device-side wait (the reference waits forever) */
     int32_t device;         /* CUDA device ordinal */
     uint32_t pad1;
 } gfs_config;
 
-#define GFS_NSTATS 20
+/* gfs_config.flags: read files through pread into pinned staging only, never
+ * through a registered mapping of the file (see gfs_create) */
+#define GFS_CFG_NO_FILE_MAP 1u
+
+#define GFS_NSTATS 21
 /* gfs_get_stats order: device hits(page accesses), misses, evictions,
  * writebacks, read_rpcs, bytes_read_rpc, opens, closes, timeouts, errors,
  * conflict_evictions; host requests, reads, read_bytes, writes, write_bytes,
- * opens, errors; first device failure (site << 16 | errno); requests submitted */
+ * opens, errors; first device failure (site << 16 | errno); requests
+ * submitted; host reads served by DMA from a registered file mapping */
 
 /* ---- session ---- */
 /* defaults: 64 KiB pages, 2 GiB pool, 1024 files, 4096 ring slots, 8 workers */
 void gfs_default_config(gfs_config* cfg);
 /* replaces initializer() / GPUGlobals::GPUGlobals (libgpufs/fs_initializer.cu:116-167,
- * fs_initializer.cu.h:139-178); host workers start here and serve until destroy */
+ * fs_initializer.cu.h:139-178); host workers start here and serve until destroy.
+ * Files opened read-only are mapped and registered with CUDA on their first
+ * open (kept across closes while unchanged: same inode, size and ctime, and
+ * released at destroy or when over half the host memory is mapped), so a
+ * page miss is one copy-engine DMA from the host page cache into the frame;
+ * other files, and any file whose mapping fails, go through pread into
+ * pinned staging as the reference does (host_loop.h:431-557). */
 int gfs_create(const gfs_config* cfg, gfs_ctx** out);
 /* replaces GPUGlobals::~GPUGlobals (libgpufs/fs_initializer.cu.h:180-198) */
 int gfs_destroy(gfs_ctx* ctx);

@@ -246,3 +246,30 @@ def test_stalled_host_times_out(built, shm_dir):
     with g.Session(log_page=16, pool_bytes=16 << 20, timeout_s=20) as s:
         w = np.fromfile(p, dtype=np.uint8)
         assert np.array_equal(s.pread(p, 0, w.size, nblocks=2), w)
+
+
+def test_reads_use_registered_file_mapping(built, shm_dir):
+    """Read-only opens DMA page misses straight from a registered mapping of
+    the host file; a rewritten file (new size/ctime) is mapped afresh; with
+    the mapping off every miss goes through pread into staging."""
+    p = os.path.join(shm_dir, "mapped.bin")
+    want = _mk(p, 3 * (1 << 20) + 5, seed=20)
+    with g.Session(log_page=16, pool_bytes=64 << 20, timeout_s=20) as s:
+        s.reset_stats()
+        assert np.array_equal(s.pread(p, 0, want.size, nblocks=4), want)
+        st = s.stats()
+        assert st["host_reads"] > 0 and st["host_map_reads"] == st["host_reads"]
+        # the mapping is kept across closes: a cold re-read needs no pread either
+        s.drop_cache()
+        s.reset_stats()
+        assert np.array_equal(s.pread(p, 0, want.size, nblocks=4), want)
+        assert s.stats()["host_map_reads"] == s.stats()["host_reads"] > 0
+        time.sleep(0.01)
+        want2 = _mk(p, 2 * (1 << 20) + 77, seed=21)
+        assert np.array_equal(s.pread(p, 0, want2.size, nblocks=3), want2)
+        assert s.last_error() == 0
+    with g.Session(log_page=16, pool_bytes=64 << 20, timeout_s=20, file_map=False) as s:
+        s.reset_stats()
+        assert np.array_equal(s.pread(p, 0, want2.size, nblocks=4), want2)
+        st = s.stats()
+        assert st["host_reads"] > 0 and st["host_map_reads"] == 0
