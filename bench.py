@@ -407,6 +407,31 @@ def _cpu_copy_gbs(src, dst, chunk, nt):
     return size / dt / 1e9
 
 
+def _host_pwrite_gbs(src, dst, chunk, nt):
+    """All-threads host pwrite of src's bytes into a new file in `chunk`
+    pieces (GB/s): the host file system's write rate, which bounds any copy
+    that lands in a new host file."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    data = np.fromfile(src, dtype=np.uint8)
+    size = data.size
+    if os.path.exists(dst):
+        os.unlink(dst)
+    fd = os.open(dst, os.O_RDWR | os.O_CREAT, 0o644)
+    mv = memoryview(data)
+
+    def part(i):
+        for off in range(i * chunk, size, nt * chunk):
+            os.pwrite(fd, mv[off:off + chunk], off)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(nt) as ex:
+        list(ex.map(part, range(nt)))
+    dt = time.perf_counter() - t0
+    os.close(fd)
+    os.unlink(dst)
+    return size / dt / 1e9
+
+
 def run_workload(args, rank, ws, local, td, data_dir):
     import __graft_entry__
     if rank == 0:
@@ -436,7 +461,7 @@ def run_workload(args, rank, ws, local, td, data_dir):
                          staging_depth=4, timeout_s=60, device=local)
         import torch
         dev = torch.empty(size, dtype=torch.uint8, device="cuda:%d" % local)
-        nblocks, nthreads = size // page if size // page <= 4096 else 4096, 1024
+        nblocks, nthreads = 152, 1024  # one wave, one block per SM (measured fastest)
         clk.start()
         sess.pread_dev(src, 0, size, dev.data_ptr(), nblocks, nthreads)  # loads the cache
         for _ in range(warm):
@@ -515,6 +540,8 @@ def run_workload(args, rank, ws, local, td, data_dir):
         cpu = {"value": _cpu_copy_gbs(src, dst, 64 << 10, nt), "unit": "GB/s", "cores": nt, "kind": "port",
                "sample": "host pread/pwrite copy of the 512 MiB file in 64 KiB pieces to a new file, all threads"} \
             if rank == 0 and not args.no_cpu else None
+        fs_write = _host_pwrite_gbs(src, dst, 64 << 10, workers)
+        extra["host_file_write_gbs"] = fs_write
         achieved = size / (kms * 1e-3) / 1e9
         extra["mode1_gmmap_ms"] = sum(k1) / len(k1)
         line = {"metric": METRIC, "value": ws * size / (kms * 1e-3) / 1e9, "unit": "GB/s", "n_gpus": ws,
@@ -523,10 +550,11 @@ def run_workload(args, rank, ws, local, td, data_dir):
                 "config": {"workload": "memcopy: one 512 MiB file copied to a new file by 112 blocks x 256 threads "
                                        "with gread/gwrite in 64 KiB pages (source resident in the buffer cache; the "
                                        "copy is written back to the host file at gclose)", "page_bytes": 65536},
-                "roofline": {"bound": "link", "achieved": achieved, "peak": link[1] if link else None,
-                             "unit": "GB/s", "frac": achieved / link[1] if link else None,
-                             "peak_source": "measured pinned D2H", "traffic": None, "kernel": "k_memcopy",
-                             "algorithmic_bytes_per_launch": size, "mean_launch_ms": kms},
+                "roofline": {"bound": "host file write", "achieved": achieved, "peak": fs_write,
+                             "unit": "GB/s", "frac": achieved / fs_write,
+                             "peak_source": "measured: host pwrite of the same bytes into a new file, 64 KiB "
+                                            "pieces, one thread per host worker", "traffic": None,
+                             "kernel": "k_memcopy", "algorithmic_bytes_per_launch": size, "mean_launch_ms": kms},
                 "cpu_baseline": cpu,
                 "e2e": {"value": ws * size / e2e_t / 1e9, "unit": "GB/s", "h2d_bytes_per_step": size,
                         "d2h_bytes_per_step": size, "ms_per_step": e2e_t * 1e3,

@@ -55,9 +55,24 @@ extern __device__ gfs_state* g_gfs;
 
 namespace {
 
-struct Pending { /* a read whose H2D copy is in flight */
+struct Pending { /* a copy in flight: a read's H2D, or a write-back's D2H */
     uint32_t* done; /* host pointer of the completion word */
     uint32_t code;
+    int write = 0;  /* write-back: merge and pwrite once the copy landed */
+    int host_fd = -1;
+    uint64_t offset = 0;
+    size_t len = 0;
+    uint32_t rflags = 0;
+};
+
+/* Per open host fd: its size when opened and the pages written back since,
+ * so a write-once page that lands on bytes nobody has written (past the
+ * size at open, not written back before) needs no OR-merge read: those
+ * bytes are zero. */
+struct FdInfo {
+    uint64_t size_at_open = 0;
+    std::mutex mu;
+    std::vector<uint64_t> written; /* bit per page */
 };
 
 struct Worker {
@@ -163,6 +178,7 @@ struct gfs_ctx {
     std::mutex map_mu;
     std::vector<FileMap*> maps;
     std::vector<std::atomic<FileMap*>> fd_map; /* host fd -> mapping, read lock-free by workers */
+    std::vector<std::atomic<FdInfo*>> fd_info; /* host fd -> write-back bookkeeping */
     size_t mapped_bytes = 0, map_cap = 0;
     uint64_t map_clock = 0;
     std::atomic<unsigned long long> h_map_reads{0};
@@ -186,7 +202,50 @@ static void log_failure(gfs_ctx* c, const gfs_req& r, int err) {
                 strerror(err), r.host_fd, (unsigned long long)r.offset, (unsigned long long)r.length);
 }
 
-/* Complete in-flight reads whose copies have landed (in issue order). */
+/* A write-back whose page has landed in staging slot k: OR-merge with the
+ * file's bytes for write-once files (diff_and_merge, host_loop.h:76-137),
+ * unless those bytes are known to be zero, then pwrite. */
+static void finish_write(gfs_ctx* c, Worker* w, int k, const Pending& p) {
+    uint8_t* buf = w->staging + (size_t)k * w->slot_bytes;
+    const size_t len = p.len;
+    bool merge = (p.rflags & GFS_RF_DIFF) != 0;
+    FdInfo* fi = (p.host_fd >= 0 && (size_t)p.host_fd < c->fd_info.size())
+                     ? c->fd_info[(size_t)p.host_fd].load(std::memory_order_acquire)
+                     : nullptr;
+    if (fi) {
+        const uint64_t pg = p.offset >> c->hs.log_page;
+        std::lock_guard<std::mutex> lk(fi->mu);
+        if (fi->written.size() <= (size_t)(pg >> 6)) fi->written.resize((size_t)(pg >> 6) + 1, 0ULL);
+        const uint64_t bit = 1ULL << (pg & 63u);
+        if (merge && p.offset >= fi->size_at_open && !(fi->written[(size_t)(pg >> 6)] & bit)) merge = false;
+        fi->written[(size_t)(pg >> 6)] |= bit;
+    }
+    if (merge) {
+        ssize_t m = pread_full(p.host_fd, w->merge, len, (off_t)p.offset);
+        size_t i = 0;
+        for (; m >= 8 && i + 8 <= (size_t)m; i += 8) {
+            uint64_t a, b;
+            memcpy(&a, buf + i, 8);
+            memcpy(&b, w->merge + i, 8);
+            a |= b;
+            memcpy(buf + i, &a, 8);
+        }
+        for (; (ssize_t)i < m; i++) buf[i] |= w->merge[i];
+    }
+    gfs_req r{};
+    r.op = GFS_OP_WRITE;
+    r.host_fd = p.host_fd;
+    r.offset = p.offset;
+    r.length = len;
+    ssize_t put = pwrite_full(p.host_fd, buf, len, (off_t)p.offset);
+    int err = put < 0 ? errno : EIO;
+    c->h_writes++;
+    if (put >= 0) c->h_write_bytes += (unsigned long long)put;
+    if (put != (ssize_t)len) log_failure(c, r, err);
+    set_done(c, p.done, put == (ssize_t)len ? 1u + (uint32_t)len : (GFS_DONE_ERR | (uint32_t)err));
+}
+
+/* Complete in-flight copies whose data has landed (in issue order). */
 static void drain(gfs_ctx* c, Worker* w, bool block) {
     while (w->nbusy) {
         int k = w->oldest;
@@ -197,7 +256,8 @@ static void drain(gfs_ctx* c, Worker* w, bool block) {
         cudaError_t e = block ? cudaEventSynchronize(w->ev[(size_t)k]) : cudaEventQuery(w->ev[(size_t)k]);
         if (e == cudaErrorNotReady) return;
         Pending p = w->pend[(size_t)k];
-        set_done(c, p.done, e == cudaSuccess ? p.code : (GFS_DONE_ERR | (uint32_t)EIO));
+        if (p.write && e == cudaSuccess) finish_write(c, w, k, p);
+        else set_done(c, p.done, e == cudaSuccess ? p.code : (GFS_DONE_ERR | (uint32_t)EIO));
         w->busy[(size_t)k] = 0;
         w->oldest = (k + 1) % w->depth;
         w->nbusy--;
@@ -308,6 +368,11 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
                 rep.size = (uint64_t)st.st_size;
                 rep.ctime_ns = (int64_t)st.st_ctim.tv_sec * 1000000000LL + st.st_ctim.tv_nsec;
                 if ((host_open_flags(r.oflags) & O_ACCMODE) == O_RDONLY) map_attach(c, fd, st);
+                if ((size_t)fd < c->fd_info.size()) {
+                    FdInfo* fi = new FdInfo();
+                    fi->size_at_open = (uint64_t)st.st_size;
+                    delete c->fd_info[(size_t)fd].exchange(fi, std::memory_order_acq_rel);
+                }
             }
         }
         if (r.file < c->hs.n_files) {
@@ -321,6 +386,8 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
     }
     case GFS_OP_CLOSE: {
         map_detach(c, r.host_fd);
+        if (r.host_fd >= 0 && (size_t)r.host_fd < c->fd_info.size())
+            delete c->fd_info[(size_t)r.host_fd].exchange(nullptr, std::memory_order_acq_rel);
         int rc = r.host_fd >= 0 ? close(r.host_fd) : 0;
         set_done(c, done, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno));
         break;
@@ -393,6 +460,7 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         break;
     }
     case GFS_OP_WRITE: {
+        /* device -> staging now; merge and pwrite when the copy has landed */
         size_t len = (size_t)r.length;
         if (len > w->slot_bytes) len = w->slot_bytes;
         int k = slot_take(c, w);
@@ -400,25 +468,21 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         cudaError_t e = cudaMemcpyAsync(buf, (const void*)(uintptr_t)r.dev_addr, len, cudaMemcpyDeviceToHost,
                                         w->stream);
         if (e == cudaSuccess) e = cudaEventRecord(w->ev[(size_t)k], w->stream);
-        if (e == cudaSuccess) e = cudaEventSynchronize(w->ev[(size_t)k]);
-        drain(c, w, false); /* earlier reads on this stream have landed too */
         if (e != cudaSuccess) {
             log_failure(c, r, EIO);
             set_done(c, done, GFS_DONE_ERR | (uint32_t)EIO);
             break;
         }
-        if (r.rflags & GFS_RF_DIFF) {
-            /* write-once pages were never read: OR them into what is there
-             * (diff_and_merge, host_loop.h:76-137) */
-            ssize_t m = pread_full(r.host_fd, w->merge, len, (off_t)r.offset);
-            for (ssize_t i = 0; i < m; i++) buf[i] |= w->merge[i];
-        }
-        ssize_t put = pwrite_full(r.host_fd, buf, len, (off_t)r.offset);
-        int err = put < 0 ? errno : EIO;
-        c->h_writes++;
-        if (put >= 0) c->h_write_bytes += (unsigned long long)put;
-        if (put != (ssize_t)len) log_failure(c, r, err);
-        set_done(c, done, put == (ssize_t)len ? 1u + (uint32_t)len : (GFS_DONE_ERR | (uint32_t)err));
+        Pending pw{done, 0u};
+        pw.write = 1;
+        pw.host_fd = r.host_fd;
+        pw.offset = r.offset;
+        pw.len = len;
+        pw.rflags = r.rflags;
+        w->pend[(size_t)k] = pw;
+        w->busy[(size_t)k] = 1;
+        w->nbusy++;
+        drain(c, w, false);
         break;
     }
     case GFS_OP_TRUNC: {
@@ -449,8 +513,14 @@ static void worker_main(gfs_ctx* c, Worker* w) {
         unsigned spins = 0;
         while (__atomic_load_n(&slot->seq, __ATOMIC_ACQUIRE) != t + 1u) {
             if (c->stop.load(std::memory_order_relaxed)) return;
-            if ((++spins & 63u) == 0) drain(c, w, false);
-            if (spins < 4096u) continue;
+            if (w->nbusy) {
+                /* copies in flight: complete them as they land (a device
+                 * thread may be waiting on one); no backing off meanwhile */
+                drain(c, w, false);
+                spins = 0;
+                continue;
+            }
+            if (spins++ < 4096u) continue;
             if (spins < 8192u) {
                 sched_yield();
                 continue;
@@ -567,6 +637,8 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
             nfd = (size_t)rl.rlim_cur;
         c->fd_map = std::vector<std::atomic<FileMap*>>(nfd);
         for (auto& a : c->fd_map) a.store(nullptr);
+        c->fd_info = std::vector<std::atomic<FdInfo*>>(nfd);
+        for (auto& a : c->fd_info) a.store(nullptr);
         const long pages = sysconf(_SC_PHYS_PAGES), psz = sysconf(_SC_PAGESIZE);
         c->map_cap = pages > 0 && psz > 0 ? (size_t)pages * (size_t)psz / 2 : (size_t)8 << 30;
     }
@@ -664,6 +736,7 @@ int gfs_destroy(gfs_ctx* c) {
     c->workers.clear();
     for (FileMap* m : c->maps) map_release(m);
     c->maps.clear();
+    for (auto& a : c->fd_info) delete a.exchange(nullptr);
     gfs_state& s = c->hs;
     gfs_state* none = nullptr;
     if (c->ds && g_current == c) {
