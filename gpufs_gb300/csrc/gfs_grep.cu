@@ -137,17 +137,17 @@ __device__ __forceinline__ uint32_t is_alpha(uint32_t c) {
 }
 
 /* key of a token of len <= 16 at byte st of a 4-byte aligned smem buffer
- * readable 20 bytes past (st & ~3): five word loads, funnel shifts, and a
- * clamp mask per word (no branches) */
-__device__ __forceinline__ void key16(const uint8_t* base, uint32_t st, uint32_t len, uint32_t k[4]) {
+ * readable 20 bytes past (st & ~3): five word loads, funnel shifts, and the
+ * byte masks of its length from a 17-entry table in shared memory */
+__device__ __forceinline__ void key16(const uint8_t* base, uint32_t st, uint32_t len, uint32_t k[4], const uint4* km) {
     const uint32_t* w = (const uint32_t*)(base + (st & ~3u));
     const uint32_t sh = (st & 3u) * 8u;
     const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], x3 = w[3], x4 = w[4];
-    const int kb = (int)len * 8;
-    k[0] = __funnelshift_r(x0, x1, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb, 0));
-    k[1] = __funnelshift_r(x1, x2, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 32, 0));
-    k[2] = __funnelshift_r(x2, x3, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 64, 0));
-    k[3] = __funnelshift_r(x3, x4, sh) & __funnelshift_lc(0xFFFFFFFFu, 0u, (uint32_t)max(kb - 96, 0));
+    const uint4 m = km[len];
+    k[0] = __funnelshift_r(x0, x1, sh) & m.x;
+    k[1] = __funnelshift_r(x1, x2, sh) & m.y;
+    k[2] = __funnelshift_r(x2, x3, sh) & m.z;
+    k[3] = __funnelshift_r(x3, x4, sh) & m.w;
 }
 
 /* key of any len <= 32 (slow path): 9 word loads */
@@ -232,6 +232,7 @@ struct Shared {
     uint32_t win;
     uint32_t next_item; /* consumers take (chunk, segment) items in order */
     uint64_t wait_ns;   /* bound on every mbarrier wait (session timeout) */
+    uint4 kmask[17];    /* key byte masks by token length 0..16 */
 };
 
 __device__ __forceinline__ void fail(Shared& sh, const GrepDev& P, int e, uint32_t site) {
@@ -307,8 +308,9 @@ __device__ __forceinline__ uint32_t cands16(const GrepDev& P, const Tbl& t, cons
     const uint2 q2 = ((const uint2*)t.tags)[b2];
     *b1o = b1;
     *b2o = b2;
+    /* when b2 == b1 the second half repeats the first: harmless */
     uint32_t m = z16(q1.x, tt) | (z16(q1.y, tt) >> 1);
-    if (b2 != b1) m |= (z16(q2.x, tt) >> 2) | (z16(q2.y, tt) >> 3);
+    m |= (z16(q2.x, tt) >> 2) | (z16(q2.y, tt) >> 3);
     return m;
 }
 /* slot of the candidate at the highest set bit of m */
@@ -338,7 +340,7 @@ __device__ __forceinline__ uint32_t other_cands16(const GrepDev& P, const Tbl& t
 
 template <bool SMEM>
 __device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, const uint8_t* base, const StageDesc& d,
-                                             uint32_t segi, uint8_t* wscr) {
+                                             uint32_t segi, uint8_t* wscr, const uint4* km) {
     const int lane = threadIdx.x & 31;
     uint32_t* bm = (uint32_t*)wscr;
     uint16_t* slist = (uint16_t*)(wscr + GR_BM_WORDS * 4);
@@ -385,8 +387,8 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, c
         const uint32_t len0 = v0 ? run_len(bm, st0 - seg0) : 0u, len1 = v1 ? run_len(bm, st1 - seg0) : 0u;
         const bool f0 = v0 && len0 <= 16u, f1 = v1 && len1 <= 16u;
         uint32_t k0[4], k1[4];
-        key16(base, st0, f0 ? len0 : 0u, k0);
-        key16(base, st1, f1 ? len1 : 0u, k1);
+        key16(base, st0, f0 ? len0 : 0u, k0, km);
+        key16(base, st1, f1 ? len1 : 0u, k1, km);
         uint32_t b10, b20, b11, b21;
         const uint32_t m0 = f0 ? cands16(P, tbl, k0, len0, &b10, &b20) : 0u;
         const uint32_t m1 = f1 ? cands16(P, tbl, k1, len1, &b11, &b21) : 0u;
@@ -624,6 +626,14 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
         sh.abort = 0;
         sh.err = 0;
         sh.next_item = 0;
+        for (uint32_t L = 0; L <= 16u; L++) {
+            uint32_t mw[4];
+            for (uint32_t i = 0; i < 4u; i++) {
+                const int b = (int)L * 8 - 32 * (int)i;
+                mw[i] = b >= 32 ? 0xFFFFFFFFu : (b <= 0 ? 0u : (1u << b) - 1u);
+            }
+            sh.kmask[L] = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+        }
         sh.wait_ns = S->timeout_ns;
         uint32_t w = P.win_pages ? P.win_pages : GR_WIN;
         const uint32_t mw = (uint32_t)((GR_LB + GR_CH + GR_LA + S->page_size - 1) / S->page_size) + 1u;
@@ -669,7 +679,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
         ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
         if (ok && !sh.abort) {
             const StageDesc d = sh.desc[s];
-            scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % GR_CONS, wscr);
+            scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % GR_CONS, wscr, sh.kmask);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&sh.empty[s]);
