@@ -85,6 +85,7 @@ _SIGS = {
     "gfs_grep_info": (_int, [_c_p, ctypes.POINTER(ctypes.c_longlong), _int]),
     "gfs_grep_close": (_int, [_c_p]),
     "gfs_grep_text": (_int, [_c_p, _c_s, ctypes.POINTER(_c_s), _int, _c_p, _int]),
+    "gfs_grep_batch": (_int, [_c_p, _int, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_float)]),
     "gfs_grep_bench": (_int, [_c_p, _int, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "gfs_drop_cache": (_i64, [_c_p]),
     "gfs_bigmatrix": (_int, [_c_p, _c_s, _c_s, _c_s, _int, _int, ctypes.POINTER(ctypes.c_float)]),
@@ -298,6 +299,19 @@ class Grep:
             raise GfsError(-rc, "gfs_grep_run failed: status 0x%x site 0x%x, session %s" % (
                 self.status, self.status_site, self.s.error_report()))
         return ms.value
+
+    def batch(self, n_ctas=0):
+        """Batched form: counts and per-file XXH64 in one persistent graph
+        launch; returns (xxh64 list, kernel ms).  counts() then holds the
+        counts."""
+        out = (ctypes.c_ulonglong * max(self.n_files, 1))()
+        ms = ctypes.c_float(0)
+        rc = self.s.L.gfs_grep_batch(self._h, n_ctas, out, ctypes.byref(ms))
+        if rc < 0:
+            self._info()
+            raise GfsError(-rc, "gfs_grep_batch failed: status 0x%x site 0x%x, session %s" % (
+                self.status, self.status_site, self.s.error_report()))
+        return [int(v) for v in out[:self.n_files]], ms.value
 
     def counts(self):
         out = np.zeros((self.n_words, self.n_files), dtype=np.uint32)

@@ -27,6 +27,7 @@
 #include "fs_calls.cu.h"
 #include "gfs_device.cuh"
 #include "gfs_block.cuh"
+#include "gfs_xxh64.cuh"
 #include "gfs_runtime.h"
 
 extern __device__ gfs_state* g_gfs;
@@ -175,24 +176,7 @@ __global__ void k_bigmatrix(const char* f_v, const char* f_m, const char* f_o, f
         res[blockIdx.x] = result ? result : (c0 < 0 ? c0 : (c1 < 0 ? c1 : (c2 < 0 ? c2 : (long long)(r1 > r0 ? r1 - r0 : 0))));
 }
 
-/* ---------------- XXH64 (public xxHash specification) ---------------- */
-#define XP1 0x9E3779B185EBCA87ULL
-#define XP2 0xC2B2AE3D27D4EB4FULL
-#define XP3 0x165667B19E3779F9ULL
-#define XP4 0x85EBCA77C2B2AE63ULL
-#define XP5 0x27D4EB2F165667C5ULL
-
-__device__ __forceinline__ uint64_t xrotl(uint64_t x, int r) { return (x << r) | (x >> (64 - r)); }
-__device__ __forceinline__ uint64_t xround(uint64_t acc, uint64_t in) {
-    acc += in * XP2;
-    acc = xrotl(acc, 31);
-    return acc * XP1;
-}
-__device__ __forceinline__ uint64_t xmerge(uint64_t acc, uint64_t v) {
-    acc ^= xround(0, v);
-    return acc * XP1 + XP4;
-}
-
+/* ---------------- XXH64 (gfs_xxh64.cuh, public xxHash specification) ---------------- */
 /* One warp per file: pages are pinned one at a time by lane 0; every 512
  * bytes are staged in shared memory by the whole warp (16 B per lane) and
  * lanes 0..3 run the four accumulator lanes of the stripes over them.  The
@@ -206,7 +190,7 @@ __global__ void k_xxh64(const int* fds, const uint64_t* sizes, int n, unsigned l
     for (int f = (int)(blockIdx.x * warps) + wib; f < n; f += (int)(gridDim.x * warps)) {
         const uint64_t size = sizes[f];
         gfsd::PinFile pf = gfsd::pin_file(S, fds[f]);
-        uint64_t v1 = XP1 + XP2, v2 = XP2, v3 = 0, v4 = 0ULL - XP1;
+        uint64_t v1 = gfsx::acc_init(0), v2 = gfsx::acc_init(1), v3 = gfsx::acc_init(2), v4 = gfsx::acc_init(3);
         const uint64_t body = size >= 32 ? size / 32 * 32 : 0;
         /* stripes are consumed 512 bytes at a time; a page holds whole 512s */
         int fr = -1;
@@ -231,7 +215,7 @@ __global__ void k_xxh64(const int* fds, const uint64_t* sizes, int n, unsigned l
             __syncwarp();
             if (lane < 4) {
                 uint64_t v = lane == 0 ? v1 : lane == 1 ? v2 : lane == 2 ? v3 : v4;
-                for (uint32_t s = 0; s < chunk / 32; s++) v = xround(v, *(const uint64_t*)(st + s * 32 + lane * 8));
+                v = gfsx::acc_stripes(v, st, (uint32_t)(chunk / 32), lane);
                 if (lane == 0) v1 = v; else if (lane == 1) v2 = v; else if (lane == 2) v3 = v; else v4 = v;
             }
             __syncwarp();
@@ -241,17 +225,6 @@ __global__ void k_xxh64(const int* fds, const uint64_t* sizes, int n, unsigned l
         v3 = __shfl_sync(0xFFFFFFFFu, v3, 2);
         v4 = __shfl_sync(0xFFFFFFFFu, v4, 3);
         if (lane == 0 && !bad) {
-            uint64_t h;
-            if (size >= 32) {
-                h = xrotl(v1, 1) + xrotl(v2, 7) + xrotl(v3, 12) + xrotl(v4, 18);
-                h = xmerge(h, v1);
-                h = xmerge(h, v2);
-                h = xmerge(h, v3);
-                h = xmerge(h, v4);
-            } else {
-                h = XP5;
-            }
-            h += size;
             /* tail bytes [body, size) */
             uint8_t tail[32];
             for (uint64_t q = body; q < size && !bad; q++) {
@@ -266,30 +239,7 @@ __global__ void k_xxh64(const int* fds, const uint64_t* sizes, int n, unsigned l
                 }
                 tail[q - body] = S->pool[((size_t)fr << S->log_page) + (q & (S->page_size - 1u))];
             }
-            uint32_t tn = (uint32_t)(size - body), i = 0;
-            for (; i + 8 <= tn; i += 8) {
-                uint64_t k = 0;
-                for (int b = 7; b >= 0; b--) k = (k << 8) | tail[i + b];
-                h ^= xround(0, k);
-                h = xrotl(h, 27) * XP1 + XP4;
-            }
-            if (i + 4 <= tn) {
-                uint64_t k = (uint64_t)tail[i] | ((uint64_t)tail[i + 1] << 8) | ((uint64_t)tail[i + 2] << 16) |
-                             ((uint64_t)tail[i + 3] << 24);
-                h ^= k * XP1;
-                h = xrotl(h, 23) * XP2 + XP3;
-                i += 4;
-            }
-            for (; i < tn; i++) {
-                h ^= (uint64_t)tail[i] * XP5;
-                h = xrotl(h, 11) * XP1;
-            }
-            h ^= h >> 33;
-            h *= XP2;
-            h ^= h >> 29;
-            h *= XP3;
-            h ^= h >> 32;
-            out[f] = h;
+            if (!bad) out[f] = gfsx::finish(v1, v2, v3, v4, size, tail);
         }
         if (lane == 0 && fr >= 0) gfsd::unpin(S, (uint32_t)fr);
         bad = __shfl_sync(0xFFFFFFFFu, bad, 0);

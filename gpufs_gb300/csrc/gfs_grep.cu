@@ -48,13 +48,16 @@
 #include "gfs_device.cuh"
 #include "gfs_block.cuh"
 #include "gfs_grep_common.h"
+#include "gfs_xxh64.cuh"
 #include "gfs_runtime.h"
 #include "gpufs_gb300.h"
 
 #define GR_CONS 31                    /* consumer warps; warp 31 is the producer */
+#define GR_CONS_B 30                  /* batched scan: consumers; warp 30 hashes */
 #define GR_THREADS 1024
 #define GR_SEG 512                    /* bytes per consumer warp per chunk */
 #define GR_CH (GR_CONS * GR_SEG)      /* 15872-byte chunks */
+#define GR_CH_B (GR_CONS_B * GR_SEG)  /* 15360-byte chunks of the batched scan */
 #define GR_LB 16                      /* look-behind bytes staged before a chunk */
 #define GR_LA 64                      /* look-ahead bytes staged after it */
 #define GR_STAGE (GR_LB + GR_CH + GR_LA + 32)
@@ -81,6 +84,10 @@ struct GrepDev {
     uint32_t* long_flags;         /* per file: a run of >= 33 letters was seen */
     uint32_t* status;             /* [0] error bits, [1] first failure: site << 16 | errno */
     uint32_t win_pages;           /* pages per window (two windows per CTA may be pinned) */
+    /* batched scan: CTAs take whole files, longest first, and hash them */
+    const int* file_order;        /* file indices by decreasing size */
+    uint32_t* file_next;          /* next position in file_order */
+    unsigned long long* xxh;      /* per-file XXH64 */
 };
 
 namespace {
@@ -115,7 +122,8 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;" ::"r"(GR_CONS * 32) : "memory"); }
+template <int NC>
+__device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;" ::"r"(NC * 32) : "memory"); }
 
 /* ---------------- byte classification ---------------- */
 /* bit 7 of each byte of the result is set iff the byte is [A-Za-z_] */
@@ -216,10 +224,10 @@ __device__ void lookup_count(const GrepDev& P, const Tbl& t, bool smem, const ui
 
 struct StageDesc {
     uint64_t pos;   /* file offset of chunk byte 0 */
-    int f;          /* file */
+    int f;          /* file; -1 marks the end of a batched CTA's work */
     uint32_t clen;  /* chunk bytes */
     uint32_t avail; /* staged bytes from chunk byte 0 (chunk + look-ahead, to end of file) */
-    uint32_t pad;
+    uint32_t fseq;  /* batched scan: the file's number among this CTA's files */
 };
 
 struct Shared {
@@ -233,6 +241,8 @@ struct Shared {
     uint32_t next_item; /* consumers take (chunk, segment) items in order */
     uint64_t wait_ns;   /* bound on every mbarrier wait (session timeout) */
     uint4 kmask[17];    /* key byte masks by token length 0..16 */
+    int fileseq[8];     /* batched scan: file of fseq j at [j & 7] */
+    uint64_t cbar;      /* batched scan: the consumers' flush barrier (bounded waits) */
 };
 
 __device__ __forceinline__ void fail(Shared& sh, const GrepDev& P, int e, uint32_t site) {
@@ -421,11 +431,11 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, c
     }
 }
 
-template <bool SMEM>
+template <bool SMEM, int NC>
 __device__ void flush_counts(const GrepDev& P, const Tbl& t, int f) {
     if (!SMEM) return;
     const uint32_t nslots = 4u * P.nb;
-    for (uint32_t i = threadIdx.x; i < nslots; i += GR_CONS * 32) {
+    for (uint32_t i = threadIdx.x; i < nslots; i += NC * 32) {
         const uint32_t n = t.cnt[i];
         if (n) {
             t.cnt[i] = 0u;
@@ -467,119 +477,156 @@ __device__ void unpin_window(gfs_state* S, Shared& sh, Window& w) {
     w.live = false;
 }
 
-__device__ void producer(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* stages, uint64_t c0, uint64_t c1) {
+/* Stream chunks [k, kend) of file f (chunk size CH) into the stage ring,
+ * pinning page windows as it goes; g counts the chunks this CTA produced.
+ * false: aborted. */
+template <uint32_t CH>
+__device__ bool stream_file(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* stages, int f, uint32_t fseq,
+                            uint64_t k, uint64_t kend, Window& prev, uint32_t& g) {
     const int lane = threadIdx.x & 31;
     const uint32_t lp = S->log_page, page = S->page_size, pmask = page - 1u;
-    Window prev = {0, 0, 1, 0, false};
-    uint32_t g = 0;
     /* pages one chunk with its look-behind and look-ahead can touch */
-    const uint32_t minwin = (uint32_t)((GR_LB + GR_CH + GR_LA + page - 1) / page) + 1u;
-    uint64_t c = c0;
-    while (c < c1) {
-        const int f = file_of(P, c);
-        const uint64_t fsize = P.sizes[f];
-        const uint64_t kend = (P.chunk_prefix[f + 1] < c1 ? P.chunk_prefix[f + 1] : c1) - P.chunk_prefix[f];
-        uint64_t k = c - P.chunk_prefix[f];
-        while (k < kend) {
-            /* window: chunks [k, kw) whose bytes, look-behind and look-ahead
-             * lie in at most sh.win pages */
-            const uint64_t lbpos = k * GR_CH >= GR_LB ? k * GR_CH - GR_LB : 0;
-            const uint32_t lb = (uint32_t)(lbpos >> lp);
-            uint64_t kw;
-            uint32_t n;
-            int buf = prev.buf ^ 1;
-            int e = 0;
-            bool hard = false;
-            for (;;) {
-                const uint64_t lim = ((uint64_t)lb + sh.win) << lp; /* first byte not covered */
-                kw = lim >= fsize + GR_LA ? kend : (lim > GR_LA ? (lim - GR_LA) / GR_CH : 0);
-                if (kw > kend) kw = kend;
-                if (kw <= k) kw = k + 1; /* a window always holds at least one chunk */
-                uint64_t endb = kw * GR_CH + GR_LA;
-                if (endb > fsize) endb = fsize;
-                n = (uint32_t)(((endb + pmask) >> lp) - lb);
-                if (n > GR_WIN) { kw = k + 1; endb = kw * GR_CH + GR_LA < fsize ? kw * GR_CH + GR_LA : fsize; n = (uint32_t)(((endb + pmask) >> lp) - lb); }
-                e = pin_pages(S, sh, buf, P.fds[f], lb, n, hard ? false : true);
-                if (e == -GFS_ENOMEM && !hard) {
-                    /* the pool is short: shrink the window; at the smallest
-                     * window drop the previous one first, then wait for frames */
-                    if (sh.win > minwin) {
-                        if (lane == 0) sh.win = sh.win / 2 > minwin ? sh.win / 2 : minwin;
-                    } else if (prev.live) {
-                        if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, 7);
-                        __syncwarp();
-                        unpin_window(S, sh, prev);
-                    } else {
-                        hard = true;
-                    }
+    const uint32_t minwin = (uint32_t)((GR_LB + CH + GR_LA + page - 1) / page) + 1u;
+    const uint64_t fsize = P.sizes[f];
+    while (k < kend) {
+        /* window: chunks [k, kw) whose bytes, look-behind and look-ahead
+         * lie in at most sh.win pages */
+        const uint64_t lbpos = k * CH >= GR_LB ? k * CH - GR_LB : 0;
+        const uint32_t lb = (uint32_t)(lbpos >> lp);
+        uint64_t kw;
+        uint32_t n;
+        int buf = prev.buf ^ 1;
+        int e = 0;
+        bool hard = false;
+        for (;;) {
+            const uint64_t lim = ((uint64_t)lb + sh.win) << lp; /* first byte not covered */
+            kw = lim >= fsize + GR_LA ? kend : (lim > GR_LA ? (lim - GR_LA) / CH : 0);
+            if (kw > kend) kw = kend;
+            if (kw <= k) kw = k + 1; /* a window always holds at least one chunk */
+            uint64_t endb = kw * CH + GR_LA;
+            if (endb > fsize) endb = fsize;
+            n = (uint32_t)(((endb + pmask) >> lp) - lb);
+            if (n > GR_WIN) { kw = k + 1; endb = kw * CH + GR_LA < fsize ? kw * CH + GR_LA : fsize; n = (uint32_t)(((endb + pmask) >> lp) - lb); }
+            e = pin_pages(S, sh, buf, P.fds[f], lb, n, hard ? false : true);
+            if (e == -GFS_ENOMEM && !hard) {
+                /* the pool is short: shrink the window; at the smallest
+                 * window drop the previous one first, then wait for frames */
+                if (sh.win > minwin) {
+                    if (lane == 0) sh.win = sh.win / 2 > minwin ? sh.win / 2 : minwin;
+                } else if (prev.live) {
+                    if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, 7);
                     __syncwarp();
-                    continue;
+                    unpin_window(S, sh, prev);
+                } else {
+                    hard = true;
                 }
-                break;
-            }
-            if (e) {
-                if (lane == 0) fail(sh, P, e, 2);
                 __syncwarp();
-                break;
+                continue;
             }
-            /* the previous window's copies have all landed once its last
-             * chunk's full phase completed (its stage is not re-armed yet) */
-            if (prev.live) {
-                if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, 3);
-                __syncwarp();
-                unpin_window(S, sh, prev);
-            }
-            for (uint64_t kk = k; kk < kw; kk++, g++) {
-                const uint32_t s = g % GR_STAGES;
-                if (lane == 0) {
-                    bool ok = true;
-                    if (g >= GR_STAGES) ok = wait_phase(sh, P, &sh.empty[s], ((g / GR_STAGES) - 1u) & 1u, 4);
-                    const uint64_t pos = kk * GR_CH;
-                    const uint64_t rem = fsize - pos;
-                    StageDesc& dsc = sh.desc[s];
-                    dsc.pos = pos;
-                    dsc.f = f;
-                    dsc.clen = (uint32_t)(rem < GR_CH ? rem : GR_CH);
-                    dsc.avail = (uint32_t)(rem < (uint64_t)GR_CH + GR_LA ? rem : (uint64_t)GR_CH + GR_LA);
-                    uint8_t* dst = stages + (size_t)s * GR_STAGE;
-                    if (!ok || sh.abort) {
-                        mbar_arrive(&sh.full[s]); /* release the consumers; they see abort */
-                    } else {
-                        const uint32_t body = (dsc.avail + 15u) & ~15u;
-                        const uint32_t lbb = pos > 0 ? (uint32_t)GR_LB : 0u;
-                        fence_proxy_async();
-                        mbar_expect_tx(&sh.full[s], lbb + body);
-                        uint64_t from = pos - lbb;
-                        uint32_t done = 0, total = lbb + body;
-                        while (done < total) {
-                            const uint64_t q = from + done;
-                            const uint32_t pg = (uint32_t)(q >> lp);
-                            const uint32_t inpg = (uint32_t)(q & pmask);
-                            uint32_t piece = page - inpg;
-                            if (piece > total - done) piece = total - done;
-                            const uint8_t* src = S->pool + ((size_t)sh.frames[buf][pg - lb] << lp) + inpg;
-                            bulk_g2s(dst + (GR_LB - lbb) + done, src, piece, &sh.full[s]);
-                            done += piece;
-                        }
+            break;
+        }
+        if (e) {
+            if (lane == 0) fail(sh, P, e, 2);
+            __syncwarp();
+            return false;
+        }
+        /* the previous window's copies have all landed once its last
+         * chunk's full phase completed (its stage is not re-armed yet) */
+        if (prev.live) {
+            if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, 3);
+            __syncwarp();
+            unpin_window(S, sh, prev);
+        }
+        for (uint64_t kk = k; kk < kw; kk++, g++) {
+            const uint32_t s = g % GR_STAGES;
+            if (lane == 0) {
+                bool ok = true;
+                if (g >= GR_STAGES) ok = wait_phase(sh, P, &sh.empty[s], ((g / GR_STAGES) - 1u) & 1u, 4);
+                const uint64_t pos = kk * CH;
+                const uint64_t rem = fsize - pos;
+                StageDesc& dsc = sh.desc[s];
+                dsc.pos = pos;
+                dsc.f = f;
+                dsc.fseq = fseq;
+                dsc.clen = (uint32_t)(rem < CH ? rem : CH);
+                dsc.avail = (uint32_t)(rem < (uint64_t)CH + GR_LA ? rem : (uint64_t)CH + GR_LA);
+                uint8_t* dst = stages + (size_t)s * GR_STAGE;
+                if (!ok || sh.abort) {
+                    mbar_arrive(&sh.full[s]); /* release the consumers; they see abort */
+                } else {
+                    const uint32_t body = (dsc.avail + 15u) & ~15u;
+                    const uint32_t lbb = pos > 0 ? (uint32_t)GR_LB : 0u;
+                    fence_proxy_async();
+                    mbar_expect_tx(&sh.full[s], lbb + body);
+                    uint64_t from = pos - lbb;
+                    uint32_t done = 0, total = lbb + body;
+                    while (done < total) {
+                        const uint64_t q = from + done;
+                        const uint32_t pg = (uint32_t)(q >> lp);
+                        const uint32_t inpg = (uint32_t)(q & pmask);
+                        uint32_t piece = page - inpg;
+                        if (piece > total - done) piece = total - done;
+                        const uint8_t* src = S->pool + ((size_t)sh.frames[buf][pg - lb] << lp) + inpg;
+                        bulk_g2s(dst + (GR_LB - lbb) + done, src, piece, &sh.full[s]);
+                        done += piece;
                     }
                 }
-                __syncwarp();
             }
-            prev.lb = lb;
-            prev.n = n;
-            prev.buf = buf;
-            prev.last_g = g - 1u;
-            prev.live = true;
-            k = kw;
+            __syncwarp();
         }
-        if (sh.abort) break;
-        c = P.chunk_prefix[f] + kend;
+        prev.lb = lb;
+        prev.n = n;
+        prev.buf = buf;
+        prev.last_g = g - 1u;
+        prev.live = true;
+        k = kw;
+        if (sh.abort) return false;
     }
+    return true;
+}
+
+__device__ void release_window(gfs_state* S, const GrepDev& P, Shared& sh, Window& prev, uint32_t site) {
+    const int lane = threadIdx.x & 31;
     if (prev.live) {
-        if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, 5);
+        if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, site);
         __syncwarp();
         unpin_window(S, sh, prev);
     }
+}
+
+/* A stage with no bytes (an empty file, or f = -1: the end of a batched
+ * CTA's work): published by arriving on its full barrier without a copy. */
+__device__ void emit_marker(const GrepDev& P, Shared& sh, int f, uint32_t fseq, uint32_t& g) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t s = g % GR_STAGES;
+    if (lane == 0) {
+        if (g >= GR_STAGES) wait_phase(sh, P, &sh.empty[s], ((g / GR_STAGES) - 1u) & 1u, 6);
+        StageDesc& dsc = sh.desc[s];
+        dsc.pos = 0;
+        dsc.f = f;
+        dsc.fseq = fseq;
+        dsc.clen = 0;
+        dsc.avail = 0;
+        mbar_arrive(&sh.full[s]);
+    }
+    __syncwarp();
+    g++;
+}
+
+/* Producer of the plain scan: the CTA's static run of chunks [c0, c1) of
+ * the concatenated corpus. */
+__device__ void producer(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* stages, uint64_t c0, uint64_t c1) {
+    const int lane = threadIdx.x & 31;
+    Window prev = {0, 0, 1, 0, false};
+    uint32_t g = 0;
+    uint64_t c = c0;
+    while (c < c1) {
+        const int f = file_of(P, c);
+        const uint64_t kend = (P.chunk_prefix[f + 1] < c1 ? P.chunk_prefix[f + 1] : c1) - P.chunk_prefix[f];
+        if (!stream_file<GR_CH>(S, P, sh, stages, f, 0u, c - P.chunk_prefix[f], kend, prev, g)) break;
+        c = P.chunk_prefix[f] + kend;
+    }
+    release_window(S, P, sh, prev, 5);
     /* chunks never produced after an abort: release their consumers */
     if (sh.abort && lane == 0) {
         uint64_t total = c1 - c0;
@@ -593,12 +640,87 @@ __device__ void producer(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* st
     }
 }
 
+/* Producer of the batched scan: whole files from the shared queue (longest
+ * first), each numbered in sequence for the consumers' per-file flushes;
+ * an empty file is one empty stage (the hasher still finishes its XXH64);
+ * the end is an f = -1 stage numbered one past the last file. */
+__device__ void producer_batch(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* stages) {
+    const int lane = threadIdx.x & 31;
+    Window prev = {0, 0, 1, 0, false};
+    uint32_t g = 0, fseq = 0;
+    for (;;) {
+        int f = -1;
+        if (lane == 0) {
+            const uint32_t i = atomicAdd(P.file_next, 1u);
+            f = i < (uint32_t)P.n_files ? P.file_order[i] : -1;
+        }
+        f = __shfl_sync(0xFFFFFFFFu, f, 0);
+        if (f < 0 || sh.abort) break;
+        if (lane == 0) sh.fileseq[fseq & 7u] = f;
+        __syncwarp();
+        const uint64_t nch = (P.sizes[f] + GR_CH_B - 1) / GR_CH_B;
+        if (nch == 0) emit_marker(P, sh, f, fseq, g);
+        else if (!stream_file<GR_CH_B>(S, P, sh, stages, f, fseq, 0, nch, prev, g)) break;
+        fseq++;
+    }
+    release_window(S, P, sh, prev, 5);
+    emit_marker(P, sh, -1, fseq, g);
+}
+
 } // namespace
 
+/* The batched scan's consumer barrier (the n-th one a warp passes): an
+ * mbarrier of NC arrivals with a bounded wait, so a warp that gave up
+ * (timeout, abort) cannot leave the others waiting forever.  false: give up. */
+__device__ __forceinline__ bool cbar_wait(Shared& sh, const GrepDev& P, uint32_t n) {
+    __syncwarp();
+    bool ok = true;
+    if ((threadIdx.x & 31) == 0) {
+        mbar_arrive(&sh.cbar);
+        ok = wait_phase(sh, P, &sh.cbar, n & 1u, 9);
+    }
+    return __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
+}
+
+/* The batched scan's hasher warp: the XXH64 of each file, over the staged
+ * chunks in order (chunks are whole 32-byte stripes except a file's last),
+ * lanes 0..3 carrying the four accumulators; it releases every stage it has
+ * read like a consumer. */
+__device__ void hasher(const GrepDev& P, Shared& sh, uint8_t* stages) {
+    const int lane = threadIdx.x & 31;
+    uint64_t v = gfsx::acc_init(lane & 3);
+    for (uint32_t g = 0;; g++) {
+        const uint32_t s = g % GR_STAGES;
+        bool ok = true;
+        if (lane == 0) ok = wait_phase(sh, P, &sh.full[s], (g / GR_STAGES) & 1u, 8);
+        ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
+        const StageDesc d = sh.desc[s];
+        if (!ok || d.f < 0) return;
+        if (!sh.abort) {
+            const uint8_t* base = stages + (size_t)s * GR_STAGE + GR_LB;
+            if (d.pos == 0) v = gfsx::acc_init(lane & 3);
+            const uint32_t stripes = d.clen / 32u;
+            if (lane < 4) v = gfsx::acc_stripes(v, base, stripes, lane);
+            const uint64_t size = P.sizes[d.f];
+            if (d.pos + d.clen == size) {
+                const uint64_t v1 = __shfl_sync(0xFFFFFFFFu, v, 0), v2 = __shfl_sync(0xFFFFFFFFu, v, 1),
+                               v3 = __shfl_sync(0xFFFFFFFFu, v, 2), v4 = __shfl_sync(0xFFFFFFFFu, v, 3);
+                if (lane == 0) P.xxh[d.f] = gfsx::finish(v1, v2, v3, v4, size, base + (size_t)stripes * 32u);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sh.empty[s]);
+    }
+}
+
 /* One persistent 1024-thread CTA per SM: warp 31 pins pages and streams
- * chunks (TMA), warps 0..30 scan them; see the file comment. */
-template <bool SMEM>
+ * chunks (TMA), warps 0..30 scan them; see the file comment.  BATCH: the
+ * CTA takes whole files from a shared queue instead of a static run of
+ * chunks, warps 0..29 scan and warp 30 computes each file's XXH64. */
+template <bool SMEM, bool BATCH>
 __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepDev P) {
+    constexpr int NC = BATCH ? GR_CONS_B : GR_CONS;
+    constexpr uint32_t CH = (uint32_t)NC * GR_SEG;
     extern __shared__ __align__(128) uint8_t dsm[];
     __shared__ Shared sh;
     /* shared memory: slot tags (8 B per bucket), slot counters (16 B per
@@ -620,8 +742,9 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
     if (threadIdx.x == 0) {
         for (int s = 0; s < GR_STAGES; s++) {
             mbar_init(&sh.full[s], 1u);
-            mbar_init(&sh.empty[s], GR_CONS);
+            mbar_init(&sh.empty[s], (uint32_t)NC + (BATCH ? 1u : 0u));
         }
+        mbar_init(&sh.cbar, (uint32_t)NC);
         fence_mbar_init();
         sh.abort = 0;
         sh.err = 0;
@@ -636,10 +759,44 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
         }
         sh.wait_ns = S->timeout_ns;
         uint32_t w = P.win_pages ? P.win_pages : GR_WIN;
-        const uint32_t mw = (uint32_t)((GR_LB + GR_CH + GR_LA + S->page_size - 1) / S->page_size) + 1u;
+        const uint32_t mw = (uint32_t)((GR_LB + CH + GR_LA + S->page_size - 1) / S->page_size) + 1u;
         sh.win = w > GR_WIN ? GR_WIN : (w < mw ? mw : w);
     }
     __syncthreads();
+
+    if (BATCH) {
+        if (warp == 31) { producer_batch(S, P, sh, stages); return; }
+        if (warp == NC) { hasher(P, sh, stages); return; }
+        /* Items (chunk, segment) in order from the shared counter, as below;
+         * file boundaries come from the stages: each file is numbered in
+         * sequence, and a warp whose item has a higher number first passes
+         * one flush barrier per file in between, so every warp passes the
+         * same barriers in the same order even if it saw none of a small
+         * file's chunks.  The end marker (f = -1) is numbered one past the
+         * last file, which flushes it. */
+        uint32_t cur = 0, nbar = 0;
+        for (;;) {
+            uint32_t it = 0;
+            if (lane == 0) it = atomicAdd(&sh.next_item, 1u);
+            it = __shfl_sync(0xFFFFFFFFu, it, 0);
+            const uint32_t g = it / NC, s = g % GR_STAGES;
+            bool ok = true;
+            if (lane == 0) ok = wait_phase(sh, P, &sh.full[s], (g / GR_STAGES) & 1u, 1);
+            ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
+            if (!ok) return; /* gave up: the others see the abort in their waits */
+            const StageDesc d = sh.desc[s];
+            while (cur < d.fseq) {
+                if (!cbar_wait(sh, P, nbar++)) return;
+                if (!sh.abort) flush_counts<SMEM, NC>(P, tbl, sh.fileseq[cur & 7u]);
+                if (!cbar_wait(sh, P, nbar++)) return;
+                cur++;
+            }
+            if (d.f < 0) return;
+            if (!sh.abort) scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % NC, wscr, sh.kmask);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sh.empty[s]);
+        }
+    }
 
     const uint64_t total = P.total_chunks;
     const uint64_t c0 = total * blockIdx.x / gridDim.x, c1 = total * (blockIdx.x + 1) / gridDim.x;
@@ -649,14 +806,14 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
     }
     /* Items (chunk, segment) are taken in order from a shared counter, so a
      * warp that finishes early takes the next segment instead of idling
-     * behind the slowest warp of its chunk.  A chunk has exactly GR_CONS
-     * items, one per consumer warp: a chunk's items cannot all be finished
-     * before it has landed, so no warp can take an item of the chunk four
+     * behind the slowest warp of its chunk.  A chunk has exactly NC items,
+     * one per consumer warp: a chunk's items cannot all be finished before
+     * it has landed, so no warp can take an item of the chunk GR_STAGES
      * stages later while its stage still holds an earlier phase (the parity
      * waits stay unambiguous).  Counts are flushed per file: a warp whose
      * item lies beyond the current file waits at the consumers' barrier,
      * which every warp passes once per file in the same order. */
-    const uint32_t nchunks = (uint32_t)(c1 - c0), n_items = nchunks * GR_CONS;
+    const uint32_t nchunks = (uint32_t)(c1 - c0), n_items = nchunks * NC;
     if (nchunks == 0) return;
     int f = file_of(P, c0);
     uint32_t fend = (uint32_t)((P.chunk_prefix[f + 1] < c1 ? P.chunk_prefix[f + 1] : c1) - c0);
@@ -664,11 +821,11 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
         uint32_t it = 0;
         if (lane == 0) it = atomicAdd(&sh.next_item, 1u);
         it = __shfl_sync(0xFFFFFFFFu, it, 0);
-        const uint32_t g = it < n_items ? it / GR_CONS : nchunks;
+        const uint32_t g = it < n_items ? it / NC : nchunks;
         while (g >= fend) {
-            consumers_sync();
-            if (!sh.abort) flush_counts<SMEM>(P, tbl, f);
-            consumers_sync();
+            consumers_sync<NC>();
+            if (!sh.abort) flush_counts<SMEM, NC>(P, tbl, f);
+            consumers_sync<NC>();
             if (fend >= nchunks) return;
             f = file_of(P, c0 + fend);
             fend = (uint32_t)((P.chunk_prefix[f + 1] < c1 ? P.chunk_prefix[f + 1] : c1) - c0);
@@ -679,7 +836,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
         ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
         if (ok && !sh.abort) {
             const StageDesc d = sh.desc[s];
-            scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % GR_CONS, wscr, sh.kmask);
+            scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % NC, wscr, sh.kmask);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&sh.empty[s]);
@@ -776,8 +933,10 @@ __global__ void k_grep_fixup(gfs_state* S, GrepDev P) {
     pc.release();
 }
 
-template __global__ void k_grep_scan<true>(gfs_state*, GrepDev);
-template __global__ void k_grep_scan<false>(gfs_state*, GrepDev);
+template __global__ void k_grep_scan<true, false>(gfs_state*, GrepDev);
+template __global__ void k_grep_scan<false, false>(gfs_state*, GrepDev);
+template __global__ void k_grep_scan<true, true>(gfs_state*, GrepDev);
+template __global__ void k_grep_scan<false, true>(gfs_state*, GrepDev);
 
 /* ------------------------------------------------------------------ */
 /* host side: dictionary table, file opening, launch                   */
@@ -933,6 +1092,9 @@ struct gfs_grep {
     size_t smem_bytes = 0;
     int sms = 0;
     uint32_t last_status[2] = {0, 0};
+    /* batched run: captured once per grid size, replayed */
+    cudaGraphExec_t batch_graph = nullptr;
+    int batch_ctas = 0;
 };
 
 /* Pages per window so that all CTAs' pinned windows (two each) fit in half
@@ -949,8 +1111,10 @@ extern "C" {
 
 void gfs__preload_grep() {
     cudaFuncAttributes a;
-    cudaFuncGetAttributes(&a, k_grep_scan<true>);
-    cudaFuncGetAttributes(&a, k_grep_scan<false>);
+    cudaFuncGetAttributes(&a, k_grep_scan<true, false>);
+    cudaFuncGetAttributes(&a, k_grep_scan<false, false>);
+    cudaFuncGetAttributes(&a, k_grep_scan<true, true>);
+    cudaFuncGetAttributes(&a, k_grep_scan<false, true>);
     cudaFuncGetAttributes(&a, k_grep_fixup);
     cudaFuncGetAttributes(&a, k_open_files);
     cudaFuncGetAttributes(&a, k_close_files);
@@ -991,7 +1155,8 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
            o_fds = align_up(o_cnt + (size_t)g->n_words * n_files * 4 + 4, 256), o_sz = align_up(o_fds + (size_t)n_files * 4, 256),
            o_pf = align_up(o_sz + (size_t)n_files * 8, 256), o_fl = align_up(o_pf + (size_t)(n_files + 1) * 8, 256),
            o_st = align_up(o_fl + (size_t)n_files * 4, 256), o_names = align_up(o_st + 64, 256),
-           total = align_up(o_names + (size_t)n_files * GFS_NAME_MAX, 256);
+           o_fo = align_up(o_names + (size_t)n_files * GFS_NAME_MAX, 256), o_fn = align_up(o_fo + (size_t)n_files * 4, 256),
+           o_xxh = align_up(o_fn + 64, 256), total = align_up(o_xxh + (size_t)n_files * 8, 256);
     if (cudaMalloc(&g->dmem, total) != cudaSuccess) { delete g; return -GFS_ENOMEM; }
     uint8_t* b = (uint8_t*)g->dmem;
     cudaMemset(b, 0, total);
@@ -1025,6 +1190,9 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     d.counts = (uint32_t*)(b + o_cnt);
     d.long_flags = (uint32_t*)(b + o_fl);
     d.status = (uint32_t*)(b + o_st);
+    d.file_order = (const int*)(b + o_fo);
+    d.file_next = (uint32_t*)(b + o_fn);
+    d.xxh = (unsigned long long*)(b + o_xxh);
     cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
     k_open_files<<<n_files, 128, 0, s>>>((const char*)(b + o_names), n_files, (int*)d.fds, (uint64_t*)d.sizes);
     if (cudaStreamSynchronize(s) != cudaSuccess) { gfs_grep_close(g); return -GFS_EIO; }
@@ -1042,13 +1210,24 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     for (int i = 0; i < n_files; i++) pf[(size_t)i + 1] = pf[(size_t)i] + (g->sizes[(size_t)i] + GR_CH - 1) / GR_CH;
     cudaMemcpy((void*)d.chunk_prefix, pf.data(), pf.size() * 8, cudaMemcpyHostToDevice);
     d.total_chunks = pf[(size_t)n_files];
+    {
+        /* batched runs take files longest first (LPT: the largest file
+         * bounds the run, so it starts first) */
+        std::vector<int> order((size_t)n_files);
+        for (int i = 0; i < n_files; i++) order[(size_t)i] = i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int x, int y) { return g->sizes[(size_t)x] > g->sizes[(size_t)y]; });
+        cudaMemcpy((void*)d.file_order, order.data(), order.size() * 4, cudaMemcpyHostToDevice);
+    }
     /* shared memory: table (if it fits) + stages + token lists + scratch */
     g->sms = sms;
     size_t with_tbl = align_up((size_t)nb * 8, 128) + align_up((size_t)nb * 16, 128) + fixed;
     g->smem = with_tbl <= (size_t)maxsm;
     g->smem_bytes = g->smem ? with_tbl : fixed;
-    cudaFuncSetAttribute(k_grep_scan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
-    cudaFuncSetAttribute(k_grep_scan<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
+    cudaFuncSetAttribute(k_grep_scan<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
+    cudaFuncSetAttribute(k_grep_scan<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
+    cudaFuncSetAttribute(k_grep_scan<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
+    cudaFuncSetAttribute(k_grep_scan<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
     *out = g;
     return 0;
 }
@@ -1069,8 +1248,8 @@ int gfs_grep_run(gfs_grep* g, int n_ctas, float* kernel_ms) {
         cudaEventCreate(&b);
         cudaEventRecord(a, s);
     }
-    if (g->smem) k_grep_scan<true><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
-    else k_grep_scan<false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
+    if (g->smem) k_grep_scan<true, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
+    else k_grep_scan<false, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
     cudaError_t le = cudaGetLastError();
     k_grep_fixup<<<g->n_files, 32, 0, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
     if (kernel_ms) {
@@ -1111,8 +1290,8 @@ int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* s
         cudaMemsetAsync(d.counts, 0, (size_t)g->n_words * g->n_files * 4, s);
         cudaMemsetAsync(d.long_flags, 0, (size_t)g->n_files * 4, s);
         cudaEventRecord(ev[2 + 2 * (size_t)i], s);
-        if (g->smem) k_grep_scan<true><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
-        else k_grep_scan<false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+        if (g->smem) k_grep_scan<true, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+        else k_grep_scan<false, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
         cudaEventRecord(ev[3 + 2 * (size_t)i], s);
         k_grep_fixup<<<g->n_files, 32, 0, s>>>(S, d);
     }
@@ -1134,6 +1313,63 @@ int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* s
     g->last_status[0] = status[0];
     g->last_status[1] = status[1];
     return status[0] ? -GFS_EIO : 0;
+}
+
+/* Batched run: every file's dictionary counts and XXH64 in one persistent
+ * launch (CTAs take whole files, longest first), captured as a CUDA graph
+ * on first use and replayed after. */
+int gfs_grep_batch(gfs_grep* g, int n_ctas, unsigned long long* host_xxh, float* kernel_ms) {
+    if (!g) return -GFS_EINVAL;
+    if (gfs__activate(g->ctx)) return -GFS_EIO;
+    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(g->ctx);
+    GrepDev& d = g->dev;
+    if (n_ctas <= 0) n_ctas = g->sms;
+    if (!g->batch_graph || g->batch_ctas != n_ctas) {
+        if (g->batch_graph) cudaGraphExecDestroy(g->batch_graph);
+        g->batch_graph = nullptr;
+        set_window(g, n_ctas);
+        gfs_state* S = (gfs_state*)gfs_device_state(g->ctx);
+        cudaGraph_t graph = nullptr;
+        /* thread-local capture: the host workers' copies on their own
+         * streams go on while this thread records */
+        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return -GFS_EIO;
+        cudaMemsetAsync(d.counts, 0, (size_t)g->n_words * g->n_files * 4, s);
+        cudaMemsetAsync(d.long_flags, 0, (size_t)g->n_files * 4, s);
+        cudaMemsetAsync(d.status, 0, 8, s);
+        cudaMemsetAsync(d.file_next, 0, 4, s);
+        if (g->smem) k_grep_scan<true, true><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+        else k_grep_scan<false, true><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+        k_grep_fixup<<<g->n_files, 32, 0, s>>>(S, d);
+        cudaError_t ce = cudaStreamEndCapture(s, &graph);
+        if (ce != cudaSuccess || !graph) return -GFS_EIO;
+        ce = cudaGraphInstantiate(&g->batch_graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) {
+            g->batch_graph = nullptr;
+            return -GFS_EIO;
+        }
+        g->batch_ctas = n_ctas;
+    }
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+    cudaError_t le = cudaGraphLaunch(g->batch_graph, s);
+    cudaEventRecord(b, s);
+    cudaError_t e = cudaStreamSynchronize(s); /* kernels first, then copies back */
+    if (kernel_ms) cudaEventElapsedTime(kernel_ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (le != cudaSuccess || e != cudaSuccess) {
+        fprintf(stderr, "gpufs_gb300: batched grep failed: %s\n", cudaGetErrorString(le != cudaSuccess ? le : e));
+        return -GFS_EIO;
+    }
+    uint32_t status[2] = {0, 0};
+    cudaMemcpy(status, d.status, 8, cudaMemcpyDeviceToHost);
+    g->last_status[0] = status[0];
+    g->last_status[1] = status[1];
+    if (host_xxh) cudaMemcpy(host_xxh, d.xxh, (size_t)g->n_files * 8, cudaMemcpyDeviceToHost);
+    return status[0] ? -((status[0] & GFS_ERRB_TIMEOUT) ? GFS_ETIMEDOUT : GFS_EIO) : 0;
 }
 
 int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts) {
@@ -1173,6 +1409,7 @@ int gfs_grep_close(gfs_grep* g) {
             cudaFree(rcs);
         }
     }
+    if (g->batch_graph) cudaGraphExecDestroy(g->batch_graph);
     cudaFree(g->dmem);
     delete g;
     return rc;

@@ -169,6 +169,11 @@ int gfs_grep_close(gfs_grep* g);
 /* `steps` runs back to back on the kernel stream; *total_ms: all of them
  * (CUDA events), *scan_ms: mean duration of one scan kernel */
 int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* scan_ms);
+/* Batched form: every file's counts and its XXH64 (seed 0) in one persistent
+ * launch, CTAs taking whole files longest first, captured as a CUDA graph on
+ * first use (per grid size) and replayed; host_xxh[n_files] (optional).
+ * The first call must not run inside another stream capture. */
+int gfs_grep_batch(gfs_grep* g, int n_ctas, unsigned long long* host_xxh, float* kernel_ms);
 /* one call: open + run + counts to host + close (the reference sample's whole run) */
 int gfs_grep_text(gfs_ctx* ctx, const char* dict_path, const char* const* paths, int n_files, uint32_t* host_counts,
                   int n_ctas);

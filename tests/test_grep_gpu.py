@@ -143,3 +143,49 @@ def test_many_sessions_in_one_process(built, shm_dir):
             with g.Grep(s, dpath, paths) as gr:
                 gr.run(0)
                 assert np.array_equal(gr.counts(), want), i
+
+
+def _batch_files(d, seed):
+    """Files of uneven sizes, half Zipf text, half random bytes; sizes around
+    the batched chunk (15,360 B), a 32-byte stripe and pages, plus empties."""
+    rng = np.random.default_rng(seed)
+    voc = datagen.vocab(3000, seed=seed)
+    sizes = [0, 1, 31, 32, 33, 63, 4096, 15359, 15360, 15361, 30720, 65537, 100000, 1 << 20,
+             3 * (1 << 20) + 7, 0, 5]
+    sizes += [int(x) for x in rng.integers(1, 400000, 16)]
+    paths = []
+    for i, n in enumerate(sizes):
+        p = os.path.join(d, "b%03d.dat" % i)
+        if i % 2:
+            datagen.uniform_bytes(p, n, seed=seed * 100 + i)
+        else:
+            datagen.zipf_files([p], [n], voc, s=1.1, seed=seed * 100 + i)
+        paths.append(p)
+    dpath = os.path.join(d, "bdict.gpu")
+    datagen.dictionary(dpath, voc, 900, seed=seed)
+    return paths, dpath
+
+
+@pytest.mark.parametrize("n_ctas,pool_mb", [(0, 512), (5, 6)])
+def test_batched_counts_and_xxh64(built, shm_dir, n_ctas, pool_mb):
+    """The batched form (whole files per CTA, longest first, one graph) gives
+    every file's counts and XXH64 exactly; replays agree; a pool smaller
+    than the files forces eviction."""
+    paths, dpath = _batch_files(shm_dir, seed=11 + pool_mb)
+    files = [open(p, "rb").read() for p in paths]
+    want = oracle.grep_counts(open(dpath, "rb").read(), files, mode="fast")
+    want_x = oracle.xxh64_many([np.frombuffer(f, dtype=np.uint8) for f in files])
+    with g.Session(log_page=16, pool_bytes=pool_mb << 20, max_files=256, timeout_s=30) as s:
+        with g.Grep(s, dpath, paths) as gr:
+            xxh, _ = gr.batch(n_ctas)
+            got = gr.counts()
+            assert xxh == want_x
+            bad = np.argwhere(got != want)
+            assert bad.size == 0, (bad[:5], got[tuple(bad[0])], want[tuple(bad[0])])
+            xxh2, _ = gr.batch(n_ctas)  # graph replay
+            assert xxh2 == want_x and np.array_equal(gr.counts(), want)
+            gr.run(n_ctas)  # the plain scan agrees
+            assert np.array_equal(gr.counts(), want)
+        if pool_mb < 8:
+            assert s.stats()["evictions"] > 0
+        assert s.last_error() == 0
