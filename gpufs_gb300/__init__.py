@@ -86,6 +86,10 @@ _SIGS = {
     "gfs_grep_close": (_int, [_c_p]),
     "gfs_grep_text": (_int, [_c_p, _c_s, ctypes.POINTER(_c_s), _int, _c_p, _int]),
     "gfs_grep_batch": (_int, [_c_p, _int, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_float)]),
+    "gfs_serve_open": (_int, [_c_p, _c_s, ctypes.POINTER(_c_s), _int, ctypes.POINTER(_c_s), _int,
+                              ctypes.POINTER(_c_p)]),
+    "gfs_serve_run": (_int, [_c_p, _c_p, _int, _c_p, _u64, _int]),
+    "gfs_serve_close": (_int, [_c_p]),
     "gfs_grep_bench": (_int, [_c_p, _int, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "gfs_drop_cache": (_i64, [_c_p]),
     "gfs_bigmatrix": (_int, [_c_p, _c_s, _c_s, _c_s, _int, _int, ctypes.POINTER(ctypes.c_float)]),
@@ -357,3 +361,53 @@ def measure_link(nbytes=1 << 30, reps=5):
     b = ctypes.c_float(0)
     _check(lib().gfs_measure_link(nbytes, reps, ctypes.byref(a), ctypes.byref(b)), "gfs_measure_link")
     return a.value, b.value
+
+
+# ---- served form ----
+SV_READ, SV_GREP, SV_WRITE = 1, 2, 3
+SERVE_REQ = np.dtype([("op", "<u4"), ("file", "<u4"), ("offset", "<u8"), ("length", "<u8"), ("arrival_ns", "<u8")])
+SERVE_RES = np.dtype([("result", "<u8"), ("status", "<i4"), ("pad", "<u4"), ("submit_ns", "<u8"),
+                      ("complete_ns", "<u8")])
+
+
+class Server:
+    """Served form: a persistent device loop over a request ring; files stay
+    open on the device for the server's life."""
+
+    def __init__(self, sess, dict_path, paths, out_paths=()):
+        self.s = sess
+        self.paths = list(paths)
+        self.out_paths = list(out_paths)
+        h = ctypes.c_void_p()
+        outs = _paths(self.out_paths) if self.out_paths else None
+        _check(sess.L.gfs_serve_open(sess.handle, _p(dict_path), _paths(self.paths), len(self.paths), outs,
+                                     len(self.out_paths), ctypes.byref(h)), "gfs_serve_open")
+        self._h = h
+
+    def run(self, reqs, inflight_pages=1 << 62, warps_per_sm=8):
+        """reqs: SERVE_REQ array sorted by arrival_ns.  Returns a SERVE_RES array."""
+        reqs = np.ascontiguousarray(reqs, dtype=SERVE_REQ)
+        res = np.zeros(reqs.size, dtype=SERVE_RES)
+        _check(self.s.L.gfs_serve_run(self._h, reqs.ctypes.data if reqs.size else None, reqs.size,
+                                      res.ctypes.data if reqs.size else None, int(inflight_pages), warps_per_sm),
+               "gfs_serve_run")
+        return res
+
+    def close(self):
+        if self._h:
+            rc = self.s.L.gfs_serve_close(self._h)
+            self._h = None
+            _check(rc, "gfs_serve_close")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def serve_pattern(offset, length, req_id):
+    """The bytes a GFS_SV_WRITE request writes (the device's pattern)."""
+    x = np.arange(offset, offset + length, dtype=np.uint64).astype(np.uint32)
+    v = (x * np.uint32(0x9E3779B1) + np.uint32((req_id * 0x85EBCA77) & 0xFFFFFFFF)) >> np.uint32(24)
+    return v.astype(np.uint8)

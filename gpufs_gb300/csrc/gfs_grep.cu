@@ -38,10 +38,14 @@
 #include <errno.h>
 #include <fcntl.h>
 #include <unistd.h>
+#include <sched.h>
+#include <time.h>
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -206,8 +210,26 @@ __device__ __forceinline__ void count_hit(const GrepDev& P, const Tbl& t, bool s
     else flush_slot(P, slot, 1u, f);
 }
 
+/* Where a scan's dictionary hits go: the scans count per slot (and flag
+ * files with runs of 33+ letters for the fix-up); the served loop counts
+ * matching tokens per request. */
+struct CountSink {
+    const GrepDev& P;
+    const Tbl& t;
+    bool smem;
+    int f;
+    __device__ __forceinline__ void hit(uint32_t slot) const { count_hit(P, t, smem, slot, f); }
+    __device__ __forceinline__ void long_run() const { atomicOr(&P.long_flags[f], 1u); }
+};
+struct TotalSink {
+    uint32_t n = 0;
+    __device__ __forceinline__ void hit(uint32_t) { n++; }
+    __device__ __forceinline__ void long_run() {}
+};
+
 /* Slow, general lookup: every tag match in both buckets is verified. */
-__device__ void lookup_count(const GrepDev& P, const Tbl& t, bool smem, const uint32_t k[8], uint32_t len, int f) {
+template <class Sink>
+__device__ void lookup_hit(const GrepDev& P, const Tbl& t, const uint32_t k[8], uint32_t len, Sink& sink) {
     const uint32_t h1 = grep_h1(grep_mix(k, (int)len));
     const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h1, P.nb), tag = grep_tag(h1, (int)len);
     const uint32_t bs[2] = {b1, b2};
@@ -217,7 +239,7 @@ __device__ void lookup_count(const GrepDev& P, const Tbl& t, bool smem, const ui
             const uint32_t tg = t.tags[slot];
             if (tg != tag) continue;
             if (!rec_equal(P, slot, (tg & GREP_TAG_LONG) != 0u, k, len)) continue;
-            count_hit(P, t, smem, slot, f);
+            sink.hit(slot);
             return;
         }
 }
@@ -348,9 +370,9 @@ __device__ __forceinline__ uint32_t other_cands16(const GrepDev& P, const Tbl& t
     return 0xFFFFFFFFu;
 }
 
-template <bool SMEM>
+template <bool SMEM, class Sink>
 __device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, const uint8_t* base, const StageDesc& d,
-                                             uint32_t segi, uint8_t* wscr, const uint4* km) {
+                                             uint32_t segi, uint8_t* wscr, const uint4* km, Sink& sink) {
     const int lane = threadIdx.x & 31;
     uint32_t* bm = (uint32_t*)wscr;
     uint16_t* slist = (uint16_t*)(wscr + GR_BM_WORDS * 4);
@@ -407,25 +429,25 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, c
         const uint4 r1 = m1 ? __ldg(P.rec_lo + s1) : make_uint4(0, 0, 0, 0);
         if (m0 && !key_eq(r0, k0)) s0 = other_cands16(P, tbl, k0, len0);
         if (m1 && !key_eq(r1, k1)) s1 = other_cands16(P, tbl, k1, len1);
-        if (s0 != 0xFFFFFFFFu) count_hit(P, tbl, SMEM, s0, d.f);
-        if (s1 != 0xFFFFFFFFu) count_hit(P, tbl, SMEM, s1, d.f);
+        if (s0 != 0xFFFFFFFFu) sink.hit(s0);
+        if (s1 != 0xFFFFFFFFu) sink.hit(s1);
         const bool slow0 = v0 && len0 > 16u, slow1 = v1 && len1 > 16u;
         /* rare: tokens of 17..32 letters take the general lookup; a run of 33+
          * letters flags the file for the fix-up kernel */
         if (slow0) {
-            if (len0 > 32u) atomicOr(&P.long_flags[d.f], 1u);
+            if (len0 > 32u) sink.long_run();
             else {
                 uint32_t kk[8];
                 key32(base, st0, len0, kk);
-                lookup_count(P, tbl, SMEM, kk, len0, d.f);
+                lookup_hit(P, tbl, kk, len0, sink);
             }
         }
         if (slow1) {
-            if (len1 > 32u) atomicOr(&P.long_flags[d.f], 1u);
+            if (len1 > 32u) sink.long_run();
             else {
                 uint32_t kk[8];
                 key32(base, st1, len1, kk);
-                lookup_count(P, tbl, SMEM, kk, len1, d.f);
+                lookup_hit(P, tbl, kk, len1, sink);
             }
         }
     }
@@ -792,7 +814,10 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
                 cur++;
             }
             if (d.f < 0) return;
-            if (!sh.abort) scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % NC, wscr, sh.kmask);
+            if (!sh.abort) {
+                CountSink sink{P, tbl, SMEM, d.f};
+                scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % NC, wscr, sh.kmask, sink);
+            }
             __syncwarp();
             if (lane == 0) mbar_arrive(&sh.empty[s]);
         }
@@ -836,7 +861,8 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
         ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
         if (ok && !sh.abort) {
             const StageDesc d = sh.desc[s];
-            scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % NC, wscr, sh.kmask);
+            CountSink sink{P, tbl, SMEM, d.f};
+            scan_segment<SMEM>(P, tbl, stages + (size_t)s * GR_STAGE + GR_LB, d, it % NC, wscr, sh.kmask, sink);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&sh.empty[s]);
@@ -885,7 +911,8 @@ __device__ void count_piece(const GrepDev& P, PageCursor& pc, uint64_t a, uint64
     Tbl t;
     t.tags = P.tags;
     t.cnt = nullptr;
-    lookup_count(P, t, false, k, (uint32_t)len, f);
+    CountSink sink{P, t, false, f};
+    lookup_hit(P, t, k, (uint32_t)len, sink);
 }
 } // namespace
 
@@ -941,11 +968,324 @@ template __global__ void k_grep_scan<false, true>(gfs_state*, GrepDev);
 /* ------------------------------------------------------------------ */
 /* host side: dictionary table, file opening, launch                   */
 /* ------------------------------------------------------------------ */
-static __global__ void k_open_files(const char* names, int n, int* fds, uint64_t* sizes) {
+/* ------------------------------------------------------------------ */
+/* served loop: a persistent kernel whose warps take requests from a    */
+/* ring in mapped host memory and serve them through the buffer cache  */
+/* ------------------------------------------------------------------ */
+struct SvReq { /* ring slot: the host fills it, then publishes seq = ticket + 1 */
+    uint32_t seq;
+    uint32_t op;
+    uint32_t file;
+    uint32_t id;
+    uint64_t offset;
+    uint64_t length;
+};
+struct SvComp { /* completion, indexed by request id: done is written last */
+    unsigned long long result;
+    int status;
+    uint32_t done;
+};
+struct ServeDev {
+    GrepDev G;              /* the dictionary (table in global memory) */
+    SvReq* ring;            /* device view of the mapped ring */
+    uint32_t ring_mask;
+    uint32_t* head;         /* next ticket (device memory) */
+    SvComp* comp;           /* device view of the mapped completions */
+    const int* fds;         /* served files, opened once for the server's life */
+    const uint64_t* sizes;
+    const int* out_fds;     /* output files (write-once) */
+    int n_files, n_out;
+    const uint32_t* stop;   /* mapped: set by the host when every request is done */
+};
+#define SV_WARPS 8
+#define SV_STAGE (GR_LB + GR_SEG + GR_LA + 16)
+
+namespace {
+
+__device__ __forceinline__ uint32_t sv_pattern(uint64_t x, uint32_t id) {
+    /* byte x of a served write: a fixed function of the file offset and request */
+    return (uint32_t)(((uint32_t)x * 0x9E3779B1u + id * 0x85EBCA77u) >> 24);
+}
+
+/* lane 0 keeps up to two pinned pages of one file (pg0 < pg1) */
+struct PagePair {
+    uint32_t pg[2];
+    int fr[2];
+};
+__device__ __forceinline__ void pp_init(PagePair& p) { p.pg[0] = p.pg[1] = 0xFFFFFFFFu; p.fr[0] = p.fr[1] = -1; }
+__device__ __forceinline__ void pp_release(gfs_state* S, PagePair& p) {
+    for (int i = 0; i < 2; i++)
+        if (p.fr[i] >= 0) unpin(S, (uint32_t)p.fr[i]);
+    pp_init(p);
+}
+/* make pages [a, b] (b <= a + 1) the pinned pair; returns 0 or -error */
+__device__ int pp_cover(gfs_state* S, const PinFile& pf, PagePair& p, uint32_t a, uint32_t b) {
+    PagePair q;
+    pp_init(q);
+    for (int i = 0; i < 2; i++) {
+        if (p.fr[i] < 0) continue;
+        if (p.pg[i] == a) { q.pg[0] = a; q.fr[0] = p.fr[i]; }
+        else if (p.pg[i] == b && b != a) { q.pg[1] = b; q.fr[1] = p.fr[i]; }
+        else unpin(S, (uint32_t)p.fr[i]);
+    }
+    const uint32_t want[2] = {a, b};
+    for (int i = 0; i < (b == a ? 1 : 2); i++) {
+        if (q.fr[i] >= 0) continue;
+        bool fresh;
+        const int r = pin_page(S, pf, want[i], GFS_PIN_READ, &fresh);
+        if (r < 0) {
+            for (int j = 0; j < 2; j++)
+                if (q.fr[j] >= 0) unpin(S, (uint32_t)q.fr[j]);
+            pp_init(p);
+            return r;
+        }
+        if (fresh) publish_valid(S, (uint32_t)r);
+        q.pg[i] = want[i];
+        q.fr[i] = r;
+    }
+    p = q;
+    return 0;
+}
+
+/* read + XXH64 of [off, end) of a served file, by one warp */
+__device__ int sv_read_xxh(gfs_state* S, const ServeDev& D, int fd, uint64_t off, uint64_t end, uint8_t* st,
+                           unsigned long long* result) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lp = S->log_page, pmask = S->page_size - 1u;
+    PinFile pf;
+    if (lane == 0) pf = pin_file(S, fd);
+    uint64_t v = gfsx::acc_init(lane & 3);
+    int fr = -1, err = 0;
+    uint32_t cur = 0xFFFFFFFFu;
+    const uint8_t* tail = st;
+    for (uint64_t pos = off; pos < end;) {
+        const uint32_t pg = (uint32_t)(pos >> lp);
+        if (pg != cur) {
+            if (lane == 0) {
+                if (fr >= 0) unpin(S, (uint32_t)fr);
+                bool fresh;
+                fr = pin_page(S, pf, pg, GFS_PIN_READ, &fresh);
+                if (fr >= 0 && fresh) publish_valid(S, (uint32_t)fr);
+            }
+            fr = __shfl_sync(0xFFFFFFFFu, fr, 0);
+            if (fr < 0) { err = fr; break; }
+            cur = pg;
+        }
+        const uint32_t piece = end - pos < 512 ? (uint32_t)(end - pos) : 512u;
+        const uint8_t* src = S->pool + ((size_t)fr << lp) + (pos & pmask); /* 16-byte aligned */
+        const uint32_t o = (uint32_t)lane * 16u;
+        if (o + 16u <= piece) *(uint4*)(st + o) = ld_cg4(src + o);
+        else if (o < piece)
+            for (uint32_t b = o; b < piece; b++) st[b] = src[b];
+        __syncwarp();
+        const uint32_t stripes = piece / 32u;
+        if (lane < 4) v = gfsx::acc_stripes(v, st, stripes, lane);
+        tail = st + stripes * 32u;
+        pos += piece;
+        if (pos < end) __syncwarp();
+    }
+    if (lane == 0 && fr >= 0 && !err) unpin(S, (uint32_t)fr);
+    if (err) return err;
+    const uint64_t v1 = __shfl_sync(0xFFFFFFFFu, v, 0), v2 = __shfl_sync(0xFFFFFFFFu, v, 1),
+                   v3 = __shfl_sync(0xFFFFFFFFu, v, 2), v4 = __shfl_sync(0xFFFFFFFFu, v, 3);
+    if (lane == 0) *result = gfsx::finish(v1, v2, v3, v4, end - off, tail);
+    __syncwarp();
+    return 0;
+}
+
+/* dictionary words among the tokens of [off, end), the range read as a
+ * text of its own (bytes outside it are not letters), by one warp */
+__device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, uint64_t end, uint8_t* st,
+                       uint8_t* wscr, const uint4* km, unsigned long long* result) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lp = S->log_page, pmask = S->page_size - 1u;
+    PinFile pf;
+    PagePair pp;
+    if (lane == 0) { pf = pin_file(S, fd); pp_init(pp); }
+    Tbl t;
+    t.tags = D.G.tags;
+    t.cnt = nullptr;
+    TotalSink sink;
+    int err = 0;
+    for (uint64_t seg = off; seg < end; seg += GR_SEG) {
+        /* stage [seg - 16, seg + 512 + 64) with bytes outside [off, end) zero */
+        const uint64_t lo = seg >= off + GR_LB ? seg - GR_LB : off;
+        const uint64_t hi = seg + GR_SEG + GR_LA < end ? seg + GR_SEG + GR_LA : end;
+        int r = 0;
+        if (lane == 0) r = pp_cover(S, pf, pp, (uint32_t)(lo >> lp), (uint32_t)((hi - 1) >> lp));
+        r = __shfl_sync(0xFFFFFFFFu, r, 0);
+        if (r < 0) { err = r; break; }
+        uint32_t pg0 = 0, pg1 = 0;
+        int f0 = 0, f1 = 0;
+        if (lane == 0) { pg0 = pp.pg[0]; pg1 = pp.pg[1]; f0 = pp.fr[0]; f1 = pp.fr[1]; }
+        pg0 = __shfl_sync(0xFFFFFFFFu, pg0, 0);
+        pg1 = __shfl_sync(0xFFFFFFFFu, pg1, 0);
+        f0 = __shfl_sync(0xFFFFFFFFu, f0, 0);
+        f1 = __shfl_sync(0xFFFFFFFFu, f1, 0);
+        for (uint32_t u = (uint32_t)lane; u < (GR_LB + GR_SEG + GR_LA) / 16u; u += 32u) {
+            const int64_t a = (int64_t)seg - GR_LB + 16 * (int64_t)u; /* file offset of this 16-byte unit */
+            uint4 w = make_uint4(0, 0, 0, 0);
+            if (a >= (int64_t)off && (uint64_t)a < end) {
+                const uint32_t pg = (uint32_t)((uint64_t)a >> lp);
+                const int fr = pg == pg0 ? f0 : f1;
+                w = ld_cg4(S->pool + ((size_t)fr << lp) + ((uint64_t)a & pmask));
+                const uint64_t rem = end - (uint64_t)a;
+                if (rem < 16) { /* zero the bytes past the end */
+                    uint32_t* ww = (uint32_t*)&w;
+                    for (int q = 0; q < 4; q++) {
+                        const int keep = (int)rem - 4 * q;
+                        ww[q] &= keep >= 4 ? 0xFFFFFFFFu : (keep <= 0 ? 0u : (1u << (8 * keep)) - 1u);
+                    }
+                }
+            }
+            *(uint4*)(st + 16 * u) = w;
+        }
+        __syncwarp();
+        StageDesc d;
+        d.pos = seg == off ? 0 : 1; /* only its being zero matters: no byte before the range */
+        d.f = 0;
+        d.fseq = 0;
+        d.clen = end - seg < GR_SEG ? (uint32_t)(end - seg) : (uint32_t)GR_SEG;
+        d.avail = end - seg < GR_SEG + GR_LA ? (uint32_t)(end - seg) : (uint32_t)(GR_SEG + GR_LA);
+        scan_segment<false>(D.G, t, st + GR_LB, d, 0u, wscr, km, sink);
+        __syncwarp();
+    }
+    if (lane == 0) pp_release(S, pp);
+    if (err) return err;
+    uint32_t n = sink.n;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xFFFFFFFFu, n, o);
+    if (lane == 0) *result = n;
+    __syncwarp();
+    return 0;
+}
+
+/* write the request's pattern over [off, off+len) of a write-once output
+ * file, page by page (the page-level steps of gwrite), by one warp */
+__device__ int sv_write(gfs_state* S, int fd, uint64_t off, uint64_t len, uint32_t id, unsigned long long* result) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lp = S->log_page;
+    const uint64_t page = 1ull << lp, end = off + len;
+    PinFile pf;
+    if (lane == 0) pf = pin_file(S, fd);
+    for (uint64_t pos = off; pos < end;) {
+        const uint64_t pst = pos & ~(page - 1ull), pe = pst + page < end ? pst + page : end;
+        int fr = 0;
+        bool fresh = false;
+        if (lane == 0) {
+            const bool full = pos == pst && pe == pst + page;
+            fr = pin_page(S, pf, (uint32_t)(pos >> lp), full ? GFS_PIN_WFULL : GFS_PIN_WONCE, &fresh);
+        }
+        fr = __shfl_sync(0xFFFFFFFFu, fr, 0);
+        fresh = __shfl_sync(0xFFFFFFFFu, fresh ? 1 : 0, 0) != 0;
+        if (fr < 0) return fr;
+        uint8_t* d = frame_data(S, (uint32_t)fr);
+        if (fresh) { /* bytes of the page this write does not cover start at zero */
+            if (pos > pst) warp_zero(d, pos - pst, lane);
+            if (pe < pst + page) warp_zero(d + (pe - pst), pst + page - pe, lane);
+        }
+        for (uint64_t x = pos + (uint64_t)lane * 4u; x < pe; x += 128u) {
+            uint32_t w = 0;
+            for (int b = 0; b < 4; b++)
+                if (x + (uint64_t)b < pe) w |= (sv_pattern(x + (uint64_t)b, id) & 0xFFu) << (8 * b);
+            if (x + 4 <= pe) *(uint32_t*)(d + (x - pst)) = w;
+            else for (int b = 0; x + (uint64_t)b < pe; b++) d[x - pst + (uint64_t)b] = (uint8_t)(w >> (8 * b));
+        }
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence();
+            atomicMax(&S->frames[fr].content, (uint32_t)(pe - pst));
+            if (fresh) publish_valid(S, (uint32_t)fr);
+            mark_dirty(S, (uint32_t)fr);
+            unpin(S, (uint32_t)fr);
+            atomicMax((unsigned long long*)&S->files[pf.slot].size, (unsigned long long)pe);
+        }
+        __syncwarp();
+        pos = pe;
+    }
+    if (lane == 0) *result = len;
+    return 0;
+}
+
+} // namespace
+
+/* Served loop: each warp takes the next ticket, waits (bounded by the
+ * session timeout, or until the host sets stop) for that request, frees
+ * its ring slot, serves it and publishes the completion. */
+__global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev D) {
+    __shared__ __align__(16) uint8_t stage[SV_WARPS][SV_STAGE];
+    __shared__ __align__(16) uint8_t wscr[SV_WARPS][GR_WSCR];
+    __shared__ uint4 kmask[17];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x <= 16u) {
+        uint32_t mw[4];
+        for (uint32_t i = 0; i < 4u; i++) {
+            const int b = (int)threadIdx.x * 8 - 32 * (int)i;
+            mw[i] = b >= 32 ? 0xFFFFFFFFu : (b <= 0 ? 0u : (1u << b) - 1u);
+        }
+        kmask[threadIdx.x] = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+    }
+    __syncthreads();
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(D.head, 1u);
+        t = __shfl_sync(0xFFFFFFFFu, t, 0);
+        SvReq* slot = &D.ring[t & D.ring_mask];
+        uint32_t have = 0;
+        uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
+        if (lane == 0) {
+            const uint64_t t0 = gtimer();
+            uint32_t ns = 64, k = 0;
+            for (;;) {
+                if (ld_acq_sys(&slot->seq) == t + 1u) { have = 1; break; }
+                if (ld_rlx_sys(D.stop)) break;
+                if ((++k & 63u) == 0u && gtimer() - t0 > S->timeout_ns) break; /* idle too long: leave */
+                __nanosleep(ns);
+                if (ns < 2048) ns <<= 1;
+            }
+            if (have) {
+                asm volatile("ld.relaxed.sys.global.v4.u32 {%0,%1,%2,%3}, [%4];"
+                             : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w) : "l"(slot) : "memory");
+                asm volatile("ld.relaxed.sys.global.v4.u32 {%0,%1,%2,%3}, [%4];"
+                             : "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w) : "l"((const uint8_t*)slot + 16) : "memory");
+                st_rel_sys(&slot->seq, t + D.ring_mask + 1u); /* the slot is free for the host again */
+            }
+        }
+        have = __shfl_sync(0xFFFFFFFFu, have, 0);
+        if (!have) return;
+        const uint32_t op = __shfl_sync(0xFFFFFFFFu, a.y, 0), file = __shfl_sync(0xFFFFFFFFu, a.z, 0),
+                       id = __shfl_sync(0xFFFFFFFFu, a.w, 0);
+        const uint64_t off = ((uint64_t)__shfl_sync(0xFFFFFFFFu, b.y, 0) << 32) | __shfl_sync(0xFFFFFFFFu, b.x, 0);
+        const uint64_t len = ((uint64_t)__shfl_sync(0xFFFFFFFFu, b.w, 0) << 32) | __shfl_sync(0xFFFFFFFFu, b.z, 0);
+        unsigned long long res = 0;
+        int status = 0;
+        if (off & 15u) {
+            status = -GFS_EINVAL; /* offsets are 16-byte aligned (vector loads and stores) */
+        } else if (op == GFS_SV_WRITE) {
+            status = (int)file < D.n_out ? sv_write(S, D.out_fds[file], off, len, id, &res) : -GFS_EINVAL;
+        } else if ((int)file < D.n_files && (op == GFS_SV_READ || op == GFS_SV_GREP)) {
+            const uint64_t size = D.sizes[file];
+            const uint64_t o = off < size ? off : size, e = len < size - o ? o + len : size;
+            if (op == GFS_SV_READ) status = sv_read_xxh(S, D, D.fds[file], o, e, stage[warp], &res);
+            else status = sv_grep(S, D, D.fds[file], o, e, stage[warp], wscr[warp], kmask, &res);
+        } else {
+            status = -GFS_EINVAL;
+        }
+        if (lane == 0) {
+            SvComp* c = &D.comp[id];
+            asm volatile("st.relaxed.sys.global.u64 [%0], %1;" ::"l"(&c->result), "l"(res) : "memory");
+            asm volatile("st.relaxed.sys.global.u32 [%0], %1;" ::"l"(&c->status), "r"((uint32_t)status) : "memory");
+            st_rel_sys(&c->done, 1u);
+        }
+        __syncwarp();
+    }
+}
+
+static __global__ void k_open_files(const char* names, int n, int* fds, uint64_t* sizes, int oflags = O_GRDONLY) {
     int f = blockIdx.x;
     if (f >= n) return;
     gfs_state* S = g_gfs;
-    int fd = gfsd::blk_open(S, names + (size_t)f * GFS_NAME_MAX, O_GRDONLY);
+    int fd = gfsd::blk_open(S, names + (size_t)f * GFS_NAME_MAX, oflags);
     if (threadIdx.x == 0) {
         fds[f] = fd;
         sizes[f] = fd >= 0 ? gfsd::ld_rlx64(&S->files[fd].size) : 0;
@@ -1115,6 +1455,7 @@ void gfs__preload_grep() {
     cudaFuncGetAttributes(&a, k_grep_scan<false, false>);
     cudaFuncGetAttributes(&a, k_grep_scan<true, true>);
     cudaFuncGetAttributes(&a, k_grep_scan<false, true>);
+    cudaFuncGetAttributes(&a, k_serve);
     cudaFuncGetAttributes(&a, k_grep_fixup);
     cudaFuncGetAttributes(&a, k_open_files);
     cudaFuncGetAttributes(&a, k_close_files);
@@ -1412,6 +1753,226 @@ int gfs_grep_close(gfs_grep* g) {
     if (g->batch_graph) cudaGraphExecDestroy(g->batch_graph);
     cudaFree(g->dmem);
     delete g;
+    return rc;
+}
+
+/* ---------------- served loop: host side ---------------- */
+struct gfs_server {
+    gfs_ctx* ctx = nullptr;
+    gfs_grep* dict = nullptr; /* dictionary table (and no corpus) */
+    int n_files = 0, n_out = 0;
+    uint8_t* dmem = nullptr;  /* fds, sizes, out fds, names, head */
+    int* fds = nullptr;
+    uint64_t* sizes = nullptr;
+    int* out_fds = nullptr;
+    uint32_t* head = nullptr;
+    SvReq* ring_h = nullptr;  /* mapped */
+    SvReq* ring_d = nullptr;
+    uint32_t ring_n = 0;
+    uint32_t* stop_h = nullptr; /* mapped */
+    uint32_t* stop_d = nullptr;
+    int sms = 0;
+    std::vector<uint64_t> host_sizes;
+};
+
+static uint64_t now_ns() {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (uint64_t)ts.tv_sec * 1000000000ull + (uint64_t)ts.tv_nsec;
+}
+
+int gfs_serve_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths, int n_files,
+                   const char* const* out_paths, int n_out, gfs_server** out) {
+    *out = nullptr;
+    if (n_files < 1 || n_out < 0 || !dict_path) return -GFS_EINVAL;
+    for (int i = 0; i < n_files; i++)
+        if (!paths[i] || strlen(paths[i]) >= GFS_NAME_MAX) return -GFS_EINVAL;
+    for (int i = 0; i < n_out; i++)
+        if (!out_paths[i] || strlen(out_paths[i]) >= GFS_NAME_MAX) return -GFS_EINVAL;
+    gfs_server* sv = new gfs_server();
+    sv->ctx = ctx;
+    sv->n_files = n_files;
+    sv->n_out = n_out;
+    /* the dictionary: a grep plan over no corpus file but the dictionary itself */
+    const char* none[1] = {dict_path};
+    int rc = gfs_grep_open(ctx, dict_path, none, 1, &sv->dict);
+    if (rc < 0) { delete sv; return rc; }
+    if (gfs__activate(ctx)) { gfs_serve_close(sv); return -GFS_EIO; }
+    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
+    const size_t n_all = (size_t)n_files + (size_t)n_out;
+    size_t o_fds = 0, o_sz = align_up(o_fds + (size_t)n_files * 4, 256), o_ofd = align_up(o_sz + (size_t)n_files * 8, 256),
+           o_osz = align_up(o_ofd + (size_t)n_out * 4 + 4, 256), o_head = align_up(o_osz + (size_t)n_out * 8 + 8, 256),
+           o_names = align_up(o_head + 64, 256), total = align_up(o_names + n_all * GFS_NAME_MAX, 256);
+    if (cudaMalloc(&sv->dmem, total) != cudaSuccess) { gfs_serve_close(sv); return -GFS_ENOMEM; }
+    cudaMemset(sv->dmem, 0, total);
+    sv->fds = (int*)(sv->dmem + o_fds);
+    sv->sizes = (uint64_t*)(sv->dmem + o_sz);
+    sv->out_fds = (int*)(sv->dmem + o_ofd);
+    sv->head = (uint32_t*)(sv->dmem + o_head);
+    {
+        std::vector<char> names(n_all * GFS_NAME_MAX, 0);
+        for (int i = 0; i < n_files; i++) memcpy(&names[(size_t)i * GFS_NAME_MAX], paths[i], strlen(paths[i]));
+        for (int i = 0; i < n_out; i++)
+            memcpy(&names[((size_t)n_files + (size_t)i) * GFS_NAME_MAX], out_paths[i], strlen(out_paths[i]));
+        cudaMemcpy(sv->dmem + o_names, names.data(), names.size(), cudaMemcpyHostToDevice);
+    }
+    /* every file opened once, for the server's life (the open-file table
+     * stays on the device across requests) */
+    k_open_files<<<n_files, 128, 0, s>>>((const char*)(sv->dmem + o_names), n_files, sv->fds, sv->sizes);
+    if (n_out)
+        k_open_files<<<n_out, 128, 0, s>>>((const char*)(sv->dmem + o_names) + (size_t)n_files * GFS_NAME_MAX, n_out,
+                                           sv->out_fds, (uint64_t*)(sv->dmem + o_osz), O_GWRONCE);
+    if (cudaStreamSynchronize(s) != cudaSuccess) { gfs_serve_close(sv); return -GFS_EIO; }
+    std::vector<int> h((size_t)n_files + (size_t)n_out);
+    cudaMemcpy(h.data(), sv->fds, (size_t)n_files * 4, cudaMemcpyDeviceToHost);
+    if (n_out) cudaMemcpy(h.data() + n_files, sv->out_fds, (size_t)n_out * 4, cudaMemcpyDeviceToHost);
+    sv->host_sizes.resize((size_t)n_files);
+    cudaMemcpy(sv->host_sizes.data(), sv->sizes, (size_t)n_files * 8, cudaMemcpyDeviceToHost);
+    for (int x : h)
+        if (x < 0) { gfs_serve_close(sv); return x; }
+    sv->ring_n = 1u << 16;
+    if (cudaHostAlloc((void**)&sv->ring_h, (size_t)sv->ring_n * sizeof(SvReq), cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&sv->ring_d, sv->ring_h, 0) != cudaSuccess ||
+        cudaHostAlloc((void**)&sv->stop_h, 64, cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&sv->stop_d, sv->stop_h, 0) != cudaSuccess) {
+        gfs_serve_close(sv);
+        return -GFS_ENOMEM;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sv->sms, cudaDevAttrMultiProcessorCount, dev);
+    *out = sv;
+    return 0;
+}
+
+/* Open-loop run: request k is published at (or after) its arrival time,
+ * once the pages of the requests in flight leave room for it under
+ * inflight_pages (memory-gated admission); latencies are completion minus
+ * arrival, host clock.  warps_per_sm: serving warps per SM (multiple of 8). */
+int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_res* res, uint64_t inflight_pages,
+                  int warps_per_sm) {
+    if (!sv || n < 0 || (n && (!reqs || !res))) return -GFS_EINVAL;
+    if (gfs__activate(sv->ctx)) return -GFS_EIO;
+    if (warps_per_sm < SV_WARPS) warps_per_sm = SV_WARPS;
+    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(sv->ctx);
+    SvComp* comp_h = nullptr;
+    SvComp* comp_d = nullptr;
+    if (cudaHostAlloc((void**)&comp_h, (size_t)(n ? n : 1) * sizeof(SvComp), cudaHostAllocMapped) != cudaSuccess)
+        return -GFS_ENOMEM;
+    cudaHostGetDevicePointer((void**)&comp_d, comp_h, 0);
+    memset(comp_h, 0, (size_t)(n ? n : 1) * sizeof(SvComp));
+    for (uint32_t i = 0; i < sv->ring_n; i++) __atomic_store_n(&sv->ring_h[i].seq, i, __ATOMIC_RELAXED);
+    __atomic_store_n(sv->stop_h, 0u, __ATOMIC_RELEASE);
+    cudaMemsetAsync(sv->head, 0, 4, s);
+    ServeDev D{};
+    D.G = sv->dict->dev;
+    D.ring = sv->ring_d;
+    D.ring_mask = sv->ring_n - 1u;
+    D.head = sv->head;
+    D.comp = comp_d;
+    D.fds = sv->fds;
+    D.sizes = sv->sizes;
+    D.out_fds = sv->out_fds;
+    D.n_files = sv->n_files;
+    D.n_out = sv->n_out;
+    D.stop = sv->stop_d;
+    const uint32_t page = gfs_page_size(sv->ctx);
+    const int blocks = sv->sms * (warps_per_sm / SV_WARPS);
+    k_serve<<<blocks, SV_WARPS * 32, 0, s>>>((gfs_state*)gfs_device_state(sv->ctx), D);
+    if (cudaGetLastError() != cudaSuccess) { cudaFreeHost(comp_h); return -GFS_EIO; }
+    std::vector<uint32_t> cost((size_t)n);
+    for (int k = 0; k < n; k++) cost[(size_t)k] = (uint32_t)((reqs[k].length + page - 1) / page) + 1u;
+    std::atomic<uint64_t> inflight{0};
+    std::atomic<int> submitted{0}, completed{0};
+    std::atomic<int> quit{0};
+    const uint64_t t0 = now_ns();
+    /* completions: scanned in submission order from the oldest open one */
+    std::thread poller([&] {
+        std::vector<char> seen((size_t)n, 0);
+        int lo = 0;
+        while (completed.load() < n && !quit.load()) {
+            const int hi = submitted.load(std::memory_order_acquire);
+            bool any = false;
+            for (int k = lo; k < hi; k++) {
+                if (seen[(size_t)k]) continue;
+                if (__atomic_load_n(&comp_h[k].done, __ATOMIC_ACQUIRE)) {
+                    res[k].complete_ns = now_ns() - t0;
+                    res[k].result = comp_h[k].result;
+                    res[k].status = comp_h[k].status;
+                    seen[(size_t)k] = 1;
+                    inflight.fetch_sub(cost[(size_t)k]);
+                    completed.fetch_add(1);
+                    any = true;
+                }
+            }
+            while (lo < hi && seen[(size_t)lo]) lo++;
+            if (!any) sched_yield();
+        }
+    });
+    const uint64_t limit_ns = 4ull * gfs__timeout_ns(sv->ctx) + 1000000000ull;
+    int rc = 0;
+    for (int k = 0; k < n && !rc; k++) {
+        const uint64_t due = reqs[k].arrival_ns;
+        while (now_ns() - t0 < due) {
+        }
+        /* memory-gated admission */
+        while (inflight.load() + cost[(size_t)k] > inflight_pages && inflight.load() > 0) {
+            if (now_ns() - t0 > due + limit_ns) { rc = -GFS_ETIMEDOUT; break; }
+        }
+        if (rc) break;
+        SvReq* slot = &sv->ring_h[(uint32_t)k & (sv->ring_n - 1u)];
+        while (__atomic_load_n(&slot->seq, __ATOMIC_ACQUIRE) != (uint32_t)k) {
+            if (now_ns() - t0 > due + limit_ns) { rc = -GFS_ETIMEDOUT; break; }
+        }
+        if (rc) break;
+        slot->op = reqs[k].op;
+        slot->file = reqs[k].file;
+        slot->id = (uint32_t)k;
+        slot->offset = reqs[k].offset;
+        slot->length = reqs[k].length;
+        res[k].submit_ns = now_ns() - t0;
+        inflight.fetch_add(cost[(size_t)k]);
+        __atomic_store_n(&slot->seq, (uint32_t)k + 1u, __ATOMIC_RELEASE);
+        submitted.store(k + 1, std::memory_order_release);
+    }
+    const uint64_t wait_from = now_ns();
+    while (!rc && completed.load() < n) {
+        if (now_ns() - wait_from > limit_ns) { rc = -GFS_ETIMEDOUT; break; }
+        sched_yield();
+    }
+    quit.store(1);
+    __atomic_store_n(sv->stop_h, 1u, __ATOMIC_RELEASE);
+    cudaError_t e = cudaStreamSynchronize(s);
+    poller.join();
+    cudaFreeHost(comp_h);
+    if (e != cudaSuccess) return -GFS_EIO;
+    return rc;
+}
+
+int gfs_serve_close(gfs_server* sv) {
+    if (!sv) return 0;
+    int rc = 0;
+    if (sv->dmem && sv->fds) {
+        gfs__activate(sv->ctx);
+        cudaStream_t s = (cudaStream_t)gfs_kernel_stream(sv->ctx);
+        int* rcs = nullptr;
+        const int n_all = sv->n_files + sv->n_out;
+        if (n_all && cudaMalloc(&rcs, (size_t)n_all * 4) == cudaSuccess) {
+            k_close_files<<<sv->n_files, 128, 0, s>>>(sv->fds, sv->n_files, rcs);
+            if (sv->n_out) k_close_files<<<sv->n_out, 128, 0, s>>>(sv->out_fds, sv->n_out, rcs + sv->n_files);
+            cudaStreamSynchronize(s);
+            std::vector<int> h((size_t)n_all);
+            cudaMemcpy(h.data(), rcs, h.size() * 4, cudaMemcpyDeviceToHost);
+            for (int x : h)
+                if (x < 0 && !rc) rc = x;
+            cudaFree(rcs);
+        }
+    }
+    if (sv->ring_h) cudaFreeHost(sv->ring_h);
+    if (sv->stop_h) cudaFreeHost(sv->stop_h);
+    cudaFree(sv->dmem);
+    if (sv->dict) gfs_grep_close(sv->dict);
+    delete sv;
     return rc;
 }
 

@@ -759,6 +759,7 @@ int gfs_destroy(gfs_ctx* c) {
 }
 
 void* gfs_kernel_stream(gfs_ctx* c) { return (void*)c->kstream; }
+unsigned long long gfs__timeout_ns(gfs_ctx* c) { return c->cfg.timeout_ns; }
 void* gfs_device_state(gfs_ctx* c) { return (void*)c->ds; }
 uint32_t gfs_page_size(gfs_ctx* c) { return c->hs.page_size; }
 uint32_t gfs_num_frames(gfs_ctx* c) { return c->hs.n_frames; }

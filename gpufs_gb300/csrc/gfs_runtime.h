@@ -10,6 +10,8 @@ extern "C" {
 #endif
 void* gfs__scratch(gfs_ctx* c, size_t bytes);
 int gfs__activate(gfs_ctx* c);
+/* the session's bound on device-side waits (ns) */
+unsigned long long gfs__timeout_ns(gfs_ctx* c);
 void gfs__preload_kernels(void);
 void gfs__preload_runtime(void);
 void gfs__preload_workloads(void);

@@ -174,6 +174,40 @@ int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* s
  * first use (per grid size) and replayed; host_xxh[n_files] (optional).
  * The first call must not run inside another stream capture. */
 int gfs_grep_batch(gfs_grep* g, int n_ctas, unsigned long long* host_xxh, float* kernel_ms);
+/* ---- served form (no reference counterpart: the reference serves one
+ * kernel at a time) ----
+ * A persistent kernel whose warps take (file, offset, length, op) requests
+ * from a ring in mapped host memory and serve them through the buffer
+ * cache; served files are opened once and stay open on the device.
+ * Offsets must be 16-byte aligned (else -GFS_EINVAL for that request). */
+#define GFS_SV_READ 1  /* read the range of a served file; result: its XXH64 (seed 0) */
+#define GFS_SV_GREP 2  /* result: tokens of the range (read as a text of its own) that are dictionary words */
+#define GFS_SV_WRITE 3 /* write the request's byte pattern over the range of an output file; result: bytes */
+typedef struct gfs_serve_req {
+    uint32_t op;
+    uint32_t file;       /* served file index, or output file index for GFS_SV_WRITE */
+    uint64_t offset;
+    uint64_t length;
+    uint64_t arrival_ns; /* open-loop arrival time from the start of the run */
+} gfs_serve_req;
+typedef struct gfs_serve_res {
+    unsigned long long result;
+    int32_t status;      /* 0 or -errno */
+    uint32_t pad;
+    uint64_t submit_ns;  /* published to the ring (after admission) */
+    uint64_t complete_ns; /* completion seen by the host; latency = complete_ns - arrival_ns */
+} gfs_serve_res;
+typedef struct gfs_server gfs_server;
+/* dictionary (grep_text record format), served files, write-once output files */
+int gfs_serve_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths, int n_files,
+                   const char* const* out_paths, int n_out, gfs_server** out);
+/* one open-loop run over requests sorted by arrival; inflight_pages bounds the
+ * pages of admitted, unfinished requests (memory-gated admission) */
+int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_res* res, uint64_t inflight_pages,
+                  int warps_per_sm);
+/* closes every file (dirty output pages are written back) */
+int gfs_serve_close(gfs_server* sv);
+
 /* one call: open + run + counts to host + close (the reference sample's whole run) */
 int gfs_grep_text(gfs_ctx* ctx, const char* dict_path, const char* const* paths, int n_files, uint32_t* host_counts,
                   int n_ctas);
