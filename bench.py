@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--no-extra", action="store_true", help="skip the link-bandwidth measurement")
     ap.add_argument("--corpus-mb", type=int, default=TOTAL_BYTES >> 20,
                     help="smaller corpora are for profiling only; the benchmark is 1024")
-    ap.add_argument("--workload", default="grep_text", choices=["grep_text", "gread", "memcopy", "bigmatrix", "batched"],
+    ap.add_argument("--workload", default="grep_text", choices=["grep_text", "gread", "memcopy", "bigmatrix", "batched", "served"],
                     help="grep_text is the benchmark line; the others measure the other configurations")
     return ap.parse_args()
 
@@ -562,6 +562,8 @@ def run_workload(args, rank, ws, local, td, data_dir):
                 "gpu_launches": steps, "clocks": clocks, "parity": {"xxh64_equal": bool(ok)}, "extra": extra}
     elif args.workload == "batched":
         line = _run_batched(args, rank, ws, local, td, d, nt, workers, hbm, how, link, extra, clk)
+    elif args.workload == "served":
+        line = _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk)
     else:  # bigmatrix
         rows, cols = 16384, 65536
         vp = _stamped(d, "vec.f32", "n %d 11" % cols, lambda p: datagen.normal_f32(p, cols, seed=11))
@@ -752,6 +754,226 @@ def _run_batched(args, rank, ws, local, td, d, nt, workers, hbm, how, link, extr
                     "d2h_bytes_per_step": counts.nbytes + 8 * n_files, "ms_per_step": e2e_t * 1e3,
                     "call": "Grep open + batch + counts + close, cold buffer cache"},
             "gpu_launches": steps, "clocks": clocks, "parity": parity, "extra": extra}
+
+
+def _served_data(d, target_bytes, max_files):
+    """Served corpus: 100,000 files of log-uniform sizes 4 KiB .. 3.3 MiB (mean
+    about 0.5 MB, 48 GiB) -- or, where the host allows fewer open files,
+    max_files files whose log-uniform range is scaled up to the same total --
+    alternately seeded random bytes and Zipf text; the grep_text dictionary."""
+    import math
+    import numpy as np
+    from gpufs_gb300 import datagen
+    os.makedirs(d, exist_ok=True)
+    n_files = min(100000, max_files)
+    lo, hi = 4096.0, 3.3 * (1 << 20)
+    mean = target_bytes / n_files
+    while (hi - lo) / math.log(hi / lo) < mean:  # widen the range until its mean covers the total
+        hi *= 1.05
+        lo *= 1.05
+    sizes = np.asarray(datagen.loguniform_sizes(n_files, int(lo), int(hi), seed=0x73657276), dtype=np.int64)
+    csum = np.cumsum(sizes)
+    n = int(np.searchsorted(csum, target_bytes)) + 1
+    n = min(n, sizes.size)
+    sizes = [int(x) for x in sizes[:n]]
+    paths = [os.path.join(d, "s%06d.%s" % (i, "txt" if i % 2 == 0 else "bin")) for i in range(n)]
+    dpath = os.path.join(d, "dict.gpu")
+    stamp = os.path.join(d, "STAMP")
+    want = "served %d %d" % (n, sum(sizes))
+    if not (os.path.exists(stamp) and open(stamp).read() == want):
+        voc = datagen.vocab(N_VOCAB, seed=0x766f6361 ^ SEED)
+        text = list(range(0, n, 2))
+        for i0 in range(0, len(text), 4096):
+            part = text[i0:i0 + 4096]
+            datagen.zipf_files([paths[i] for i in part], [sizes[i] for i in part], voc, s=1.1, seed=0x7a697066 + i0)
+        for i in range(1, n, 2):
+            datagen.uniform_bytes(paths[i], sizes[i], seed=0x73000000 + i)
+        datagen.dictionary(dpath, voc, N_DICT, seed=0x64696374 ^ SEED)
+        with open(stamp, "w") as f:
+            f.write(want)
+    return paths, dpath, sizes
+
+
+def _served_trace(sizes, n_req, n_out, rng):
+    """Requests: file popularity Zipf(0.9) over a seeded permutation, lengths
+    log-uniform 4 KiB .. 16 MiB, offsets 4 KiB-aligned within the file, op mix
+    80 % read+XXH64 / 15 % grep / 5 % write (writes to disjoint 16 MiB regions
+    of the output files)."""
+    import numpy as np
+    import gpufs_gb300 as g
+    n_files = len(sizes)
+    ranks = np.arange(1, n_files + 1, dtype=np.float64)
+    p = ranks ** -0.9
+    p /= p.sum()
+    perm = rng.permutation(n_files)
+    files = perm[rng.choice(n_files, n_req, p=p)]
+    lengths = np.exp(rng.uniform(np.log(4096), np.log(16 << 20), n_req)).astype(np.uint64)
+    ops = rng.choice([g.SV_READ, g.SV_GREP, g.SV_WRITE], n_req, p=[0.80, 0.15, 0.05])
+    reqs = np.zeros(n_req, dtype=g.SERVE_REQ)
+    wcount = 0
+    sz = np.asarray(sizes, dtype=np.uint64)
+    for k in range(n_req):
+        if ops[k] == g.SV_WRITE:
+            o = wcount % n_out
+            reqs[k] = (g.SV_WRITE, o, (wcount // n_out) * (16 << 20), lengths[k], 0)
+            wcount += 1
+        else:
+            f = int(files[k])
+            pages = int(sz[f]) // 4096
+            off = int(rng.integers(0, pages + 1)) * 4096 if pages else 0
+            reqs[k] = (ops[k], f, off, lengths[k], 0)
+    return reqs
+
+
+def _served_bytes(reqs, sizes):
+    import numpy as np
+    import gpufs_gb300 as g
+    sz = np.asarray(sizes, dtype=np.uint64)
+    tot = 0
+    for q in reqs:
+        if q["op"] == g.SV_WRITE:
+            tot += int(q["length"])
+        else:
+            size = int(sz[q["file"]])
+            o = min(int(q["offset"]), size)
+            tot += min(int(q["length"]), size - o)
+    return tot
+
+
+def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
+    import resource
+    import numpy as np
+    import gpufs_gb300 as g
+    soft, hard = resource.getrlimit(resource.RLIMIT_NOFILE)
+    if hard == resource.RLIM_INFINITY or hard > (1 << 20):
+        hard = 1 << 20
+    if soft < hard:
+        resource.setrlimit(resource.RLIMIT_NOFILE, (hard, hard))
+    soft, hard = resource.getrlimit(resource.RLIMIT_NOFILE)
+    avail = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_AVPHYS_PAGES")
+    target = min(48 << 30, int(avail * 0.3))
+    paths, dpath, sizes = _served_data(d, target, max(1000, soft - 2000))
+    total = sum(sizes)
+    n_out = 64
+    outs = [os.path.join(d, "w%02d.out" % i) for i in range(n_out)]
+    for o in outs:
+        if os.path.exists(o):
+            os.unlink(o)
+    rng = np.random.default_rng(0x5e)
+    page_log = 18
+    pool = 24 << 30
+    sess = g.Session(log_page=page_log, pool_bytes=pool, max_files=1 << 18, ring_slots=1 << 14, host_workers=workers,
+                     staging_depth=8, timeout_s=120, device=local)
+    budget = (pool >> page_log) // 2
+    clk.start()
+    t0 = time.perf_counter()
+    sv = g.Server(sess, dpath, paths, outs)
+    t_open = time.perf_counter() - t0
+    # saturation: a burst of requests all due at once
+    burst = _served_trace(sizes, 30000, n_out, rng)
+    sv.run(burst[:2000], inflight_pages=budget, warps_per_sm=16)  # warm-up
+    res = sv.run(burst, inflight_pages=budget, warps_per_sm=16)
+    # saturation: the whole burst (long enough that its last large requests
+    # are a small part of it), every request due at once
+    span = float(res["complete_ns"].max()) / 1e9
+    sat_rps = burst.size / span
+    sat_gbs = _served_bytes(burst, sizes) / span / 1e9
+    loads = []
+    checks = []
+    for frac in (0.1, 0.3, 0.5, 0.7, 0.9):
+        n_req = 20000
+        reqs = _served_trace(sizes, n_req, n_out, rng)
+        rate = frac * sat_rps
+        reqs["arrival_ns"] = np.cumsum(rng.exponential(1e9 / rate, n_req)).astype(np.uint64)
+        r = sv.run(reqs, inflight_pages=budget, warps_per_sm=16)
+        lat = (r["complete_ns"].astype(np.int64) - reqs["arrival_ns"].astype(np.int64)) / 1e3
+        dur = (int(r["complete_ns"].max()) - int(reqs["arrival_ns"].min())) / 1e9
+        loads.append({"offered_frac": frac, "offered_rps": rate, "achieved_rps": n_req / dur,
+                      "gbs": _served_bytes(reqs, sizes) / dur / 1e9,
+                      "p50_us": float(np.percentile(lat, 50)), "p99_us": float(np.percentile(lat, 99)),
+                      "p999_us": float(np.percentile(lat, 99.9)), "errors": int((r["status"] != 0).sum())})
+        checks.append((reqs, r))
+    sv.close()
+    st = sess.stats()
+    clocks = clk.stop()
+    sess.close()
+    parity = cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle
+        ok = True
+        n_checked = 0
+        raw = open(dpath, "rb").read()
+        for reqs, r in checks:
+            for k in range(0, reqs.size, 97):
+                q = reqs[k]
+                if q["op"] == g.SV_WRITE:
+                    continue
+                size = sizes[q["file"]]
+                o = min(int(q["offset"]), size)
+                e = min(o + int(q["length"]), size)
+                with open(paths[q["file"]], "rb") as f:
+                    f.seek(o)
+                    data = f.read(e - o)
+                if q["op"] == g.SV_READ:
+                    ok = ok and int(r[k]["result"]) == oracle.xxh64(np.frombuffer(data, dtype=np.uint8))
+                else:
+                    c = oracle.grep_counts(raw, [data], mode="fast")
+                    ok = ok and int(r[k]["result"]) == int(c[:, 0].sum())
+                n_checked += 1
+        parity = {"requests_checked": n_checked, "results_equal_oracle": bool(ok),
+                  "errors": int(sum(x["errors"] for x in loads))}
+        # CPU server: the same kind of requests on a thread pool (pread + XXH64 / tokenise)
+        from concurrent.futures import ThreadPoolExecutor
+        cpu_reqs = burst[:600]
+
+        def serve_cpu(q):
+            if q["op"] == g.SV_WRITE:
+                return 0
+            size = sizes[q["file"]]
+            o = min(int(q["offset"]), size)
+            e = min(o + int(q["length"]), size)
+            fd = os.open(paths[q["file"]], os.O_RDONLY)
+            try:
+                data = os.pread(fd, e - o, o)
+            finally:
+                os.close(fd)
+            if q["op"] == g.SV_READ:
+                return oracle.xxh64(np.frombuffer(data, dtype=np.uint8))
+            return int(oracle.grep_counts(raw, [data], mode="fast")[:, 0].sum())
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(nt) as ex:
+            list(ex.map(serve_cpu, cpu_reqs))
+        cpu_t = time.perf_counter() - t0
+        cpu = {"value": len(cpu_reqs) / cpu_t, "unit": "req/s", "cores": nt, "kind": "port",
+               "gbs": _served_bytes(cpu_reqs, sizes) / cpu_t / 1e9,
+               "sample": "600 requests of the saturation trace (reads and greps; writes skipped) on a thread pool: "
+                         "pread + XXH64 or tokenise + lookup (oracle)"}
+    if rank != 0:
+        return None
+    top = loads[-1]
+    extra.update({"files": len(paths), "total_bytes": total, "open_ms": t_open * 1e3, "saturation_rps": sat_rps,
+                  "saturation_gbs": sat_gbs, "loads": loads,
+                  "cache_stats": {k: st[k] for k in ("misses", "evictions", "writebacks", "host_map_reads")}})
+    return {"metric": METRIC, "value": ws * top["achieved_rps"], "unit": "req/s", "n_gpus": ws, "steps": len(loads),
+            "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u8",
+            "data": "synthetic: seeded files (random bytes and Zipf text), seeded request trace, Poisson arrivals",
+            "config": {"workload": "served: (file, offset, length, op) requests over %d files (%.1f GiB; the host's "
+                                   "open-file limit caps the file count, sizes scaled to keep the total), popularity "
+                                   "Zipf(0.9), lengths log-uniform 4 KiB-16 MiB, 80%% read+XXH64 / 15%% grep / 5%% "
+                                   "write, 24 GiB buffer cache, memory-gated admission, open-loop Poisson arrivals at "
+                                   "10-90%% of saturation" % (len(paths), total / 2 ** 30),
+                       "page_bytes": 1 << page_log, "warps_per_sm": 16, "admission_pages": budget,
+                       "value_at": "90%% of saturation load, p99 %.0f us" % top["p99_us"]},
+            "roofline": {"bound": "link", "achieved": top["gbs"], "peak": link[0] if link else None, "unit": "GB/s",
+                         "frac": top["gbs"] / link[0] if link else None, "peak_source": "measured pinned H2D",
+                         "traffic": None, "kernel": "k_serve", "algorithmic_bytes_per_launch": None,
+                         "mean_launch_ms": None},
+            "cpu_baseline": cpu,
+            "e2e": {"value": ws * top["achieved_rps"], "unit": "req/s", "p50_us": top["p50_us"],
+                    "p99_us": top["p99_us"], "p999_us": top["p999_us"], "gbs": top["gbs"],
+                    "call": "Server.run over the open-loop trace (host submission, device service, host completion)"},
+            "gpu_launches": len(loads) + 2, "clocks": clocks, "parity": parity, "extra": extra}
 
 
 def oracle_xxh64_file(path):

@@ -1047,44 +1047,56 @@ __device__ int pp_cover(gfs_state* S, const PinFile& pf, PagePair& p, uint32_t a
     return 0;
 }
 
-/* read + XXH64 of [off, end) of a served file, by one warp */
+/* read + XXH64 of [off, end) of a served file, by one warp.  Pages are
+ * pinned up to 8 at a time, one lane each, so the misses of a large request
+ * are in flight together; a pool short of frames falls back to one page at
+ * a time (multi-page pins do not wait for frames). */
 __device__ int sv_read_xxh(gfs_state* S, const ServeDev& D, int fd, uint64_t off, uint64_t end, uint8_t* st,
                            unsigned long long* result) {
     const int lane = threadIdx.x & 31;
     const uint32_t lp = S->log_page, pmask = S->page_size - 1u;
-    PinFile pf;
-    if (lane == 0) pf = pin_file(S, fd);
+    const PinFile pf = pin_file(S, fd);
     uint64_t v = gfsx::acc_init(lane & 3);
-    int fr = -1, err = 0;
-    uint32_t cur = 0xFFFFFFFFu;
+    int err = 0;
+    uint32_t batch = 8;
     const uint8_t* tail = st;
-    for (uint64_t pos = off; pos < end;) {
-        const uint32_t pg = (uint32_t)(pos >> lp);
-        if (pg != cur) {
-            if (lane == 0) {
-                if (fr >= 0) unpin(S, (uint32_t)fr);
-                bool fresh;
-                fr = pin_page(S, pf, pg, GFS_PIN_READ, &fresh);
-                if (fr >= 0 && fresh) publish_valid(S, (uint32_t)fr);
-            }
-            fr = __shfl_sync(0xFFFFFFFFu, fr, 0);
-            if (fr < 0) { err = fr; break; }
-            cur = pg;
+    for (uint64_t pos = off; pos < end && !err;) {
+        const uint32_t first = (uint32_t)(pos >> lp), last = (uint32_t)((end - 1) >> lp);
+        const uint32_t nb = last - first + 1u < batch ? last - first + 1u : batch;
+        int fr = -1;
+        if ((uint32_t)lane < nb) {
+            bool fresh;
+            fr = pin_page(S, pf, first + (uint32_t)lane, GFS_PIN_READ | (nb > 1 ? GFS_PIN_NOALLOC : 0), &fresh);
+            if (fr >= 0 && fresh) publish_valid(S, (uint32_t)fr);
         }
-        const uint32_t piece = end - pos < 512 ? (uint32_t)(end - pos) : 512u;
-        const uint8_t* src = S->pool + ((size_t)fr << lp) + (pos & pmask); /* 16-byte aligned */
-        const uint32_t o = (uint32_t)lane * 16u;
-        if (o + 16u <= piece) *(uint4*)(st + o) = ld_cg4(src + o);
-        else if (o < piece)
-            for (uint32_t b = o; b < piece; b++) st[b] = src[b];
-        __syncwarp();
-        const uint32_t stripes = piece / 32u;
-        if (lane < 4) v = gfsx::acc_stripes(v, st, stripes, lane);
-        tail = st + stripes * 32u;
-        pos += piece;
-        if (pos < end) __syncwarp();
+        const unsigned nomem = __ballot_sync(0xFFFFFFFFu, (uint32_t)lane < nb && fr == -GFS_ENOMEM);
+        const unsigned bad = __ballot_sync(0xFFFFFFFFu, (uint32_t)lane < nb && fr < 0 && fr != -GFS_ENOMEM);
+        if (bad || nomem) {
+            if ((uint32_t)lane < nb && fr >= 0) unpin(S, (uint32_t)fr);
+            if (bad) err = __shfl_sync(0xFFFFFFFFu, fr, __ffs(bad) - 1);
+            else batch = 1; /* take the pages one at a time, waiting for frames */
+            continue;
+        }
+        for (uint32_t j = 0; j < nb; j++) {
+            const int f = __shfl_sync(0xFFFFFFFFu, fr, (int)j);
+            const uint64_t pend = (((uint64_t)(first + j) + 1u) << lp) < end ? (((uint64_t)(first + j) + 1u) << lp) : end;
+            while (pos < pend) {
+                const uint32_t piece = pend - pos < 512 ? (uint32_t)(pend - pos) : 512u;
+                const uint8_t* src = S->pool + ((size_t)f << lp) + (pos & pmask); /* 16-byte aligned */
+                const uint32_t o = (uint32_t)lane * 16u;
+                if (o + 16u <= piece) *(uint4*)(st + o) = ld_cg4(src + o);
+                else if (o < piece)
+                    for (uint32_t b = o; b < piece; b++) st[b] = src[b];
+                __syncwarp();
+                const uint32_t stripes = piece / 32u;
+                if (lane < 4) v = gfsx::acc_stripes(v, st, stripes, lane);
+                tail = st + stripes * 32u;
+                pos += piece;
+                if (pos < end) __syncwarp();
+            }
+        }
+        if ((uint32_t)lane < nb) unpin(S, (uint32_t)fr);
     }
-    if (lane == 0 && fr >= 0 && !err) unpin(S, (uint32_t)fr);
     if (err) return err;
     const uint64_t v1 = __shfl_sync(0xFFFFFFFFu, v, 0), v2 = __shfl_sync(0xFFFFFFFFu, v, 1),
                    v3 = __shfl_sync(0xFFFFFFFFu, v, 2), v4 = __shfl_sync(0xFFFFFFFFu, v, 3);
