@@ -757,25 +757,15 @@ def _run_batched(args, rank, ws, local, td, d, nt, workers, hbm, how, link, extr
 
 
 def _served_data(d, target_bytes, max_files):
-    """Served corpus: 100,000 files of log-uniform sizes 4 KiB .. 3.3 MiB (mean
-    about 0.5 MB, 48 GiB) -- or, where the host allows fewer open files,
-    max_files files whose log-uniform range is scaled up to the same total --
+    """Served corpus: max_files (100,000) files of log-uniform sizes 4 KiB ..
+    3.3 MiB (mean about 0.5 MB), scaled so they total target_bytes (48 GiB),
     alternately seeded random bytes and Zipf text; the grep_text dictionary."""
-    import math
     import numpy as np
     from gpufs_gb300 import datagen
     os.makedirs(d, exist_ok=True)
-    n_files = min(100000, max_files)
-    lo, hi = 4096.0, 3.3 * (1 << 20)
-    mean = target_bytes / n_files
-    while (hi - lo) / math.log(hi / lo) < mean:  # widen the range until its mean covers the total
-        hi *= 1.05
-        lo *= 1.05
-    sizes = np.asarray(datagen.loguniform_sizes(n_files, int(lo), int(hi), seed=0x73657276), dtype=np.int64)
-    csum = np.cumsum(sizes)
-    n = int(np.searchsorted(csum, target_bytes)) + 1
-    n = min(n, sizes.size)
-    sizes = [int(x) for x in sizes[:n]]
+    n = max_files
+    sizes = np.asarray(datagen.loguniform_sizes(n, 4096, int(3.3 * (1 << 20)), seed=0x73657276), dtype=np.float64)
+    sizes = [max(1, int(x)) for x in sizes * (target_bytes / sizes.sum())]
     paths = [os.path.join(d, "s%06d.%s" % (i, "txt" if i % 2 == 0 else "bin")) for i in range(n)]
     dpath = os.path.join(d, "dict.gpu")
     stamp = os.path.join(d, "STAMP")
@@ -852,7 +842,7 @@ def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
     soft, hard = resource.getrlimit(resource.RLIMIT_NOFILE)
     avail = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_AVPHYS_PAGES")
     target = min(48 << 30, int(avail * 0.3))
-    paths, dpath, sizes = _served_data(d, target, max(1000, soft - 2000))
+    paths, dpath, sizes = _served_data(d, target, 100000)
     total = sum(sizes)
     n_out = 64
     outs = [os.path.join(d, "w%02d.out" % i) for i in range(n_out)]
@@ -958,8 +948,8 @@ def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
             "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u8",
             "data": "synthetic: seeded files (random bytes and Zipf text), seeded request trace, Poisson arrivals",
-            "config": {"workload": "served: (file, offset, length, op) requests over %d files (%.1f GiB; the host's "
-                                   "open-file limit caps the file count, sizes scaled to keep the total), popularity "
+            "config": {"workload": "served: (file, offset, length, op) requests over %d files (%.1f GiB, all open "
+                                   "on the device for the server's life), popularity "
                                    "Zipf(0.9), lengths log-uniform 4 KiB-16 MiB, 80%% read+XXH64 / 15%% grep / 5%% "
                                    "write, 24 GiB buffer cache, memory-gated admission, open-loop Poisson arrivals at "
                                    "10-90%% of saturation" % (len(paths), total / 2 ** 30),

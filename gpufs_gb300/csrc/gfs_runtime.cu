@@ -44,7 +44,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <memory>
 #include <mutex>
+#include <unordered_map>
 #include <thread>
 #include <vector>
 
@@ -53,25 +55,36 @@
 
 extern __device__ gfs_state* g_gfs;
 
+struct FileMap;
+
 namespace {
 
 struct Pending { /* a copy in flight: a read's H2D, or a write-back's D2H */
     uint32_t* done; /* host pointer of the completion word */
     uint32_t code;
     int write = 0;  /* write-back: merge and pwrite once the copy landed */
-    int host_fd = -1;
+    uint32_t file = 0; /* device file slot */
     uint64_t offset = 0;
     size_t len = 0;
     uint32_t rflags = 0;
 };
 
-/* Per open host fd: its size when opened and the pages written back since,
- * so a write-once page that lands on bytes nobody has written (past the
- * size at open, not written back before) needs no OR-merge read: those
- * bytes are zero. */
-struct FdInfo {
-    uint64_t size_at_open = 0;
+/* Host side of a device file slot (requests name the slot): the name and
+ * flags it was opened with, its host fd -- closed when the process nears its
+ * open-file limit and reopened by name when a request needs it -- its
+ * registered mapping, its size when opened and the pages written back
+ * since (a write-once page landing past the size at open on bytes not
+ * written back before needs no OR-merge read: those bytes are zero). */
+struct HostSlot {
     std::mutex mu;
+    char name[GFS_NAME_MAX + 1] = {0};
+    int oflags = 0; /* for reopening: no O_CREAT/O_TRUNC/O_EXCL */
+    int fd = -1;
+    int users = 0;  /* requests inside a syscall on fd */
+    bool open = false;
+    uint64_t last = 0;
+    std::atomic<FileMap*> map{nullptr};
+    uint64_t size_at_open = 0;
     std::vector<uint64_t> written; /* bit per page */
 };
 
@@ -176,9 +189,13 @@ struct gfs_ctx {
     size_t d_scratch_cap = 0;
     /* registered file mappings */
     std::mutex map_mu;
-    std::vector<FileMap*> maps;
-    std::vector<std::atomic<FileMap*>> fd_map; /* host fd -> mapping, read lock-free by workers */
-    std::vector<std::atomic<FdInfo*>> fd_info; /* host fd -> write-back bookkeeping */
+    std::unordered_multimap<uint64_t, FileMap*> maps; /* by inode */
+    size_t map_count_cap = 0; /* mappings, well under the process's map-area limit */
+    std::unique_ptr<HostSlot[]> slots; /* one per device file slot */
+    std::atomic<int> open_fds{0};
+    int fd_cap = 0;
+    std::atomic<uint64_t> fd_clock{0};
+    std::atomic<uint32_t> evict_hand{0};
     size_t mapped_bytes = 0, map_cap = 0;
     uint64_t map_clock = 0;
     std::atomic<unsigned long long> h_map_reads{0};
@@ -205,23 +222,36 @@ static void log_failure(gfs_ctx* c, const gfs_req& r, int err) {
 /* A write-back whose page has landed in staging slot k: OR-merge with the
  * file's bytes for write-once files (diff_and_merge, host_loop.h:76-137),
  * unless those bytes are known to be zero, then pwrite. */
+static int slot_acquire_fd(gfs_ctx* c, uint32_t s);
+static void slot_release_fd(gfs_ctx* c, uint32_t s);
+
 static void finish_write(gfs_ctx* c, Worker* w, int k, const Pending& p) {
     uint8_t* buf = w->staging + (size_t)k * w->slot_bytes;
     const size_t len = p.len;
     bool merge = (p.rflags & GFS_RF_DIFF) != 0;
-    FdInfo* fi = (p.host_fd >= 0 && (size_t)p.host_fd < c->fd_info.size())
-                     ? c->fd_info[(size_t)p.host_fd].load(std::memory_order_acquire)
-                     : nullptr;
-    if (fi) {
+    gfs_req r{};
+    r.op = GFS_OP_WRITE;
+    r.file = p.file;
+    r.offset = p.offset;
+    r.length = len;
+    const int fd = slot_acquire_fd(c, p.file);
+    if (fd < 0) {
+        log_failure(c, r, -fd);
+        set_done(c, p.done, GFS_DONE_ERR | (uint32_t)(-fd));
+        return;
+    }
+    r.host_fd = fd;
+    {
+        HostSlot& h = c->slots[p.file];
         const uint64_t pg = p.offset >> c->hs.log_page;
-        std::lock_guard<std::mutex> lk(fi->mu);
-        if (fi->written.size() <= (size_t)(pg >> 6)) fi->written.resize((size_t)(pg >> 6) + 1, 0ULL);
+        std::lock_guard<std::mutex> lk(h.mu);
+        if (h.written.size() <= (size_t)(pg >> 6)) h.written.resize((size_t)(pg >> 6) + 1, 0ULL);
         const uint64_t bit = 1ULL << (pg & 63u);
-        if (merge && p.offset >= fi->size_at_open && !(fi->written[(size_t)(pg >> 6)] & bit)) merge = false;
-        fi->written[(size_t)(pg >> 6)] |= bit;
+        if (merge && p.offset >= h.size_at_open && !(h.written[(size_t)(pg >> 6)] & bit)) merge = false;
+        h.written[(size_t)(pg >> 6)] |= bit;
     }
     if (merge) {
-        ssize_t m = pread_full(p.host_fd, w->merge, len, (off_t)p.offset);
+        ssize_t m = pread_full(fd, w->merge, len, (off_t)p.offset);
         size_t i = 0;
         for (; m >= 8 && i + 8 <= (size_t)m; i += 8) {
             uint64_t a, b;
@@ -232,13 +262,9 @@ static void finish_write(gfs_ctx* c, Worker* w, int k, const Pending& p) {
         }
         for (; (ssize_t)i < m; i++) buf[i] |= w->merge[i];
     }
-    gfs_req r{};
-    r.op = GFS_OP_WRITE;
-    r.host_fd = p.host_fd;
-    r.offset = p.offset;
-    r.length = len;
-    ssize_t put = pwrite_full(p.host_fd, buf, len, (off_t)p.offset);
+    ssize_t put = pwrite_full(fd, buf, len, (off_t)p.offset);
     int err = put < 0 ? errno : EIO;
+    slot_release_fd(c, p.file);
     c->h_writes++;
     if (put >= 0) c->h_write_bytes += (unsigned long long)put;
     if (put != (ssize_t)len) log_failure(c, r, err);
@@ -282,40 +308,52 @@ static void map_release(FileMap* m) {
 
 /* Mapping for a file just opened read-only (host fd `fd`, stat `st`), made
  * on first use and kept while unchanged; nullptr when it cannot be made. */
-static void map_attach(gfs_ctx* c, int fd, const struct stat& st) {
-    if ((c->cfg.flags & GFS_CFG_NO_FILE_MAP) || !S_ISREG(st.st_mode) || st.st_size < (off_t)(64 << 10)) return;
-    if (fd < 0 || (size_t)fd >= c->fd_map.size()) return;
+static FileMap* map_attach(gfs_ctx* c, int fd, const struct stat& st) {
+    if ((c->cfg.flags & GFS_CFG_NO_FILE_MAP) || !S_ISREG(st.st_mode) || st.st_size < (off_t)(64 << 10)) return nullptr;
     const int64_t ct = (int64_t)st.st_ctim.tv_sec * 1000000000LL + st.st_ctim.tv_nsec;
     const size_t len = (size_t)st.st_size;
+    const uint64_t key = (uint64_t)st.st_ino * 0x9E3779B97F4A7C15ULL ^ (uint64_t)st.st_dev;
     {
         std::lock_guard<std::mutex> lk(c->map_mu);
-        for (FileMap* m : c->maps)
+        auto rg = c->maps.equal_range(key);
+        for (auto it = rg.first; it != rg.second; ++it) {
+            FileMap* m = it->second;
             if (m->dev == (uint64_t)st.st_dev && m->ino == (uint64_t)st.st_ino && m->size == (uint64_t)len &&
                 m->ctime_ns == ct) {
                 m->refs++;
                 m->last = ++c->map_clock;
-                c->fd_map[(size_t)fd].store(m, std::memory_order_release);
-                return;
+                return m;
             }
-        if (c->mapped_bytes + len > c->map_cap) {
+        }
+        if (c->mapped_bytes + len > c->map_cap || c->maps.size() + 1 > c->map_count_cap) {
             /* evict unused mappings, least recently used first */
-            std::sort(c->maps.begin(), c->maps.end(), [](FileMap* a, FileMap* b) { return a->last < b->last; });
-            for (size_t i = 0; i < c->maps.size() && c->mapped_bytes + len > c->map_cap;) {
-                FileMap* m = c->maps[i];
-                if (m->refs) { i++; continue; }
+            std::vector<std::pair<uint64_t, FileMap*>> idle;
+            for (auto& e : c->maps)
+                if (!e.second->refs) idle.push_back({e.second->last, e.second});
+            std::sort(idle.begin(), idle.end());
+            for (size_t i = 0; i < idle.size() &&
+                               (c->mapped_bytes + len > c->map_cap || c->maps.size() + 1 > c->map_count_cap);
+                 i++) {
+                FileMap* m = idle[i].second;
+                const uint64_t k = m->ino * 0x9E3779B97F4A7C15ULL ^ m->dev;
+                auto r2 = c->maps.equal_range(k);
+                for (auto it = r2.first; it != r2.second; ++it)
+                    if (it->second == m) {
+                        c->maps.erase(it);
+                        break;
+                    }
                 c->mapped_bytes -= m->len;
-                c->maps.erase(c->maps.begin() + (long)i);
                 map_release(m);
             }
-            if (c->mapped_bytes + len > c->map_cap) return;
+            if (c->mapped_bytes + len > c->map_cap || c->maps.size() + 1 > c->map_count_cap) return nullptr;
         }
     }
     void* p = mmap(nullptr, len, PROT_READ, MAP_SHARED | MAP_POPULATE, fd, 0);
-    if (p == MAP_FAILED) return;
+    if (p == MAP_FAILED) return nullptr;
     if (cudaHostRegister(p, len, cudaHostRegisterDefault) != cudaSuccess) {
         cudaGetLastError();
         munmap(p, len);
-        return;
+        return nullptr;
     }
     FileMap* m = new FileMap();
     m->dev = (uint64_t)st.st_dev;
@@ -327,17 +365,63 @@ static void map_attach(gfs_ctx* c, int fd, const struct stat& st) {
     m->refs = 1;
     std::lock_guard<std::mutex> lk(c->map_mu);
     m->last = ++c->map_clock;
-    c->maps.push_back(m);
+    c->maps.emplace(key, m);
     c->mapped_bytes += len;
-    c->fd_map[(size_t)fd].store(m, std::memory_order_release);
+    return m;
 }
 
-static void map_detach(gfs_ctx* c, int fd) {
-    if (fd < 0 || (size_t)fd >= c->fd_map.size()) return;
-    FileMap* m = c->fd_map[(size_t)fd].exchange(nullptr, std::memory_order_acq_rel);
+static void map_detach(gfs_ctx* c, FileMap* m) {
     if (!m) return;
     std::lock_guard<std::mutex> lk(c->map_mu);
     m->refs--;
+}
+
+/* Close the host fds of idle slots (clock order) until the process is
+ * comfortably below its open-file limit; `keep` is spared. */
+static void fd_evict(gfs_ctx* c, uint32_t keep) {
+    const uint32_t n = c->hs.n_files;
+    const int target = c->fd_cap - c->fd_cap / 8;
+    for (uint32_t tries = 0; tries < 2 * n && c->open_fds.load() > target; tries++) {
+        const uint32_t i = c->evict_hand.fetch_add(1) % n;
+        if (i == keep) continue;
+        HostSlot& h = c->slots[i];
+        if (!h.mu.try_lock()) continue;
+        if (h.fd >= 0 && h.users == 0) {
+            close(h.fd);
+            h.fd = -1;
+            c->open_fds--;
+        }
+        h.mu.unlock();
+    }
+}
+
+/* The host fd of slot s for one syscall (reopened by name if it was
+ * closed); -errno when the slot is not open.  Pair with slot_release_fd. */
+static int slot_acquire_fd(gfs_ctx* c, uint32_t s) {
+    if (s >= c->hs.n_files) return -EBADF;
+    HostSlot& h = c->slots[s];
+    bool reopened = false;
+    int fd;
+    {
+        std::lock_guard<std::mutex> lk(h.mu);
+        if (!h.open) return -EBADF;
+        if (h.fd < 0) {
+            h.fd = open(h.name, h.oflags | O_CLOEXEC);
+            if (h.fd < 0) return -errno;
+            reopened = true;
+        }
+        h.users++;
+        h.last = ++c->fd_clock;
+        fd = h.fd;
+    }
+    if (reopened && ++c->open_fds > c->fd_cap) fd_evict(c, s);
+    return fd;
+}
+
+static void slot_release_fd(gfs_ctx* c, uint32_t s) {
+    HostSlot& h = c->slots[s];
+    std::lock_guard<std::mutex> lk(h.mu);
+    h.users--;
 }
 
 static int host_open_flags(int oflags) {
@@ -357,23 +441,33 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         char name[GFS_NAME_MAX + 1];
         memcpy(name, r.name, GFS_NAME_MAX);
         name[GFS_NAME_MAX] = 0;
-        int fd = open(name, host_open_flags(r.oflags) | O_CLOEXEC, 0644);
-        int err = fd < 0 ? errno : 0;
+        const int hflags = host_open_flags(r.oflags);
+        int fd = r.file < c->hs.n_files ? open(name, hflags | O_CLOEXEC, 0644) : -1;
+        int err = fd < 0 ? (r.file < c->hs.n_files ? errno : EBADF) : 0;
         gfs_open_reply rep{};
         rep.host_fd = fd;
         rep.err = err;
         if (fd >= 0) {
             struct stat st;
-            if (fstat(fd, &st) == 0) {
-                rep.size = (uint64_t)st.st_size;
-                rep.ctime_ns = (int64_t)st.st_ctim.tv_sec * 1000000000LL + st.st_ctim.tv_nsec;
-                if ((host_open_flags(r.oflags) & O_ACCMODE) == O_RDONLY) map_attach(c, fd, st);
-                if ((size_t)fd < c->fd_info.size()) {
-                    FdInfo* fi = new FdInfo();
-                    fi->size_at_open = (uint64_t)st.st_size;
-                    delete c->fd_info[(size_t)fd].exchange(fi, std::memory_order_acq_rel);
-                }
+            if (fstat(fd, &st) != 0) memset(&st, 0, sizeof st);
+            rep.size = (uint64_t)st.st_size;
+            rep.ctime_ns = (int64_t)st.st_ctim.tv_sec * 1000000000LL + st.st_ctim.tv_nsec;
+            FileMap* fm = (hflags & O_ACCMODE) == O_RDONLY ? map_attach(c, fd, st) : nullptr;
+            HostSlot& h = c->slots[r.file];
+            {
+                std::lock_guard<std::mutex> lk(h.mu);
+                if (h.fd >= 0) { close(h.fd); c->open_fds--; } /* left over from an unclean close */
+                map_detach(c, h.map.exchange(fm));
+                memcpy(h.name, name, sizeof h.name);
+                h.oflags = hflags & ~(O_CREAT | O_TRUNC | O_EXCL);
+                h.fd = fd;
+                h.users = 0;
+                h.open = true;
+                h.last = ++c->fd_clock;
+                h.size_at_open = (uint64_t)st.st_size;
+                h.written.clear();
             }
+            if (++c->open_fds > c->fd_cap) fd_evict(c, r.file);
         }
         if (r.file < c->hs.n_files) {
             gfs_open_reply* dst = (gfs_open_reply*)(c->hmap + c->reply_off + (size_t)r.file * sizeof(gfs_open_reply));
@@ -385,11 +479,21 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         break;
     }
     case GFS_OP_CLOSE: {
-        map_detach(c, r.host_fd);
-        if (r.host_fd >= 0 && (size_t)r.host_fd < c->fd_info.size())
-            delete c->fd_info[(size_t)r.host_fd].exchange(nullptr, std::memory_order_acq_rel);
-        int rc = r.host_fd >= 0 ? close(r.host_fd) : 0;
-        set_done(c, done, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno));
+        int rc = 0, e = 0;
+        if (r.file < c->hs.n_files) {
+            HostSlot& h = c->slots[r.file];
+            std::lock_guard<std::mutex> lk(h.mu);
+            if (h.fd >= 0) {
+                rc = close(h.fd);
+                e = errno;
+                h.fd = -1;
+                c->open_fds--;
+            }
+            map_detach(c, h.map.exchange(nullptr));
+            h.open = false;
+            h.written.clear();
+        }
+        set_done(c, done, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)e));
         break;
     }
     case GFS_OP_READ: {
@@ -400,9 +504,7 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         size_t len = (size_t)r.length;
         if (len > w->slot_bytes) len = w->slot_bytes;
         int k = slot_take(c, w);
-        FileMap* fm = (r.host_fd >= 0 && (size_t)r.host_fd < c->fd_map.size())
-                          ? c->fd_map[(size_t)r.host_fd].load(std::memory_order_acquire)
-                          : nullptr;
+        FileMap* fm = r.file < c->hs.n_files ? c->slots[r.file].map.load(std::memory_order_acquire) : nullptr;
         if (fm && r.offset < fm->len) {
             /* DMA straight from the registered page-cache mapping */
             const size_t n = len < fm->len - (size_t)r.offset ? len : fm->len - (size_t)r.offset;
@@ -428,11 +530,18 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
             break;
         }
         uint8_t* buf = w->staging + (size_t)k * w->slot_bytes;
-        ssize_t n = pread_full(r.host_fd, buf, len, (off_t)r.offset);
+        const int fd = slot_acquire_fd(c, r.file);
+        if (fd < 0) {
+            log_failure(c, r, -fd);
+            set_done(c, done, GFS_DONE_ERR | (uint32_t)(-fd));
+            break;
+        }
+        ssize_t n = pread_full(fd, buf, len, (off_t)r.offset);
+        const int rerr = errno;
+        slot_release_fd(c, r.file);
         if (n < 0) {
-            int e = errno;
-            log_failure(c, r, e);
-            set_done(c, done, GFS_DONE_ERR | (uint32_t)e);
+            log_failure(c, r, rerr);
+            set_done(c, done, GFS_DONE_ERR | (uint32_t)rerr);
             break;
         }
         size_t cp = ((size_t)n + 4095u) & ~(size_t)4095u;
@@ -475,7 +584,7 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         }
         Pending pw{done, 0u};
         pw.write = 1;
-        pw.host_fd = r.host_fd;
+        pw.file = r.file;
         pw.offset = r.offset;
         pw.len = len;
         pw.rflags = r.rflags;
@@ -486,8 +595,15 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         break;
     }
     case GFS_OP_TRUNC: {
-        int rc = ftruncate(r.host_fd, (off_t)r.length);
-        set_done(c, done, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)errno));
+        const int fd = slot_acquire_fd(c, r.file);
+        if (fd < 0) {
+            set_done(c, done, GFS_DONE_ERR | (uint32_t)(-fd));
+            break;
+        }
+        int rc = ftruncate(fd, (off_t)r.length);
+        const int e = errno;
+        slot_release_fd(c, r.file);
+        set_done(c, done, rc == 0 ? 1u : (GFS_DONE_ERR | (uint32_t)e));
         break;
     }
     case GFS_OP_UNLINK: {
@@ -629,18 +745,23 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
     cfg.max_files = next_pow2(cfg.max_files < 64 ? 64 : cfg.max_files);
     if (cfg.max_files > (1u << 20)) { delete c; return -GFS_EINVAL; }
     {
-        /* registered file mappings: one slot per possible host fd, at most
-         * half the host memory mapped */
+        /* host fds per file slot, below the open-file limit; registered
+         * file mappings, at most half the host memory */
         struct rlimit rl;
         size_t nfd = 1u << 16;
         if (getrlimit(RLIMIT_NOFILE, &rl) == 0 && rl.rlim_cur != RLIM_INFINITY && rl.rlim_cur < (1u << 20))
             nfd = (size_t)rl.rlim_cur;
-        c->fd_map = std::vector<std::atomic<FileMap*>>(nfd);
-        for (auto& a : c->fd_map) a.store(nullptr);
-        c->fd_info = std::vector<std::atomic<FdInfo*>>(nfd);
-        for (auto& a : c->fd_info) a.store(nullptr);
+        /* host fds stay below the open-file limit, with room for the process */
+        c->fd_cap = nfd > 2048 ? (int)nfd - 1024 : (int)nfd / 2;
+        if (c->fd_cap < 16) c->fd_cap = 16;
         const long pages = sysconf(_SC_PHYS_PAGES), psz = sysconf(_SC_PAGESIZE);
         c->map_cap = pages > 0 && psz > 0 ? (size_t)pages * (size_t)psz / 2 : (size_t)8 << 30;
+        long mm = 65530;
+        if (FILE* f = fopen("/proc/sys/vm/max_map_count", "r")) {
+            if (fscanf(f, "%ld", &mm) != 1) mm = 65530;
+            fclose(f);
+        }
+        c->map_count_cap = mm > 8192 ? (size_t)(mm / 2) : 4096;
     }
     {
         uint64_t page = 1ull << cfg.log_page;
@@ -653,6 +774,7 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
         s.n_frames = (uint32_t)nf;
         s.n_buckets = next_pow2((nf + 3) / 4 < 64 ? 64 : (nf + 3) / 4);
         s.n_files = cfg.max_files;
+        c->slots.reset(new HostSlot[cfg.max_files]);
         s.ring_slots = cfg.ring_slots;
         s.timeout_ns = cfg.timeout_ns;
         CK(cudaSetDevice(cfg.device));
@@ -734,9 +856,11 @@ int gfs_destroy(gfs_ctx* c) {
         delete w;
     }
     c->workers.clear();
-    for (FileMap* m : c->maps) map_release(m);
+    if (c->slots)
+        for (uint32_t i = 0; i < c->hs.n_files; i++)
+            if (c->slots[i].fd >= 0) close(c->slots[i].fd);
+    for (auto& e : c->maps) map_release(e.second);
     c->maps.clear();
-    for (auto& a : c->fd_info) delete a.exchange(nullptr);
     gfs_state& s = c->hs;
     gfs_state* none = nullptr;
     if (c->ds && g_current == c) {
