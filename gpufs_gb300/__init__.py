@@ -97,6 +97,15 @@ _SIGS = {
                                ctypes.POINTER(ctypes.c_float)]),
     "gfs_xxh64_files_noalloc": (_int, [_c_p, ctypes.POINTER(_c_s), _int, ctypes.POINTER(ctypes.c_ulonglong)]),
     "gfs_measure_link": (_int, [_u64, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "gfs_cm_create": (_int, [_int, _int, ctypes.c_ulonglong, ctypes.POINTER(_c_p)]),
+    "gfs_cm_destroy": (_int, [_c_p]),
+    "gfs_cm_n_params": (_int, [_c_p]),
+    "gfs_cm_get_params": (_int, [_c_p, _c_p]),
+    "gfs_cm_set_params": (_int, [_c_p, _c_p]),
+    "gfs_cm_set_data": (_int, [_c_p, _c_p, _c_p, _int]),
+    "gfs_cm_grad": (_int, [_c_p, _c_p, ctypes.POINTER(ctypes.c_float)]),
+    "gfs_cm_train": (_int, [_c_p, _int, ctypes.c_float, _c_p]),
+    "gfs_cm_predict": (_int, [_c_p, _c_p, _int, _c_p]),
 }
 
 

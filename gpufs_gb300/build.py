@@ -18,7 +18,8 @@ CSRC = os.path.join(HERE, "csrc")
 INC = os.path.join(ROOT, "include")
 OUT = os.path.join(HERE, "_build")
 
-CUDA_SOURCES = ["gfs_calls.cu", "gfs_runtime.cu", "gfs_workloads.cu", "gfs_grep.cu", "gfs_apps.cu"]
+CUDA_SOURCES = ["gfs_calls.cu", "gfs_runtime.cu", "gfs_workloads.cu", "gfs_grep.cu", "gfs_apps.cu",
+                "gfs_costmodel.cu"]
 # Device-API translation units are linked as relocatable code into kernels of
 # any block size (up to 1024 threads): cap them at 64 registers per thread.
 PER_FILE_FLAGS = {"gfs_calls.cu": ["-maxrregcount=64"], "gfs_workloads.cu": ["-maxrregcount=64"],

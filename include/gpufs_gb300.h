@@ -208,6 +208,32 @@ int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_re
 /* closes every file (dirty output pages are written back) */
 int gfs_serve_close(gfs_server* sv);
 
+/* ---- learned cost model for the autotuner (no reference counterpart) ----
+ * A network n_in -> 64 -> 64 -> 1 (tanh hidden units, FP32) that predicts a
+ * run's log time from workload features and session parameters, trained on
+ * the device by the library's own forward/backward and Adam kernels (mean
+ * squared error over the data set, full batch, deterministic).  Parameters
+ * are one flat vector: W1 [n_in][64], b1 [64], W2 [64][64], b2 [64], w3 [64],
+ * b3.  X is row-major [n][n_in]. */
+#define GFS_CM_HIDDEN 64
+#define GFS_CM_MAX_INPUTS 64
+typedef struct gfs_costmodel gfs_costmodel;
+/* Glorot-uniform weights from a seeded stream, zero biases */
+int gfs_cm_create(int n_in, int device, unsigned long long seed, gfs_costmodel** out);
+int gfs_cm_destroy(gfs_costmodel* cm);
+int gfs_cm_n_params(const gfs_costmodel* cm);
+int gfs_cm_get_params(gfs_costmodel* cm, float* host_out);
+/* also resets the optimiser state */
+int gfs_cm_set_params(gfs_costmodel* cm, const float* host_in);
+/* the training set (copied to the device) */
+int gfs_cm_set_data(gfs_costmodel* cm, const float* X, const float* y, int n);
+/* loss and its gradient with respect to every parameter, on the training set */
+int gfs_cm_grad(gfs_costmodel* cm, float* host_grad, float* host_loss);
+/* `steps` full-batch Adam steps (fresh optimiser state); host_losses, when not
+ * NULL, receives the loss before each step */
+int gfs_cm_train(gfs_costmodel* cm, int steps, float lr, float* host_losses);
+int gfs_cm_predict(gfs_costmodel* cm, const float* X, int n, float* host_y);
+
 /* one call: open + run + counts to host + close (the reference sample's whole run) */
 int gfs_grep_text(gfs_ctx* ctx, const char* dict_path, const char* const* paths, int n_files, uint32_t* host_counts,
                   int n_ctas);
