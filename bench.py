@@ -883,6 +883,14 @@ def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
                       "p50_us": float(np.percentile(lat, 50)), "p99_us": float(np.percentile(lat, 99)),
                       "p999_us": float(np.percentile(lat, 99.9)), "errors": int((r["status"] != 0).sum())})
         checks.append((reqs, r))
+    # the plain per-call path: the same kind of requests, one call (one launch) each
+    single = _served_trace(sizes, 300, n_out, rng)
+    t0 = time.perf_counter()
+    for k in range(single.size):
+        sv.run(single[k:k + 1], inflight_pages=budget, warps_per_sm=1)
+    per_call_s = time.perf_counter() - t0
+    per_call = {"rps": single.size / per_call_s, "gbs": _served_bytes(single, sizes) / per_call_s / 1e9,
+                "call": "Server.run of one request at a time (a launch, a submission and a completion per request)"}
     sv.close()
     st = sess.stats()
     clocks = clk.stop()
@@ -942,7 +950,8 @@ def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
         return None
     top = loads[-1]
     extra.update({"files": len(paths), "total_bytes": total, "open_ms": t_open * 1e3, "saturation_rps": sat_rps,
-                  "saturation_gbs": sat_gbs, "loads": loads,
+                  "saturation_gbs": sat_gbs, "loads": loads, "per_call": per_call,
+                  "served_over_per_call": loads[-1]["achieved_rps"] / per_call["rps"],
                   "cache_stats": {k: st[k] for k in ("misses", "evictions", "writebacks", "host_map_reads")}})
     return {"metric": METRIC, "value": ws * top["achieved_rps"], "unit": "req/s", "n_gpus": ws, "steps": len(loads),
             "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
