@@ -277,8 +277,26 @@ def main():
             e2e_times.append(dt)
     e2e_ok = bool(np.array_equal(c, gpu_counts))
     e2e_t = allmax(td, sum(e2e_times) / len(e2e_times))
+    # where one cold call's time goes (the same steps, timed one by one)
+    sess.drop_cache()
+    t0 = time.perf_counter()
+    p2 = g.Grep(sess, dpath, paths)
+    t1 = time.perf_counter()
+    p2.run(args.ctas)
+    t2 = time.perf_counter()
+    p2.counts()
+    t3 = time.perf_counter()
+    p2.close()
+    t4 = time.perf_counter()
+    e2e_parts = {"open_ms": (t1 - t0) * 1e3, "table_build_ms": p2.build_us / 1e3, "file_open_ms": p2.open_us / 1e3,
+                 "run_cold_ms": (t2 - t1) * 1e3, "counts_ms": (t3 - t2) * 1e3, "close_ms": (t4 - t3) * 1e3}
+    sess.drop_cache()
+    with g.Grep(sess, dpath, paths) as p3:
+        t0 = time.perf_counter()
+        p3.run(args.ctas, direct=True)
+        e2e_parts["run_direct_ms"] = (time.perf_counter() - t0) * 1e3
     # ---- extras: cache-hit / cold gread, link bandwidth ----
-    extra = {}
+    extra = {"e2e_parts": e2e_parts}
     try:
         if args.no_extra:
             raise RuntimeError("skipped")
@@ -286,6 +304,13 @@ def main():
         extra["link_h2d_gbs"] = h2d
         extra["link_d2h_gbs"] = d2h
         extra["e2e_over_link_h2d"] = (corpus / e2e_t / 1e9) / h2d if h2d else None
+        # ceilings of the cold path: copies over many streams, from pinned
+        # memory and from a registered file mapping, and SM reads of both
+        probe = os.path.join(data_dir, "link_probe.bin")
+        if not os.path.exists(probe) or os.path.getsize(probe) != 1 << 30:
+            from gpufs_gb300 import datagen
+            datagen.uniform_bytes(probe, 1 << 30, seed=0x6c696e6b)
+        extra["cold_paths_gbs"] = g.measure_cold_paths(probe, streams=workers, chunk=page, reps=3)
     except Exception as ex:  # noqa: BLE001
         extra["link_error"] = str(ex)
     clocks = clk.stop()

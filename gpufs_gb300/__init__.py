@@ -80,6 +80,7 @@ _SIGS = {
     "gfs_memcopy": (_int, [_c_p, _c_s, _c_s, _int, _int, _int, ctypes.POINTER(ctypes.c_float)]),
     "gfs_grep_open": (_int, [_c_p, _c_s, ctypes.POINTER(_c_s), _int, ctypes.POINTER(_c_p)]),
     "gfs_grep_run": (_int, [_c_p, _int, ctypes.POINTER(ctypes.c_float)]),
+    "gfs_grep_run_direct": (_int, [_c_p, _int, ctypes.POINTER(ctypes.c_float)]),
     "gfs_grep_counts": (_int, [_c_p, _c_p]),
     "gfs_grep_device_counts": (_c_p, [_c_p]),
     "gfs_grep_info": (_int, [_c_p, ctypes.POINTER(ctypes.c_longlong), _int]),
@@ -97,6 +98,7 @@ _SIGS = {
                                ctypes.POINTER(ctypes.c_float)]),
     "gfs_xxh64_files_noalloc": (_int, [_c_p, ctypes.POINTER(_c_s), _int, ctypes.POINTER(ctypes.c_ulonglong)]),
     "gfs_measure_link": (_int, [_u64, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "gfs_measure_cold_paths": (_int, [_c_s, _int, _u64, _int, ctypes.POINTER(ctypes.c_float), _int]),
     "gfs_cm_create": (_int, [_int, _int, ctypes.c_ulonglong, ctypes.POINTER(_c_p)]),
     "gfs_cm_destroy": (_int, [_c_p]),
     "gfs_cm_n_params": (_int, [_c_p]),
@@ -299,14 +301,17 @@ class Grep:
         self._info()
 
     def _info(self):
-        info = (ctypes.c_longlong * 8)()
-        self.s.L.gfs_grep_info(self._h, info, 8)
+        info = (ctypes.c_longlong * 10)()
+        self.s.L.gfs_grep_info(self._h, info, 10)
         (self.n_words, self.n_files, self.buckets, self.smem_table, self.smem_bytes, self.chunks, self.status,
-         self.status_site) = [int(v) for v in info]
+         self.status_site, self.build_us, self.open_us) = [int(v) for v in info]
 
-    def run(self, n_ctas=0):
+    def run(self, n_ctas=0, direct=False):
+        """One scan; direct=True reads files with a registered host mapping
+        straight from it, bypassing the buffer cache."""
         ms = ctypes.c_float(0)
-        rc = self.s.L.gfs_grep_run(self._h, n_ctas, ctypes.byref(ms))
+        fn = self.s.L.gfs_grep_run_direct if direct else self.s.L.gfs_grep_run
+        rc = fn(self._h, n_ctas, ctypes.byref(ms))
         if rc < 0:
             self._info()
             raise GfsError(-rc, "gfs_grep_run failed: status 0x%x site 0x%x, session %s" % (
@@ -362,6 +367,17 @@ def grep_text(sess, dict_path, paths, n_ctas=0):
     _check(sess.L.gfs_grep_text(sess.handle, _p(dict_path), _paths(paths), len(paths),
                                 out.ctypes.data if out.size else None, n_ctas), "gfs_grep_text")
     return out
+
+
+def measure_cold_paths(path, streams=16, chunk=2 << 20, reps=3):
+    """Cold-read ceilings for one file (GB/s): pinned single copy, pinned
+    chunked over streams, registered file mapping chunked over streams, a
+    kernel reading pinned memory, a kernel reading the file mapping."""
+    out = (ctypes.c_float * 7)()
+    _check(lib().gfs_measure_cold_paths(os.fsencode(path), streams, chunk, reps, out, 7), "gfs_measure_cold_paths")
+    keys = ("pinned_1_copy", "pinned_streams", "file_map_streams", "kernel_pinned", "kernel_file_map",
+            "kernel_file_map_slices", "kernel_file_map_slices_1warp")
+    return dict(zip(keys, [float(v) for v in out]))
 
 
 def measure_link(nbytes=1 << 30, reps=5):

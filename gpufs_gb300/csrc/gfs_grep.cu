@@ -47,6 +47,7 @@
 #include <string>
 #include <thread>
 #include <unordered_map>
+#include <mutex>
 #include <vector>
 
 #include "gfs_device.cuh"
@@ -92,6 +93,9 @@ struct GrepDev {
     const int* file_order;        /* file indices by decreasing size */
     uint32_t* file_next;          /* next position in file_order */
     unsigned long long* xxh;      /* per-file XXH64 */
+    /* direct scan: files with a registered host mapping are read from it by
+     * the SMs, bypassing the buffer cache */
+    const uint64_t* maps;         /* per file: device address of its host mapping, 0 if none */
 };
 
 namespace {
@@ -370,6 +374,52 @@ __device__ __forceinline__ uint32_t other_cands16(const GrepDev& P, const Tbl& t
     return 0xFFFFFFFFu;
 }
 
+/* NTOK tokens per lane (list entries tb0 + lane + 32 i), straight-line so
+ * their loads overlap */
+template <int NTOK, class Sink>
+__device__ __forceinline__ void scan_tokens(const GrepDev& P, const Tbl& tbl, const uint8_t* base, const uint32_t* bm,
+                                            const uint16_t* slist, uint32_t seg0, uint32_t tb0, uint32_t n_s,
+                                            const uint4* km, Sink& sink) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t st[NTOK], len[NTOK], k[NTOK][4], b1[NTOK], b2[NTOK], m[NTOK], slot[NTOK];
+    bool v[NTOK], f[NTOK];
+#pragma unroll
+    for (int i = 0; i < NTOK; i++) {
+        const uint32_t ti = tb0 + lane + 32u * (uint32_t)i;
+        v[i] = ti < n_s;
+        st[i] = v[i] ? slist[ti] : seg0;
+        len[i] = v[i] ? run_len(bm, st[i] - seg0) : 0u;
+        f[i] = v[i] && len[i] <= 16u;
+    }
+#pragma unroll
+    for (int i = 0; i < NTOK; i++) key16(base, st[i], f[i] ? len[i] : 0u, k[i], km);
+#pragma unroll
+    for (int i = 0; i < NTOK; i++) m[i] = f[i] ? cands16(P, tbl, k[i], len[i], &b1[i], &b2[i]) : 0u;
+#pragma unroll
+    for (int i = 0; i < NTOK; i++) slot[i] = m[i] ? cand_slot(m[i], b1[i], b2[i]) : 0xFFFFFFFFu;
+    uint4 r[NTOK];
+#pragma unroll
+    for (int i = 0; i < NTOK; i++) r[i] = m[i] ? __ldg(P.rec_lo + slot[i]) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (int i = 0; i < NTOK; i++)
+        if (m[i] && !key_eq(r[i], k[i])) slot[i] = other_cands16(P, tbl, k[i], len[i]);
+#pragma unroll
+    for (int i = 0; i < NTOK; i++)
+        if (slot[i] != 0xFFFFFFFFu) sink.hit(slot[i]);
+    /* rare: tokens of 17..32 letters take the general lookup; a run of 33+
+     * letters flags the file for the fix-up kernel */
+#pragma unroll
+    for (int i = 0; i < NTOK; i++)
+        if (v[i] && len[i] > 16u) {
+            if (len[i] > 32u) sink.long_run();
+            else {
+                uint32_t kk[8];
+                key32(base, st[i], len[i], kk);
+                lookup_hit(P, tbl, kk, len[i], sink);
+            }
+        }
+}
+
 template <bool SMEM, class Sink>
 __device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, const uint8_t* base, const StageDesc& d,
                                              uint32_t segi, uint8_t* wscr, const uint4* km, Sink& sink) {
@@ -411,45 +461,11 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, c
     uint32_t js = incl - cnt;
     for (uint32_t m = starts; m; m &= m - 1u) slist[js++] = (uint16_t)(off + (uint32_t)(__ffs(m) - 1));
     __syncwarp();
+    /* rounds of two tokens per lane; a last round of at most 32 tokens takes
+     * one per lane (warp-uniform choice) */
     for (uint32_t tb0 = 0; tb0 < n_s; tb0 += 64u) {
-        /* two tokens per lane, straight-line so their loads overlap */
-        const uint32_t t0 = tb0 + (uint32_t)lane, t1 = t0 + 32u;
-        const bool v0 = t0 < n_s, v1 = t1 < n_s;
-        const uint32_t st0 = v0 ? slist[t0] : seg0, st1 = v1 ? slist[t1] : seg0;
-        const uint32_t len0 = v0 ? run_len(bm, st0 - seg0) : 0u, len1 = v1 ? run_len(bm, st1 - seg0) : 0u;
-        const bool f0 = v0 && len0 <= 16u, f1 = v1 && len1 <= 16u;
-        uint32_t k0[4], k1[4];
-        key16(base, st0, f0 ? len0 : 0u, k0, km);
-        key16(base, st1, f1 ? len1 : 0u, k1, km);
-        uint32_t b10, b20, b11, b21;
-        const uint32_t m0 = f0 ? cands16(P, tbl, k0, len0, &b10, &b20) : 0u;
-        const uint32_t m1 = f1 ? cands16(P, tbl, k1, len1, &b11, &b21) : 0u;
-        uint32_t s0 = m0 ? cand_slot(m0, b10, b20) : 0xFFFFFFFFu, s1 = m1 ? cand_slot(m1, b11, b21) : 0xFFFFFFFFu;
-        const uint4 r0 = m0 ? __ldg(P.rec_lo + s0) : make_uint4(0, 0, 0, 0);
-        const uint4 r1 = m1 ? __ldg(P.rec_lo + s1) : make_uint4(0, 0, 0, 0);
-        if (m0 && !key_eq(r0, k0)) s0 = other_cands16(P, tbl, k0, len0);
-        if (m1 && !key_eq(r1, k1)) s1 = other_cands16(P, tbl, k1, len1);
-        if (s0 != 0xFFFFFFFFu) sink.hit(s0);
-        if (s1 != 0xFFFFFFFFu) sink.hit(s1);
-        const bool slow0 = v0 && len0 > 16u, slow1 = v1 && len1 > 16u;
-        /* rare: tokens of 17..32 letters take the general lookup; a run of 33+
-         * letters flags the file for the fix-up kernel */
-        if (slow0) {
-            if (len0 > 32u) sink.long_run();
-            else {
-                uint32_t kk[8];
-                key32(base, st0, len0, kk);
-                lookup_hit(P, tbl, kk, len0, sink);
-            }
-        }
-        if (slow1) {
-            if (len1 > 32u) sink.long_run();
-            else {
-                uint32_t kk[8];
-                key32(base, st1, len1, kk);
-                lookup_hit(P, tbl, kk, len1, sink);
-            }
-        }
+        if (n_s - tb0 > 32u) scan_tokens<2>(P, tbl, base, bm, slist, seg0, tb0, n_s, km, sink);
+        else scan_tokens<1>(P, tbl, base, bm, slist, seg0, tb0, n_s, km, sink);
     }
 }
 
@@ -497,6 +513,15 @@ __device__ void unpin_window(gfs_state* S, Shared& sh, Window& w) {
     const int lane = threadIdx.x & 31;
     if (w.live && (uint32_t)lane < w.n) unpin(S, (uint32_t)sh.frames[w.buf][lane]);
     w.live = false;
+}
+
+__device__ void release_window(gfs_state* S, const GrepDev& P, Shared& sh, Window& prev, uint32_t site) {
+    const int lane = threadIdx.x & 31;
+    if (prev.live) {
+        if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, site);
+        __syncwarp();
+        unpin_window(S, sh, prev);
+    }
 }
 
 /* Stream chunks [k, kend) of file f (chunk size CH) into the stage ring,
@@ -605,15 +630,6 @@ __device__ bool stream_file(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t*
         if (sh.abort) return false;
     }
     return true;
-}
-
-__device__ void release_window(gfs_state* S, const GrepDev& P, Shared& sh, Window& prev, uint32_t site) {
-    const int lane = threadIdx.x & 31;
-    if (prev.live) {
-        if (lane == 0) wait_phase(sh, P, &sh.full[prev.last_g % GR_STAGES], (prev.last_g / GR_STAGES) & 1u, site);
-        __syncwarp();
-        unpin_window(S, sh, prev);
-    }
 }
 
 /* A stage with no bytes (an empty file, or f = -1: the end of a batched
@@ -735,11 +751,90 @@ __device__ void hasher(const GrepDev& P, Shared& sh, uint8_t* stages) {
     }
 }
 
+/* Direct scan: each consumer warp loads the window of its own segment --
+ * the segment, GR_LB bytes before it and GR_LA + 32 after -- into a private
+ * shared buffer and scans it there; no producer, no stage ring.  Bytes come
+ * from the file's registered host mapping (16-byte loads over the host
+ * link, many warps in flight) or, for a file without one, from its pages
+ * in the buffer cache, pinned by lane 0 for the copy.  Bytes outside the
+ * file read as zero.  false: failed (the CTA is aborting). */
+#define GR_DWIN (GR_LB + GR_SEG + GR_LA + 32) /* bytes per warp window (39 x 16) */
+static_assert(GR_DWIN % 16 == 0 && GR_CONS * GR_DWIN <= GR_STAGES * GR_STAGE, "direct windows live in the stage ring");
+__device__ __noinline__ bool load_window(gfs_state* S, const GrepDev& P, Shared& sh, int f, uint64_t p, uint8_t* buf) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t fsize = P.sizes[f];
+    const int64_t first = (int64_t)p - GR_LB; /* file offset of buf[0] */
+    const uint8_t* src = (const uint8_t*)P.maps[f];
+    uint32_t fr0 = 0, fr1 = 0, pg0 = 0;
+    const uint32_t lp = S->log_page;
+    if (!src) {
+        /* pages covering the window's bytes inside the file: at most two */
+        const uint64_t lo = first > 0 ? (uint64_t)first : 0u;
+        const uint64_t hi = first + GR_DWIN < (int64_t)fsize ? (uint64_t)(first + GR_DWIN) : fsize;
+        int e = 0;
+        if (lane == 0 && lo < hi) {
+            const PinFile pf = pin_file(S, P.fds[f]);
+            bool fresh = false;
+            pg0 = (uint32_t)(lo >> lp);
+            const uint32_t pg1 = (uint32_t)((hi - 1u) >> lp);
+            int r0 = pin_page(S, pf, pg0, GFS_PIN_READ, &fresh);
+            int r1 = r0;
+            if (r0 >= 0 && pg1 != pg0) {
+                r1 = pin_page(S, pf, pg1, GFS_PIN_READ, &fresh);
+                if (r1 < 0) unpin(S, (uint32_t)r0);
+            }
+            e = r0 < 0 ? r0 : (r1 < 0 ? r1 : 0);
+            if (e) fail(sh, P, e, 10);
+            fr0 = (uint32_t)r0;
+            fr1 = (uint32_t)r1;
+        }
+        e = __shfl_sync(0xFFFFFFFFu, e, 0);
+        if (e) return false;
+        fr0 = __shfl_sync(0xFFFFFFFFu, fr0, 0);
+        fr1 = __shfl_sync(0xFFFFFFFFu, fr1, 0);
+        pg0 = __shfl_sync(0xFFFFFFFFu, pg0, 0);
+    }
+    for (uint32_t u = lane; u < GR_DWIN / 16u; u += 32u) {
+        const int64_t off = first + 16 * (int64_t)u;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (off >= 0 && off < (int64_t)fsize) {
+            /* 16-byte units never straddle a page (pages are >= 4 KiB) */
+            const uint8_t* q = src ? src + off
+                                   : S->pool + ((size_t)((uint32_t)(off >> lp) == pg0 ? fr0 : fr1) << lp) +
+                                         ((uint64_t)off & ((1ull << lp) - 1u));
+            if (off + 16 <= (int64_t)fsize) {
+                v = *(const uint4*)q;
+            } else {
+                /* the file's last partial unit, byte by byte */
+                uint64_t lo = 0, hi = 0;
+                const int n = (int)((int64_t)fsize - off);
+                for (int i = 0; i < n; i++) {
+                    const uint64_t b = q[i];
+                    if (i < 8) lo |= b << (8 * i);
+                    else hi |= b << (8 * (i - 8));
+                }
+                v = make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+            }
+        }
+        *(uint4*)(buf + 16u * u) = v;
+    }
+    __syncwarp();
+    if (!src && lane == 0 && fsize > 0) {
+        const uint64_t lo = first > 0 ? (uint64_t)first : 0u;
+        const uint64_t hi = first + GR_DWIN < (int64_t)fsize ? (uint64_t)(first + GR_DWIN) : fsize;
+        if (lo < hi) {
+            unpin(S, fr0);
+            if ((uint32_t)((hi - 1u) >> lp) != pg0) unpin(S, fr1);
+        }
+    }
+    return true;
+}
+
 /* One persistent 1024-thread CTA per SM: warp 31 pins pages and streams
  * chunks (TMA), warps 0..30 scan them; see the file comment.  BATCH: the
  * CTA takes whole files from a shared queue instead of a static run of
  * chunks, warps 0..29 scan and warp 30 computes each file's XXH64. */
-template <bool SMEM, bool BATCH>
+template <bool SMEM, bool BATCH, bool DIRECT>
 __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepDev P) {
     constexpr int NC = BATCH ? GR_CONS_B : GR_CONS;
     constexpr uint32_t CH = (uint32_t)NC * GR_SEG;
@@ -826,7 +921,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
     const uint64_t total = P.total_chunks;
     const uint64_t c0 = total * blockIdx.x / gridDim.x, c1 = total * (blockIdx.x + 1) / gridDim.x;
     if (warp == GR_CONS) {
-        producer(S, P, sh, stages, c0, c1);
+        if (!DIRECT) producer(S, P, sh, stages, c0, c1);
         return;
     }
     /* Items (chunk, segment) are taken in order from a shared counter, so a
@@ -854,6 +949,26 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
             if (fend >= nchunks) return;
             f = file_of(P, c0 + fend);
             fend = (uint32_t)((P.chunk_prefix[f + 1] < c1 ? P.chunk_prefix[f + 1] : c1) - c0);
+        }
+        if (DIRECT) {
+            /* chunk c0 + g lies in file f (the loop above moved f on) */
+            StageDesc d;
+            d.f = f;
+            d.fseq = 0;
+            d.pos = (c0 + g - P.chunk_prefix[f]) * GR_CH;
+            const uint64_t rem = P.sizes[f] - d.pos;
+            d.clen = (uint32_t)(rem < GR_CH ? rem : GR_CH);
+            d.avail = (uint32_t)(rem < (uint64_t)GR_CH + GR_LA ? rem : (uint64_t)GR_CH + GR_LA);
+            const uint32_t seg0 = (it % NC) * GR_SEG;
+            if (seg0 < d.clen && !sh.abort) {
+                uint8_t* buf = stages + (size_t)warp * GR_DWIN;
+                if (load_window(S, P, sh, f, d.pos + seg0, buf)) {
+                    CountSink sink{P, tbl, SMEM, f};
+                    scan_segment<SMEM>(P, tbl, buf + GR_LB - seg0, d, it % NC, wscr, sh.kmask, sink);
+                }
+            }
+            __syncwarp();
+            continue;
         }
         const uint32_t s = g % GR_STAGES;
         bool ok = true;
@@ -960,10 +1075,12 @@ __global__ void k_grep_fixup(gfs_state* S, GrepDev P) {
     pc.release();
 }
 
-template __global__ void k_grep_scan<true, false>(gfs_state*, GrepDev);
-template __global__ void k_grep_scan<false, false>(gfs_state*, GrepDev);
-template __global__ void k_grep_scan<true, true>(gfs_state*, GrepDev);
-template __global__ void k_grep_scan<false, true>(gfs_state*, GrepDev);
+template __global__ void k_grep_scan<true, false, false>(gfs_state*, GrepDev);
+template __global__ void k_grep_scan<false, false, false>(gfs_state*, GrepDev);
+template __global__ void k_grep_scan<true, true, false>(gfs_state*, GrepDev);
+template __global__ void k_grep_scan<false, true, false>(gfs_state*, GrepDev);
+template __global__ void k_grep_scan<true, false, true>(gfs_state*, GrepDev);
+template __global__ void k_grep_scan<false, false, true>(gfs_state*, GrepDev);
 
 /* ------------------------------------------------------------------ */
 /* host side: dictionary table, file opening, launch                   */
@@ -1314,81 +1431,91 @@ static __global__ void k_close_files(const int* fds, int n, int* rcs) {
 
 namespace {
 
-struct HostTable {
-    uint32_t nb = 0;
-    std::vector<uint16_t> tags;      /* nb*4 slot tags */
-    std::vector<uint32_t> recs;      /* nb*4*8 */
-    std::vector<uint32_t> slot_word; /* nb*4 */
-    std::vector<int32_t> next_dup;   /* n_words */
-};
+static_assert(__BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__, "record keys are little-endian words, as on the device");
 
+/* Key words of a 32-byte record (bytes up to its first NUL, zero padded). */
 void rec_key(const uint8_t* rec, uint32_t k[8], int* len) {
-    int l = 0;
-    while (l < 32 && rec[l]) l++;
-    uint8_t b[32] = {0};
-    memcpy(b, rec, (size_t)l);
-    for (int i = 0; i < 8; i++)
-        k[i] = (uint32_t)b[4 * i] | ((uint32_t)b[4 * i + 1] << 8) | ((uint32_t)b[4 * i + 2] << 16) |
-               ((uint32_t)b[4 * i + 3] << 24);
+    const void* z = memchr(rec, 0, 32);
+    const int l = z ? (int)((const uint8_t*)z - rec) : 32;
+    memset(k, 0, 32);
+    memcpy(k, rec, (size_t)l);
     *len = l;
 }
 
-/* Load 0.92: the table lives in shared memory, and the less of the SM's
- * combined L1/shared storage it takes, the more L1 is left to cache the
- * records the scan verifies candidates against (measured: lower loads were
- * slower).  16-bit tags keep false candidates rare at this load. */
-bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
-    const size_t nw = n_words > 0 ? (size_t)n_words : 1u;
+/* Host workspace of table builds, kept across plans so a build touches no
+ * freshly mapped memory; one build at a time. */
+struct BuildWs {
     struct Key {
         uint32_t k[8];
         uint32_t h1;
         int len;
     };
-    std::vector<Key> key(nw);
-    std::vector<int> uniq, last(nw, -1);
-    uniq.reserve(nw);
-    T.next_dup.assign(nw, -1);
+    std::mutex mu;
+    std::vector<uint8_t> dict;
+    std::vector<Key> key;
+    std::vector<int> uniq, last, seen, slot_of;
+    std::vector<uint32_t> ba, bb;
+    std::vector<int32_t> next_dup;
+    uint32_t nb = 0;
+};
+BuildWs g_ws;
+
+/* Load 0.92: the table lives in shared memory, and the less of the SM's
+ * combined L1/shared storage it takes, the more L1 is left to cache the
+ * records the scan verifies candidates against (measured: lower loads were
+ * slower).  16-bit tags keep false candidates rare at this load.  Result in
+ * W: nb, slot_of (slot -> first record of its word, -1 empty), next_dup. */
+bool build_table(const uint8_t* dict, int n_words, BuildWs& W) {
+    const size_t nw = n_words > 0 ? (size_t)n_words : 1u;
+    auto& key = W.key;
+    key.resize(nw);
+    W.uniq.clear();
+    W.uniq.reserve(nw);
+    W.last.assign(nw, -1);
+    W.next_dup.assign(nw, -1);
     /* duplicates: open addressing on the word hash, exact key compare */
     size_t cap = 16;
     while (cap < 2 * nw) cap <<= 1;
-    std::vector<int> seen(cap, -1);
+    W.seen.assign(cap, -1);
     for (int w = 0; w < n_words; w++) {
-        Key& kw = key[(size_t)w];
+        BuildWs::Key& kw = key[(size_t)w];
         rec_key(dict + (size_t)w * 32, kw.k, &kw.len);
         if (kw.len == 0) continue;
         kw.h1 = grep_h1(grep_mix(kw.k, kw.len));
         for (size_t i = kw.h1 & (cap - 1);; i = (i + 1) & (cap - 1)) {
-            const int u = seen[i];
+            const int u = W.seen[i];
             if (u < 0) {
-                seen[i] = w;
-                uniq.push_back(w);
-                last[(size_t)w] = w;
+                W.seen[i] = w;
+                W.uniq.push_back(w);
+                W.last[(size_t)w] = w;
                 break;
             }
-            const Key& ku = key[(size_t)u];
+            const BuildWs::Key& ku = key[(size_t)u];
             if (ku.h1 == kw.h1 && ku.len == kw.len && memcmp(ku.k, kw.k, sizeof kw.k) == 0) {
-                T.next_dup[(size_t)last[(size_t)u]] = w;
-                last[(size_t)u] = w;
+                W.next_dup[(size_t)W.last[(size_t)u]] = w;
+                W.last[(size_t)u] = w;
                 break;
             }
         }
     }
     /* bucketised cuckoo placement (2 choices x 4 slots), random-walk kicks */
-    std::vector<uint32_t> ba(nw), bb(nw);
-    uint32_t nb = (uint32_t)((double)uniq.size() / (GREP_WAYS * 0.92)) + 16u;
+    W.ba.resize(nw);
+    W.bb.resize(nw);
+    uint32_t nb = (uint32_t)((double)W.uniq.size() / (GREP_WAYS * 0.92)) + 16u;
     for (int attempt = 0; attempt < 20; attempt++, nb = nb + nb / 8u + 1u) {
-        for (int w : uniq) {
-            ba[(size_t)w] = grep_bucket(key[(size_t)w].h1, nb);
-            bb[(size_t)w] = grep_b2(key[(size_t)w].h1, nb);
+        for (int w : W.uniq) {
+            W.ba[(size_t)w] = grep_bucket(key[(size_t)w].h1, nb);
+            W.bb[(size_t)w] = grep_b2(key[(size_t)w].h1, nb);
         }
-        std::vector<int> slot_of((size_t)nb * GREP_WAYS, -1);
+        auto& slot_of = W.slot_of;
+        slot_of.assign((size_t)nb * GREP_WAYS, -1);
         uint64_t rng = 0x243F6A8885A308D3ULL ^ nb;
         bool ok = true;
-        for (int w : uniq) {
+        for (int w : W.uniq) {
             int cur = w;
             int kicks = 0;
             for (;;) {
-                const uint32_t b[2] = {ba[(size_t)cur], bb[(size_t)cur]};
+                const uint32_t b[2] = {W.ba[(size_t)cur], W.bb[(size_t)cur]};
                 /* the emptier of the two buckets (fewer kicks near full load) */
                 int placed = -1, best_free = 0;
                 for (int r = 0; r < 2; r++) {
@@ -1414,18 +1541,7 @@ bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
             if (!ok) break;
         }
         if (!ok) continue;
-        T.nb = nb;
-        T.tags.assign((size_t)nb * GREP_WAYS, 0u);
-        T.recs.assign((size_t)nb * GREP_WAYS * 8, 0u);
-        T.slot_word.assign((size_t)nb * GREP_WAYS, 0xFFFFFFFFu);
-        for (uint32_t sl = 0; sl < nb * GREP_WAYS; sl++) {
-            const int w = slot_of[sl];
-            if (w < 0) continue;
-            const Key& kw = key[(size_t)w];
-            T.tags[sl] = (uint16_t)grep_tag(kw.h1, kw.len);
-            memcpy(&T.recs[(size_t)sl * 8], kw.k, 32);
-            T.slot_word[sl] = (uint32_t)w;
-        }
+        W.nb = nb;
         return true;
     }
     return false;
@@ -1436,7 +1552,7 @@ bool build_table(const uint8_t* dict, int n_words, HostTable& T) {
 struct gfs_grep {
     gfs_ctx* ctx = nullptr;
     int n_files = 0, n_words = 0;
-    HostTable T;
+    uint32_t nb = 0; /* table buckets */
     GrepDev dev{};
     void* dmem = nullptr; /* one allocation for everything */
     std::vector<uint64_t> sizes;
@@ -1444,6 +1560,7 @@ struct gfs_grep {
     size_t smem_bytes = 0;
     int sms = 0;
     uint32_t last_status[2] = {0, 0};
+    long long build_us = 0, open_us = 0; /* host time of the table build / of opening the files */
     /* batched run: captured once per grid size, replayed */
     cudaGraphExec_t batch_graph = nullptr;
     int batch_ctas = 0;
@@ -1459,14 +1576,22 @@ static void set_window(gfs_grep* g, int n_ctas) {
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+static uint64_t host_us() {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (uint64_t)ts.tv_sec * 1000000ull + (uint64_t)ts.tv_nsec / 1000ull;
+}
+
 extern "C" {
 
 void gfs__preload_grep() {
     cudaFuncAttributes a;
-    cudaFuncGetAttributes(&a, k_grep_scan<true, false>);
-    cudaFuncGetAttributes(&a, k_grep_scan<false, false>);
-    cudaFuncGetAttributes(&a, k_grep_scan<true, true>);
-    cudaFuncGetAttributes(&a, k_grep_scan<false, true>);
+    cudaFuncGetAttributes(&a, k_grep_scan<true, false, false>);
+    cudaFuncGetAttributes(&a, k_grep_scan<false, false, false>);
+    cudaFuncGetAttributes(&a, k_grep_scan<true, true, false>);
+    cudaFuncGetAttributes(&a, k_grep_scan<false, true, false>);
+    cudaFuncGetAttributes(&a, k_grep_scan<true, false, true>);
+    cudaFuncGetAttributes(&a, k_grep_scan<false, false, true>);
     cudaFuncGetAttributes(&a, k_serve);
     cudaFuncGetAttributes(&a, k_grep_fixup);
     cudaFuncGetAttributes(&a, k_open_files);
@@ -1479,14 +1604,17 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     for (int i = 0; i < n_files; i++)
         if (!paths[i] || strlen(paths[i]) >= GFS_NAME_MAX) return -GFS_EINVAL;
     if (gfs__activate(ctx)) return -GFS_EIO;
+    BuildWs& W = g_ws;
+    std::unique_lock<std::mutex> lk(W.mu);
     int fd = open(dict_path, O_RDONLY | O_CLOEXEC);
     if (fd < 0) return -errno;
     struct stat st;
-    if (fstat(fd, &st) != 0) { close(fd); return -errno; }
-    std::vector<uint8_t> dict((size_t)st.st_size + 32, 0);
+    if (fstat(fd, &st) != 0) { const int e = errno; close(fd); return -e; }
+    W.dict.resize((size_t)st.st_size + 32);
+    memset(W.dict.data() + st.st_size, 0, 32);
     ssize_t got = 0;
     while (got < st.st_size) {
-        ssize_t r = pread(fd, dict.data() + got, (size_t)(st.st_size - got), got);
+        ssize_t r = pread(fd, W.dict.data() + got, (size_t)(st.st_size - got), got);
         if (r <= 0) break;
         got += r;
     }
@@ -1500,34 +1628,57 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     const size_t fixed = (size_t)GR_STAGES * GR_STAGE + (size_t)GR_CONS * GR_WSCR + 256;
-    if (!build_table(dict.data(), g->n_words, g->T)) { delete g; return -GFS_ENOMEM; }
-    const uint32_t nb = g->T.nb;
-    /* device layout */
-    size_t o_tbl = 0, o_recs = align_up(o_tbl + (size_t)nb * 8, 256), o_sw = align_up(o_recs + (size_t)nb * 4 * 32, 256),
-           o_nd = align_up(o_sw + (size_t)nb * 16, 256), o_cnt = align_up(o_nd + (size_t)g->n_words * 4 + 4, 256),
+    const uint64_t t_build = host_us();
+    if (!build_table(W.dict.data(), g->n_words, W)) { delete g; return -GFS_ENOMEM; }
+    g->build_us = (long long)(host_us() - t_build);
+    const uint32_t nb = W.nb;
+    g->nb = nb;
+    const size_t ns = (size_t)nb * 4; /* slots */
+    /* device layout: the table image and the file names first (uploaded in
+     * one copy), then what the device fills or the host adds later */
+    size_t o_tbl = 0, o_recs = align_up(o_tbl + (size_t)nb * 8, 256), o_sw = align_up(o_recs + ns * 32, 256),
+           o_nd = align_up(o_sw + ns * 4, 256), o_names = align_up(o_nd + (size_t)g->n_words * 4 + 4, 256),
+           o_cnt = align_up(o_names + (size_t)n_files * GFS_NAME_MAX, 256),
            o_fds = align_up(o_cnt + (size_t)g->n_words * n_files * 4 + 4, 256), o_sz = align_up(o_fds + (size_t)n_files * 4, 256),
            o_pf = align_up(o_sz + (size_t)n_files * 8, 256), o_fl = align_up(o_pf + (size_t)(n_files + 1) * 8, 256),
-           o_st = align_up(o_fl + (size_t)n_files * 4, 256), o_names = align_up(o_st + 64, 256),
-           o_fo = align_up(o_names + (size_t)n_files * GFS_NAME_MAX, 256), o_fn = align_up(o_fo + (size_t)n_files * 4, 256),
-           o_xxh = align_up(o_fn + 64, 256), total = align_up(o_xxh + (size_t)n_files * 8, 256);
-    if (cudaMalloc(&g->dmem, total) != cudaSuccess) { delete g; return -GFS_ENOMEM; }
-    uint8_t* b = (uint8_t*)g->dmem;
-    cudaMemset(b, 0, total);
-    cudaMemcpy(b + o_tbl, g->T.tags.data(), (size_t)nb * 8, cudaMemcpyHostToDevice);
-    {
-        const size_t ns = (size_t)nb * 4;
-        std::vector<uint32_t> lohi(ns * 8);
-        for (size_t i = 0; i < ns; i++) {
-            memcpy(&lohi[i * 4], &g->T.recs[i * 8], 16);
-            memcpy(&lohi[(ns + i) * 4], &g->T.recs[i * 8 + 4], 16);
-        }
-        cudaMemcpy(b + o_recs, lohi.data(), ns * 32, cudaMemcpyHostToDevice);
+           o_st = align_up(o_fl + (size_t)n_files * 4, 256), o_fo = align_up(o_st + 64, 256),
+           o_fn = align_up(o_fo + (size_t)n_files * 4, 256), o_xxh = align_up(o_fn + 64, 256),
+           o_maps = align_up(o_xxh + (size_t)n_files * 8, 256), total = align_up(o_maps + (size_t)n_files * 8, 256);
+    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
+    g->dmem = gfs__dev_alloc(ctx, total, s);
+    uint8_t* hb = (uint8_t*)gfs__host_bounce(ctx, o_cnt);
+    if (!g->dmem || !hb) {
+        gfs__dev_free(ctx, g->dmem, s);
+        delete g;
+        return -GFS_ENOMEM;
     }
-    cudaMemcpy(b + o_sw, g->T.slot_word.data(), (size_t)nb * 16, cudaMemcpyHostToDevice);
-    if (g->n_words) cudaMemcpy(b + o_nd, g->T.next_dup.data(), (size_t)g->n_words * 4, cudaMemcpyHostToDevice);
-    std::vector<char> names((size_t)n_files * GFS_NAME_MAX, 0);
-    for (int i = 0; i < n_files; i++) memcpy(&names[(size_t)i * GFS_NAME_MAX], paths[i], strlen(paths[i]));
-    cudaMemcpy(b + o_names, names.data(), names.size(), cudaMemcpyHostToDevice);
+    uint8_t* b = (uint8_t*)g->dmem;
+    cudaMemsetAsync(b + o_cnt, 0, total - o_cnt, s);
+    {
+        /* the table image: slot tags, record bytes 0..15 of every slot, then
+         * bytes 16..31, first record of each slot, duplicate chains; names */
+        memset(hb, 0, o_cnt);
+        uint16_t* tags = (uint16_t*)(hb + o_tbl);
+        uint32_t* lo = (uint32_t*)(hb + o_recs);
+        uint32_t* hi = lo + ns * 4;
+        uint32_t* sw = (uint32_t*)(hb + o_sw);
+        for (size_t sl = 0; sl < ns; sl++) {
+            const int w = W.slot_of[sl];
+            if (w < 0) {
+                sw[sl] = 0xFFFFFFFFu;
+                continue;
+            }
+            const BuildWs::Key& kw = W.key[(size_t)w];
+            tags[sl] = (uint16_t)grep_tag(kw.h1, kw.len);
+            memcpy(lo + sl * 4, kw.k, 16);
+            memcpy(hi + sl * 4, kw.k + 4, 16);
+            sw[sl] = (uint32_t)w;
+        }
+        if (g->n_words) memcpy(hb + o_nd, W.next_dup.data(), (size_t)g->n_words * 4);
+        for (int i = 0; i < n_files; i++) memcpy(hb + o_names + (size_t)i * GFS_NAME_MAX, paths[i], strlen(paths[i]));
+        cudaMemcpyAsync(b, hb, o_cnt, cudaMemcpyHostToDevice, s);
+    }
+    lk.unlock();
     GrepDev& d = g->dev;
     d.n_files = n_files;
     d.n_words = g->n_words;
@@ -1546,63 +1697,86 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     d.file_order = (const int*)(b + o_fo);
     d.file_next = (uint32_t*)(b + o_fn);
     d.xxh = (unsigned long long*)(b + o_xxh);
-    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
+    d.maps = (const uint64_t*)(b + o_maps);
+    const uint64_t t_open = host_us();
     k_open_files<<<n_files, 128, 0, s>>>((const char*)(b + o_names), n_files, (int*)d.fds, (uint64_t*)d.sizes);
+    /* slots and sizes back through the pinned buffer (the image copy before
+     * the kernel on this stream is done with it by then) */
+    int* fds = (int*)hb;
+    uint64_t* szs = (uint64_t*)(hb + align_up((size_t)n_files * 4, 64));
+    cudaMemcpyAsync(fds, d.fds, (size_t)n_files * 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(szs, d.sizes, (size_t)n_files * 8, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) { gfs_grep_close(g); return -GFS_EIO; }
-    std::vector<int> fds((size_t)n_files);
-    g->sizes.resize((size_t)n_files);
-    cudaMemcpy(fds.data(), d.fds, (size_t)n_files * 4, cudaMemcpyDeviceToHost);
-    cudaMemcpy(g->sizes.data(), d.sizes, (size_t)n_files * 8, cudaMemcpyDeviceToHost);
+    g->open_us = (long long)(host_us() - t_open);
+    g->sizes.assign(szs, szs + n_files);
     for (int i = 0; i < n_files; i++)
-        if (fds[(size_t)i] < 0) {
-            int e = fds[(size_t)i];
+        if (fds[i] < 0) {
+            int e = fds[i];
             gfs_grep_close(g);
             return e;
         }
-    std::vector<uint64_t> pf((size_t)n_files + 1, 0);
-    for (int i = 0; i < n_files; i++) pf[(size_t)i + 1] = pf[(size_t)i] + (g->sizes[(size_t)i] + GR_CH - 1) / GR_CH;
-    cudaMemcpy((void*)d.chunk_prefix, pf.data(), pf.size() * 8, cudaMemcpyHostToDevice);
-    d.total_chunks = pf[(size_t)n_files];
     {
-        /* batched runs take files longest first (LPT: the largest file
-         * bounds the run, so it starts first) */
-        std::vector<int> order((size_t)n_files);
-        for (int i = 0; i < n_files; i++) order[(size_t)i] = i;
-        std::stable_sort(order.begin(), order.end(),
-                         [&](int x, int y) { return g->sizes[(size_t)x] > g->sizes[(size_t)y]; });
-        cudaMemcpy((void*)d.file_order, order.data(), order.size() * 4, cudaMemcpyHostToDevice);
+        /* per file: its host mapping's device address (direct scans read
+         * it), chunk prefix sums, and the longest-first order of batched
+         * runs (LPT: the largest file bounds the run, so it starts first);
+         * staged in the pinned buffer after the slots, one copy each */
+        uint64_t* maps = (uint64_t*)(hb + align_up((size_t)n_files * 4, 64));
+        uint64_t* pf = maps + align_up((size_t)n_files, 8);
+        int* order = (int*)(pf + align_up((size_t)n_files + 1, 8));
+        for (int i = 0; i < n_files; i++) {
+            unsigned long long a = 0, len = 0;
+            maps[i] = gfs__slot_map(ctx, (uint32_t)fds[i], &a, &len) > 0 && len >= g->sizes[(size_t)i] ? a : 0u;
+        }
+        pf[0] = 0;
+        for (int i = 0; i < n_files; i++) pf[i + 1] = pf[i] + (g->sizes[(size_t)i] + GR_CH - 1) / GR_CH;
+        d.total_chunks = pf[n_files];
+        for (int i = 0; i < n_files; i++) order[i] = i;
+        std::stable_sort(order, order + n_files, [&](int x, int y) { return g->sizes[(size_t)x] > g->sizes[(size_t)y]; });
+        cudaMemcpyAsync((void*)d.maps, maps, (size_t)n_files * 8, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync((void*)d.chunk_prefix, pf, ((size_t)n_files + 1) * 8, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync((void*)d.file_order, order, (size_t)n_files * 4, cudaMemcpyHostToDevice, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) { gfs_grep_close(g); return -GFS_EIO; }
     }
     /* shared memory: table (if it fits) + stages + token lists + scratch */
     g->sms = sms;
     size_t with_tbl = align_up((size_t)nb * 8, 128) + align_up((size_t)nb * 16, 128) + fixed;
     g->smem = with_tbl <= (size_t)maxsm;
     g->smem_bytes = g->smem ? with_tbl : fixed;
-    cudaFuncSetAttribute(k_grep_scan<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
-    cudaFuncSetAttribute(k_grep_scan<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
-    cudaFuncSetAttribute(k_grep_scan<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
-    cudaFuncSetAttribute(k_grep_scan<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
+    cudaFuncSetAttribute(k_grep_scan<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
+    cudaFuncSetAttribute(k_grep_scan<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
+    cudaFuncSetAttribute(k_grep_scan<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
+    cudaFuncSetAttribute(k_grep_scan<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
+    cudaFuncSetAttribute(k_grep_scan<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
+    cudaFuncSetAttribute(k_grep_scan<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
     *out = g;
     return 0;
 }
 
-int gfs_grep_run(gfs_grep* g, int n_ctas, float* kernel_ms) {
+static int grep_run(gfs_grep* g, int n_ctas, float* kernel_ms, int direct) {
     if (!g) return -GFS_EINVAL;
     if (gfs__activate(g->ctx)) return -GFS_EIO;
     cudaStream_t s = (cudaStream_t)gfs_kernel_stream(g->ctx);
-    GrepDev& d = g->dev;
+    GrepDev d = g->dev;
     cudaMemsetAsync(d.counts, 0, (size_t)g->n_words * g->n_files * 4, s);
     cudaMemsetAsync(d.long_flags, 0, (size_t)g->n_files * 4, s);
     cudaMemsetAsync(d.status, 0, 8, s);
     if (n_ctas <= 0) n_ctas = g->sms;
     set_window(g, n_ctas);
+    d.win_pages = g->dev.win_pages;
     cudaEvent_t a, b;
     if (kernel_ms) {
         cudaEventCreate(&a);
         cudaEventCreate(&b);
         cudaEventRecord(a, s);
     }
-    if (g->smem) k_grep_scan<true, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
-    else k_grep_scan<false, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
+    gfs_state* S = (gfs_state*)gfs_device_state(g->ctx);
+    if (direct) {
+        if (g->smem) k_grep_scan<true, false, true><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+        else k_grep_scan<false, false, true><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+    } else {
+        if (g->smem) k_grep_scan<true, false, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+        else k_grep_scan<false, false, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+    }
     cudaError_t le = cudaGetLastError();
     k_grep_fixup<<<g->n_files, 32, 0, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
     if (kernel_ms) {
@@ -1624,6 +1798,10 @@ int gfs_grep_run(gfs_grep* g, int n_ctas, float* kernel_ms) {
     return status[0] ? -((status[0] & GFS_ERRB_TIMEOUT) ? GFS_ETIMEDOUT : GFS_EIO) : 0;
 }
 
+int gfs_grep_run(gfs_grep* g, int n_ctas, float* kernel_ms) { return grep_run(g, n_ctas, kernel_ms, 0); }
+
+int gfs_grep_run_direct(gfs_grep* g, int n_ctas, float* kernel_ms) { return grep_run(g, n_ctas, kernel_ms, 1); }
+
 /* `steps` back-to-back runs on the kernel stream without host round trips;
  * *total_ms: events around all of them; *scan_ms: mean duration of the scan
  * kernel alone (events bracketing each launch on the same stream). */
@@ -1643,8 +1821,8 @@ int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* s
         cudaMemsetAsync(d.counts, 0, (size_t)g->n_words * g->n_files * 4, s);
         cudaMemsetAsync(d.long_flags, 0, (size_t)g->n_files * 4, s);
         cudaEventRecord(ev[2 + 2 * (size_t)i], s);
-        if (g->smem) k_grep_scan<true, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
-        else k_grep_scan<false, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+        if (g->smem) k_grep_scan<true, false, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+        else k_grep_scan<false, false, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
         cudaEventRecord(ev[3 + 2 * (size_t)i], s);
         k_grep_fixup<<<g->n_files, 32, 0, s>>>(S, d);
     }
@@ -1690,8 +1868,8 @@ int gfs_grep_batch(gfs_grep* g, int n_ctas, unsigned long long* host_xxh, float*
         cudaMemsetAsync(d.long_flags, 0, (size_t)g->n_files * 4, s);
         cudaMemsetAsync(d.status, 0, 8, s);
         cudaMemsetAsync(d.file_next, 0, 4, s);
-        if (g->smem) k_grep_scan<true, true><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
-        else k_grep_scan<false, true><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+        if (g->smem) k_grep_scan<true, true, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
+        else k_grep_scan<false, true, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
         k_grep_fixup<<<g->n_files, 32, 0, s>>>(S, d);
         cudaError_t ce = cudaStreamEndCapture(s, &graph);
         if (ce != cudaSuccess || !graph) return -GFS_EIO;
@@ -1728,17 +1906,31 @@ int gfs_grep_batch(gfs_grep* g, int n_ctas, unsigned long long* host_xxh, float*
 int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts) {
     if (!g) return -GFS_EINVAL;
     cudaStream_t s = (cudaStream_t)gfs_kernel_stream(g->ctx);
+    const size_t bytes = (size_t)g->n_words * g->n_files * 4;
+    /* through the session's pinned buffer, at most 16 MiB at a time: DMA at
+     * link speed, then a host copy (a pageable copy is staged by the driver
+     * and much slower) */
+    const size_t piece = bytes < ((size_t)16 << 20) ? bytes : ((size_t)16 << 20);
+    void* hb = gfs__host_bounce(g->ctx, piece);
+    if (hb) {
+        for (size_t off = 0; off < bytes; off += piece) {
+            const size_t n = bytes - off < piece ? bytes - off : piece;
+            if (cudaMemcpyAsync(hb, (const uint8_t*)g->dev.counts + off, n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess)
+                return -GFS_EIO;
+            memcpy((uint8_t*)host_counts + off, hb, n);
+        }
+        return 0;
+    }
     if (cudaStreamSynchronize(s) != cudaSuccess) return -GFS_EIO;
-    return cudaMemcpy(host_counts, g->dev.counts, (size_t)g->n_words * g->n_files * 4, cudaMemcpyDeviceToHost) ==
-                   cudaSuccess
-               ? 0
-               : -GFS_EIO;
+    return cudaMemcpy(host_counts, g->dev.counts, bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? 0 : -GFS_EIO;
 }
 
 int gfs_grep_info(gfs_grep* g, long long* out, int n) {
-    long long v[8] = {g->n_words, g->n_files, (long long)g->T.nb, g->smem ? 1 : 0, (long long)g->smem_bytes,
-                      (long long)g->dev.total_chunks, (long long)g->last_status[0], (long long)g->last_status[1]};
-    int k = n < 8 ? n : 8;
+    long long v[10] = {g->n_words, g->n_files, (long long)g->nb, g->smem ? 1 : 0, (long long)g->smem_bytes,
+                       (long long)g->dev.total_chunks, (long long)g->last_status[0], (long long)g->last_status[1],
+                       g->build_us, g->open_us};
+    int k = n < 10 ? n : 10;
     for (int i = 0; i < k; i++) out[i] = v[i];
     return k;
 }
@@ -1751,19 +1943,19 @@ int gfs_grep_close(gfs_grep* g) {
     if (g->dmem && g->dev.fds) {
         gfs__activate(g->ctx);
         cudaStream_t s = (cudaStream_t)gfs_kernel_stream(g->ctx);
-        int* rcs = nullptr;
-        if (cudaMalloc(&rcs, (size_t)g->n_files * 4) == cudaSuccess) {
+        int* rcs = (int*)gfs__dev_alloc(g->ctx, (size_t)g->n_files * 4, s);
+        int* h = (int*)gfs__host_bounce(g->ctx, (size_t)g->n_files * 4);
+        if (rcs && h) {
             k_close_files<<<g->n_files, 128, 0, s>>>(g->dev.fds, g->n_files, rcs);
+            cudaMemcpyAsync(h, rcs, (size_t)g->n_files * 4, cudaMemcpyDeviceToHost, s);
             cudaStreamSynchronize(s);
-            std::vector<int> h((size_t)g->n_files);
-            cudaMemcpy(h.data(), rcs, h.size() * 4, cudaMemcpyDeviceToHost);
-            for (int x : h)
-                if (x < 0 && !rc) rc = x;
-            cudaFree(rcs);
+            for (int i = 0; i < g->n_files; i++)
+                if (h[i] < 0 && !rc) rc = h[i];
         }
+        gfs__dev_free(g->ctx, rcs, s);
     }
     if (g->batch_graph) cudaGraphExecDestroy(g->batch_graph);
-    cudaFree(g->dmem);
+    gfs__dev_free(g->ctx, g->dmem, (cudaStream_t)gfs_kernel_stream(g->ctx));
     delete g;
     return rc;
 }
@@ -1993,7 +2185,7 @@ int gfs_grep_text(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     gfs_grep* g = nullptr;
     int rc = gfs_grep_open(ctx, dict_path, paths, n_files, &g);
     if (rc) return rc;
-    rc = gfs_grep_run(g, n_ctas, nullptr);
+    rc = gfs_grep_run_direct(g, n_ctas, nullptr); /* one pass: read straight from the files' mappings */
     if (!rc) rc = gfs_grep_counts(g, host_counts);
     int c = gfs_grep_close(g);
     return rc ? rc : c;

@@ -159,6 +159,7 @@ struct FileMap {
     uint64_t dev = 0, ino = 0, size = 0;
     int64_t ctime_ns = 0;
     uint8_t* base = nullptr;
+    uint64_t dev_addr = 0; /* the same bytes, addressed from the device */
     size_t len = 0;
     int refs = 0;      /* open host fds using it */
     uint64_t last = 0; /* LRU stamp */
@@ -179,6 +180,9 @@ struct gfs_ctx {
     std::atomic<unsigned long long> h_reads{0}, h_read_bytes{0}, h_writes{0}, h_write_bytes{0}, h_opens{0},
         h_errors{0}, h_requests{0};
     char* d_scratch = nullptr; /* small device scratch for names/results of C-ABI calls */
+    void* h_bounce = nullptr;  /* pinned host buffer for results copied back to callers' memory */
+    size_t h_bounce_cap = 0;
+    cudaMemPool_t mem_pool = nullptr; /* stream-ordered device memory of per-call objects (plans, servers) */
     /* driver entry point, resolved through the runtime so the library does
      * not link libcuda directly (it loads on machines without a driver) */
     uint8_t* hmap = nullptr;   /* mapped block: completion words + open replies (host view) */
@@ -350,12 +354,21 @@ static FileMap* map_attach(gfs_ctx* c, int fd, const struct stat& st) {
     }
     void* p = mmap(nullptr, len, PROT_READ, MAP_SHARED | MAP_POPULATE, fd, 0);
     if (p == MAP_FAILED) return nullptr;
-    if (cudaHostRegister(p, len, cudaHostRegisterDefault) != cudaSuccess) {
+    /* mapped for the device too: direct scans read it with SM loads */
+    bool reg = cudaHostRegister(p, len, cudaHostRegisterMapped | cudaHostRegisterReadOnly) == cudaSuccess;
+    if (!reg) {
         cudaGetLastError();
+        reg = cudaHostRegister(p, len, cudaHostRegisterMapped) == cudaSuccess;
+    }
+    void* dp = nullptr;
+    if (!reg || cudaHostGetDevicePointer(&dp, p, 0) != cudaSuccess) {
+        cudaGetLastError();
+        if (reg) cudaHostUnregister(p);
         munmap(p, len);
         return nullptr;
     }
     FileMap* m = new FileMap();
+    m->dev_addr = (uint64_t)(uintptr_t)dp;
     m->dev = (uint64_t)st.st_dev;
     m->ino = (uint64_t)st.st_ino;
     m->size = (uint64_t)len;
@@ -814,6 +827,22 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
         CK(cudaMemcpyToSymbol(g_gfs, &c->ds, sizeof(gfs_state*)));
         g_current = c;
         CK(cudaStreamCreateWithFlags(&c->kstream, cudaStreamNonBlocking));
+        {
+            /* the session's own pool, kept warm (nothing returned to the
+             * driver at synchronisation points) */
+            cudaMemPoolProps pp = {};
+            pp.allocType = cudaMemAllocationTypePinned;
+            pp.handleTypes = cudaMemHandleTypeNone;
+            pp.location.type = cudaMemLocationTypeDevice;
+            pp.location.id = cfg.device;
+            if (cudaMemPoolCreate(&c->mem_pool, &pp) == cudaSuccess) {
+                uint64_t keep = ~0ull;
+                cudaMemPoolSetAttribute(c->mem_pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            } else {
+                cudaGetLastError();
+                c->mem_pool = nullptr;
+            }
+        }
         c->d_scratch_cap = 1 << 20;
         CK(cudaMalloc(&c->d_scratch, c->d_scratch_cap));
         CK(cudaDeviceSynchronize());
@@ -861,6 +890,13 @@ int gfs_destroy(gfs_ctx* c) {
             if (c->slots[i].fd >= 0) close(c->slots[i].fd);
     for (auto& e : c->maps) map_release(e.second);
     c->maps.clear();
+    if (c->h_bounce) cudaFreeHost(c->h_bounce);
+    c->h_bounce = nullptr;
+    if (c->mem_pool) {
+        cudaDeviceSynchronize();
+        cudaMemPoolDestroy(c->mem_pool);
+        c->mem_pool = nullptr;
+    }
     gfs_state& s = c->hs;
     gfs_state* none = nullptr;
     if (c->ds && g_current == c) {
@@ -960,6 +996,50 @@ void* gfs__scratch(gfs_ctx* c, size_t bytes) {
     return c->d_scratch;
 }
 
+void* gfs__dev_alloc(gfs_ctx* c, size_t bytes, cudaStream_t s) {
+    void* p = nullptr;
+    if (c->mem_pool && cudaMallocFromPoolAsync(&p, bytes, c->mem_pool, s) == cudaSuccess) return p;
+    cudaGetLastError();
+    return cudaMalloc(&p, bytes) == cudaSuccess ? p : nullptr;
+}
+
+void gfs__dev_free(gfs_ctx* c, void* p, cudaStream_t s) {
+    if (!p) return;
+    if (c->mem_pool && cudaFreeAsync(p, s) == cudaSuccess) return;
+    cudaGetLastError();
+    cudaFree(p);
+}
+
+int gfs__slot_map(gfs_ctx* c, uint32_t slot, unsigned long long* dev_addr, unsigned long long* len) {
+    *dev_addr = 0;
+    *len = 0;
+    if (!c || !c->slots || slot >= c->hs.n_files) return -GFS_EINVAL;
+    HostSlot& h = c->slots[slot];
+    std::lock_guard<std::mutex> lk(h.mu);
+    FileMap* m = h.open ? h.map.load(std::memory_order_acquire) : nullptr;
+    if (!m) return 0;
+    *dev_addr = m->dev_addr;
+    *len = m->len;
+    return 1;
+}
+
+void* gfs__host_bounce(gfs_ctx* c, size_t bytes) {
+    if (bytes > c->h_bounce_cap) {
+        if (c->h_bounce) cudaFreeHost(c->h_bounce);
+        c->h_bounce = nullptr;
+        c->h_bounce_cap = 0;
+        size_t cap = (size_t)1 << 20;
+        while (cap < bytes) cap <<= 1;
+        if (cudaHostAlloc(&c->h_bounce, cap, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            c->h_bounce = nullptr;
+            return nullptr;
+        }
+        c->h_bounce_cap = cap;
+    }
+    return c->h_bounce;
+}
+
 const gfs_state* gfs__host_state(gfs_ctx* c) { return &c->hs; }
 
 void gfs__preload_runtime() {
@@ -1032,6 +1112,144 @@ int gfs_measure_link(uint64_t bytes, int reps, float* h2d_gbs, float* d2h_gbs) {
     if (h2d_gbs) *h2d_gbs = best_h2d;
     if (d2h_gbs) *d2h_gbs = best_d2h;
     return 0;
+}
+
+/* One SM-driven copy of n16 16-byte vectors from src (host memory mapped
+ * for the device) to dst, four loads in flight per thread. */
+__global__ void k_host_read(const uint4* __restrict__ src, uint64_t n16, uint4* __restrict__ dst) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n16; i += 4 * stride) {
+        const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < n16; i += stride) dst[i] = src[i];
+}
+
+/* The same copy, each CTA reading its own contiguous slice front to back
+ * (as a scan with a static run of chunks per CTA does), 8 loads in flight
+ * per thread. */
+__global__ void k_host_read_slices(const uint4* __restrict__ src, uint64_t n16, uint4* __restrict__ dst) {
+    const uint64_t per = (n16 + gridDim.x - 1) / gridDim.x;
+    const uint64_t lo = per * blockIdx.x, hi = lo + per < n16 ? lo + per : n16;
+    const uint32_t nt = blockDim.x;
+    uint64_t i = lo + threadIdx.x;
+    for (; i + 7u * nt < hi; i += 8u * nt) {
+        uint4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) v[u] = src[i + (uint64_t)u * nt];
+#pragma unroll
+        for (int u = 0; u < 8; u++) dst[i + (uint64_t)u * nt] = v[u];
+    }
+    for (; i < hi; i += nt) dst[i] = src[i];
+}
+
+/* Cold-read ceilings for one file (best of `reps` after a warm-up, GB/s):
+ * out[0] pinned host -> device, one cudaMemcpyAsync; out[1] the same bytes
+ * as `chunk`-byte copies over `streams` streams; out[2] those copies from
+ * the file's registered mapping (the session's cold path); out[3] a kernel
+ * reading the pinned buffer; out[4] a kernel reading the registered file
+ * mapping; out[5] the same, each CTA (one per SM, 1024 threads) reading its
+ * own contiguous slice; out[6] the same with one warp per CTA.  The file is
+ * mapped read-only and must not change meanwhile. */
+int gfs_measure_cold_paths(const char* path, int streams, uint64_t chunk, int reps, float* out, int n_out) {
+    if (!path || streams < 1 || streams > 64 || chunk < 4096 || reps < 1 || !out || n_out < 1) return -GFS_EINVAL;
+    int fd = open(path, O_RDONLY | O_CLOEXEC);
+    if (fd < 0) return -errno;
+    struct stat st;
+    if (fstat(fd, &st) != 0 || st.st_size < (off_t)(1 << 20)) {
+        close(fd);
+        return -GFS_EINVAL;
+    }
+    const size_t len = (size_t)st.st_size & ~(size_t)15;
+    void* map = mmap(nullptr, (size_t)st.st_size, PROT_READ, MAP_SHARED | MAP_POPULATE, fd, 0);
+    close(fd);
+    if (map == MAP_FAILED) return -errno;
+    int rc = 0;
+    void *h = nullptr, *d = nullptr, *hd = nullptr, *md = nullptr;
+    bool reg = false;
+    std::vector<cudaStream_t> ss((size_t)streams, nullptr);
+    cudaEvent_t a = nullptr, b = nullptr;
+    float best[7] = {0, 0, 0, 0, 0, 0, 0};
+    if (cudaHostAlloc(&h, len, cudaHostAllocMapped) == cudaSuccess && cudaMalloc(&d, len) == cudaSuccess) {
+        reg = cudaHostRegister(map, (size_t)st.st_size, cudaHostRegisterMapped | cudaHostRegisterReadOnly) ==
+              cudaSuccess;
+        if (!reg) {
+            cudaGetLastError();
+            reg = cudaHostRegister(map, (size_t)st.st_size, cudaHostRegisterMapped) == cudaSuccess;
+        }
+    }
+    if (!reg) {
+        cudaGetLastError();
+        rc = -GFS_ENOMEM;
+    } else {
+        memcpy(h, map, len);
+        cudaHostGetDevicePointer(&hd, h, 0);
+        cudaHostGetDevicePointer(&md, map, 0);
+        for (auto& x : ss) cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking);
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        int sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        for (int kind = 0; kind < 7 && kind < n_out; kind++) {
+            for (int r = 0; r < reps + 1; r++) {
+                cudaDeviceSynchronize();
+                cudaEventRecord(a, ss[0]);
+                if (kind == 0) {
+                    cudaMemcpyAsync(d, h, len, cudaMemcpyHostToDevice, ss[0]);
+                } else if (kind <= 2) {
+                    const uint8_t* src = kind == 1 ? (const uint8_t*)h : (const uint8_t*)map;
+                    /* every stream starts after the first event and the
+                     * closing event waits for every stream */
+                    for (size_t i = 0, k = 0; i < len; i += chunk, k++) {
+                        cudaStream_t x = ss[k % ss.size()];
+                        if (k < ss.size() && k) cudaStreamWaitEvent(x, a, 0);
+                        cudaMemcpyAsync((uint8_t*)d + i, src + i, len - i < chunk ? len - i : chunk,
+                                        cudaMemcpyHostToDevice, x);
+                    }
+                    for (size_t k = 1; k < ss.size(); k++) {
+                        cudaEvent_t j;
+                        cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
+                        cudaEventRecord(j, ss[k]);
+                        cudaStreamWaitEvent(ss[0], j, 0);
+                        cudaEventDestroy(j);
+                    }
+                } else if (kind <= 4) {
+                    const uint4* src = (const uint4*)(kind == 3 ? hd : md);
+                    k_host_read<<<sms * 4, 512, 0, ss[0]>>>(src, (uint64_t)(len / 16), (uint4*)d);
+                } else {
+                    k_host_read_slices<<<sms, kind == 5 ? 1024 : 32, 0, ss[0]>>>((const uint4*)md,
+                                                                                  (uint64_t)(len / 16), (uint4*)d);
+                }
+                cudaEventRecord(b, ss[0]);
+                if (cudaEventSynchronize(b) != cudaSuccess) {
+                    rc = -GFS_EIO;
+                    break;
+                }
+                float ms = 0;
+                cudaEventElapsedTime(&ms, a, b);
+                const float gbs = (float)((double)len / (ms * 1e-3) / 1e9);
+                if (r > 0 && gbs > best[kind]) best[kind] = gbs;
+            }
+            if (rc) break;
+        }
+    }
+    cudaGetLastError();
+    for (auto& x : ss)
+        if (x) cudaStreamDestroy(x);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (reg) cudaHostUnregister(map);
+    cudaGetLastError();
+    munmap(map, (size_t)st.st_size);
+    cudaFree(d);
+    if (h) cudaFreeHost(h);
+    for (int i = 0; i < n_out && i < 7; i++) out[i] = best[i];
+    return rc;
 }
 
 double _timestamp() {

@@ -3,12 +3,23 @@
 #ifndef GFS_RUNTIME_H
 #define GFS_RUNTIME_H
 #include <stddef.h>
+#include <cuda_runtime.h>
 #include "gpufs_gb300.h"
 #include "gfs_types.h"
 #ifdef __cplusplus
 extern "C" {
 #endif
 void* gfs__scratch(gfs_ctx* c, size_t bytes);
+/* pinned host buffer of at least `bytes` (grown on demand, session-owned;
+ * callers on one session must not overlap) */
+void* gfs__host_bounce(gfs_ctx* c, size_t bytes);
+/* device memory from the session's stream-ordered pool (cudaMalloc when
+ * the pool is unavailable), usable on stream s and after; freed on stream s */
+void* gfs__dev_alloc(gfs_ctx* c, size_t bytes, cudaStream_t s);
+void gfs__dev_free(gfs_ctx* c, void* p, cudaStream_t s);
+/* the registered host mapping of an open file slot, as a device address and
+ * its length (0 when the slot has none); valid while the slot stays open */
+int gfs__slot_map(gfs_ctx* c, uint32_t slot, unsigned long long* dev_addr, unsigned long long* len);
 int gfs__activate(gfs_ctx* c);
 /* the session's bound on device-side waits (ns) */
 unsigned long long gfs__timeout_ns(gfs_ctx* c);

@@ -85,6 +85,14 @@ int gfs_reset_stats(gfs_ctx* ctx);
 long long gfs_drop_cache(gfs_ctx* ctx);
 /* pinned host<->device cudaMemcpyAsync bandwidth, best of `reps` (GB/s) */
 int gfs_measure_link(uint64_t bytes, int reps, float* h2d_gbs, float* d2h_gbs);
+/* Cold-read ceilings for one file of at least 1 MiB (GB/s, best of reps; no
+ * reference counterpart): out[0] pinned host -> device in one copy, out[1]
+ * the same as chunk-byte copies over `streams` streams, out[2] those copies
+ * from the file's registered mapping, out[3] a kernel reading pinned host
+ * memory, out[4] a kernel reading the registered file mapping, out[5] the
+ * same with each CTA reading its own contiguous slice, out[6] the same with
+ * one warp per CTA.  The file must not change during the call. */
+int gfs_measure_cold_paths(const char* path, int streams, uint64_t chunk, int reps, float* out, int n_out);
 
 /* ---- host-side fault injection (tests only; no GPU fault is ever made) ---- */
 /* stall (1) or resume (0) the host service: device waits then time out */
@@ -159,11 +167,18 @@ typedef struct gfs_grep gfs_grep;
 int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths, int n_files, gfs_grep** out);
 /* n_ctas <= 0: one per SM.  *kernel_ms (optional): device time of the scan. */
 int gfs_grep_run(gfs_grep* g, int n_ctas, float* kernel_ms);
+/* The same scan, read once: chunks of files that have a registered host
+ * mapping are loaded by the GPU straight from it (cp.async over the
+ * host link), bypassing the buffer cache, as O_DIRECT does; other files go
+ * through the cache.  No reference counterpart (the sample reads through
+ * the cache). */
+int gfs_grep_run_direct(gfs_grep* g, int n_ctas, float* kernel_ms);
 int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts);
 /* device address of the counts (n_words * n_files uint32) */
 void* gfs_grep_device_counts(gfs_grep* g);
 /* out: n_words, n_files, buckets, table in shared memory (0/1), dynamic shared
- * bytes, chunks */
+ * bytes, chunks, last status word, last error site, host microseconds of the
+ * dictionary table build, host microseconds of opening the files */
 int gfs_grep_info(gfs_grep* g, long long* out, int n);
 int gfs_grep_close(gfs_grep* g);
 /* `steps` runs back to back on the kernel stream; *total_ms: all of them

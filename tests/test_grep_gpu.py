@@ -19,11 +19,11 @@ def sess(built):
     s.close()
 
 
-def _check(sess, dpath, paths, n_ctas=0):
+def _check(sess, dpath, paths, n_ctas=0, direct=False):
     with g.Grep(sess, dpath, paths) as gr:
-        gr.run(n_ctas)
+        gr.run(n_ctas, direct=direct)  # direct: mapped files read by the GPU, bypassing the cache
         got = gr.counts()
-        gr.run(n_ctas)  # second run: cache-resident, same answer
+        gr.run(n_ctas)  # cached run (the second one cache-resident): same answer
         got2 = gr.counts()
     want = oracle.grep_counts(open(dpath, "rb").read(), [open(p, "rb").read() for p in paths], mode="fast")
     assert got.shape == want.shape
@@ -87,6 +87,7 @@ def test_adversarial_tokens(sess, shm_dir):
         paths.append(p)
     assert any(len(oracle.split_points(open(p, "rb").read())) for p in paths)
     _check(sess, dpath, paths)
+    _check(sess, dpath, paths, direct=True)
 
 
 def test_page_sizes_and_tiny_files(built, shm_dir):
@@ -101,7 +102,7 @@ def test_page_sizes_and_tiny_files(built, shm_dir):
     paths = paths + [t1, t2]
     for lp in (12, 14, 16, 20):
         with g.Session(log_page=lp, pool_bytes=128 << 20, timeout_s=20) as s:
-            _check(s, dpath, paths)
+            _check(s, dpath, paths, direct=(lp == 14))
 
 
 def test_large_dictionary_global_table(sess, shm_dir):
@@ -121,6 +122,36 @@ def test_pool_smaller_than_corpus(built, shm_dir):
     with g.Session(log_page=16, pool_bytes=8 << 20, timeout_s=20) as s:
         _check(s, dpath, paths, n_ctas=8)
         assert s.stats()["evictions"] > 0
+
+
+@pytest.mark.parametrize("n_ctas", [0, 5])
+def test_direct_scan_reads_the_mappings(built, shm_dir, n_ctas):
+    """The direct scan reads files of 64 KiB and more from their registered
+    host mappings (no buffer-cache miss for them) and smaller files through
+    the cache; ragged sizes, a file just under and just over the mapping
+    threshold, an empty file; counts equal the oracle and a cached run."""
+    paths, dpath = datagen.grep_corpus(shm_dir, n_files=5, total_bytes=6 * (1 << 20) + 4321, n_vocab=4000,
+                                       n_dict=1500, seed=21)
+    text = open(paths[0], "rb").read()
+    extra = {"under.txt": text[:65535], "over.txt": text[:65543], "small.txt": text[:5001], "empty.txt": b""}
+    for name, data in extra.items():
+        p = os.path.join(shm_dir, name)
+        _write(p, data)
+        paths.append(p)
+    want = oracle.grep_counts(open(dpath, "rb").read(), [open(p, "rb").read() for p in paths], mode="fast")
+    unmapped_pages = sum((os.path.getsize(p) + 65535) // 65536 for p in paths if os.path.getsize(p) < 65536)
+    with g.Session(log_page=16, pool_bytes=256 << 20, timeout_s=20) as s:
+        with g.Grep(s, dpath, paths) as gr:
+            s.reset_stats()
+            gr.run(n_ctas, direct=True)
+            got = gr.counts()
+            st = s.stats()
+            assert 0 < st["misses"] <= unmapped_pages, (st["misses"], unmapped_pages)
+            gr.run(n_ctas)
+            assert np.array_equal(gr.counts(), got)
+        assert s.last_error() == 0
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, (bad[:5], got[tuple(bad[0])], want[tuple(bad[0])])
 
 
 def test_one_shot_grep_text(sess, shm_dir):
