@@ -1410,6 +1410,161 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev 
     }
 }
 
+/* ---------------- dictionary table built on the device ----------------
+ * The same table as the host build (same hashes, tags, buckets, load), made
+ * by five small kernels: keys, dedupe, duplicate chains, a parallel
+ * bucketised cuckoo insertion, and the table image.  Where several valid
+ * placements exist the device may pick another one than the host; the
+ * counts a scan produces do not depend on it. */
+struct TbDev {
+    const uint8_t* dict; /* n records of 32 bytes */
+    int n;
+    uint4* klo;          /* key bytes 0..15 / 16..31 per record */
+    uint4* khi;
+    uint32_t* h1;
+    int* len;
+    int* set;            /* dedupe set: cap entries, -1 empty */
+    uint32_t cap;
+    int* rep;            /* per record: the record its word is counted under, -1 for empty */
+    int* head;           /* per representative: its last duplicate, -1 */
+    int* chain;          /* per duplicate: the next duplicate of its word, -1 */
+    int* slot_of;        /* nb * 4 slots: representative, -1 empty */
+    uint32_t nb;
+    uint32_t* fail;      /* set when an insertion ran out of kicks */
+    /* the image */
+    uint16_t* tags;
+    uint4* rec_lo;
+    uint4* rec_hi;
+    uint32_t* slot_word;
+    int32_t* next_dup;
+};
+
+static __global__ void k_tb_keys(TbDev T) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= T.n) return;
+    const uint4* r = (const uint4*)(T.dict + (size_t)w * 32);
+    const uint4 a = r[0], b = r[1];
+    uint32_t k[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    /* length: bytes before the first NUL; key bytes after it are zero */
+    int len = 32;
+    for (int i = 0; i < 8 && len == 32; i++) {
+        const uint32_t x = k[i];
+        for (int j = 0; j < 4; j++)
+            if (((x >> (8 * j)) & 0xFFu) == 0u) {
+                len = 4 * i + j;
+                break;
+            }
+    }
+    for (int i = 0; i < 8; i++) {
+        const int kb = len * 8 - 32 * i;
+        k[i] &= kb >= 32 ? 0xFFFFFFFFu : (kb <= 0 ? 0u : ((1u << kb) - 1u));
+    }
+    T.klo[w] = make_uint4(k[0], k[1], k[2], k[3]);
+    T.khi[w] = make_uint4(k[4], k[5], k[6], k[7]);
+    T.len[w] = len;
+    T.h1[w] = len ? grep_h1(grep_mix(k, len)) : 0u;
+    T.head[w] = -1;
+    T.chain[w] = -1;
+}
+
+__device__ __forceinline__ bool tb_same(const TbDev& T, int a, int b) {
+    if (T.h1[a] != T.h1[b] || T.len[a] != T.len[b]) return false;
+    const uint4 x = T.klo[a], y = T.klo[b], u = T.khi[a], v = T.khi[b];
+    return x.x == y.x && x.y == y.y && x.z == y.z && x.w == y.w && u.x == v.x && u.y == v.y && u.z == v.z && u.w == v.w;
+}
+
+/* the first record of each distinct word to claim its set entry becomes the
+ * word's representative; the others are its duplicates */
+static __global__ void k_tb_dedupe(TbDev T) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= T.n) return;
+    if (T.len[w] == 0) {
+        T.rep[w] = -1;
+        return;
+    }
+    uint32_t i = T.h1[w] & (T.cap - 1u);
+    for (uint32_t probe = 0; probe < T.cap; probe++, i = (i + 1u) & (T.cap - 1u)) {
+        int cur = T.set[i];
+        if (cur < 0) {
+            cur = atomicCAS(&T.set[i], -1, w);
+            if (cur < 0) {
+                T.rep[w] = w;
+                return;
+            }
+        }
+        if (tb_same(T, cur, w)) {
+            T.rep[w] = cur;
+            return;
+        }
+    }
+    T.rep[w] = w; /* unreachable: the set has twice the records' entries */
+}
+
+static __global__ void k_tb_chains(TbDev T) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= T.n) return;
+    const int r = T.rep[w];
+    if (r >= 0 && r != w) T.chain[w] = atomicExch(&T.head[r], w);
+}
+
+/* one thread per representative; an evicted word is carried on by the
+ * thread that evicted it; at most 4096 moves per thread */
+static __global__ void k_tb_insert(TbDev T) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= T.n || T.rep[w] != w) return;
+    int cur = w;
+    uint32_t rng = 0x9E3779B9u ^ (uint32_t)w * 0x85EBCA6Bu;
+    for (int kick = 0; kick < 4096; kick++) {
+        const uint32_t h = T.h1[cur];
+        const uint32_t b[2] = {grep_bucket(h, T.nb), grep_b2(h, T.nb)};
+        /* the emptier of the two buckets */
+        int best = -1, best_free = 0;
+        for (int q = 0; q < 2; q++) {
+            int nfree = 0, first = -1;
+            for (int i = 0; i < GREP_WAYS; i++) {
+                const int sl = (int)(b[q] * GREP_WAYS) + i;
+                if (((volatile int*)T.slot_of)[sl] < 0) {
+                    nfree++;
+                    if (first < 0) first = sl;
+                }
+            }
+            if (nfree > best_free) {
+                best_free = nfree;
+                best = first;
+            }
+        }
+        if (best >= 0 && atomicCAS(&T.slot_of[best], -1, cur) == -1) return;
+        if (best >= 0) continue; /* lost the slot to another thread: look again */
+        rng ^= rng << 13;
+        rng ^= rng >> 17;
+        rng ^= rng << 5;
+        const int victim = (int)(b[rng & 1u] * GREP_WAYS + ((rng >> 8) & 3u));
+        cur = atomicExch(&T.slot_of[victim], cur);
+        if (cur < 0) return; /* the slot had just been freed: placed */
+    }
+    atomicOr(T.fail, 1u); /* the carried word is lost: the build is retried */
+}
+
+static __global__ void k_tb_image(TbDev T) {
+    const uint32_t sl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sl < T.nb * GREP_WAYS) {
+        const int w = T.slot_of[sl];
+        if (w < 0) {
+            T.tags[sl] = 0;
+            T.rec_lo[sl] = make_uint4(0u, 0u, 0u, 0u);
+            T.rec_hi[sl] = make_uint4(0u, 0u, 0u, 0u);
+            T.slot_word[sl] = 0xFFFFFFFFu;
+        } else {
+            T.tags[sl] = (uint16_t)grep_tag(T.h1[w], T.len[w]);
+            T.rec_lo[sl] = T.klo[w];
+            T.rec_hi[sl] = T.khi[w];
+            T.slot_word[sl] = (uint32_t)w;
+        }
+    }
+    /* duplicate chains: representative -> its duplicates -> -1 */
+    if (sl < (uint32_t)T.n) T.next_dup[sl] = T.rep[sl] == (int)sl ? T.head[sl] : T.chain[sl];
+}
+
 static __global__ void k_open_files(const char* names, int n, int* fds, uint64_t* sizes, int oflags = O_GRDONLY) {
     int f = blockIdx.x;
     if (f >= n) return;
@@ -1582,6 +1737,92 @@ static uint64_t host_us() {
     return (uint64_t)ts.tv_sec * 1000000ull + (uint64_t)ts.tv_nsec / 1000ull;
 }
 
+/* Device layout of a plan: the table image and the file names first, then
+ * what the device fills or the host adds later. */
+struct PlanLayout {
+    size_t o_tbl, o_recs, o_sw, o_nd, o_names, o_cnt, o_fds, o_sz, o_pf, o_fl, o_st, o_fo, o_fn, o_xxh, o_maps, total;
+};
+static PlanLayout plan_layout(uint32_t nb, int n_words, int n_files) {
+    PlanLayout L;
+    const size_t ns = (size_t)nb * 4;
+    L.o_tbl = 0;
+    L.o_recs = align_up(L.o_tbl + (size_t)nb * 8, 256);
+    L.o_sw = align_up(L.o_recs + ns * 32, 256);
+    L.o_nd = align_up(L.o_sw + ns * 4, 256);
+    L.o_names = align_up(L.o_nd + (size_t)n_words * 4 + 4, 256);
+    L.o_cnt = align_up(L.o_names + (size_t)n_files * GFS_NAME_MAX, 256);
+    L.o_fds = align_up(L.o_cnt + (size_t)n_words * n_files * 4 + 4, 256);
+    L.o_sz = align_up(L.o_fds + (size_t)n_files * 4, 256);
+    L.o_pf = align_up(L.o_sz + (size_t)n_files * 8, 256);
+    L.o_fl = align_up(L.o_pf + (size_t)(n_files + 1) * 8, 256);
+    L.o_st = align_up(L.o_fl + (size_t)n_files * 4, 256);
+    L.o_fo = align_up(L.o_st + 64, 256);
+    L.o_fn = align_up(L.o_fo + (size_t)n_files * 4, 256);
+    L.o_xxh = align_up(L.o_fn + 64, 256);
+    L.o_maps = align_up(L.o_xxh + (size_t)n_files * 8, 256);
+    L.total = align_up(L.o_maps + (size_t)n_files * 8, 256);
+    return L;
+}
+
+/* Device build of the dictionary table (the dictionary's n_words records
+ * are in pinned host memory at hdict; flag is 4 spare pinned bytes).  On
+ * success returns the bucket count and leaves the build state in *T and
+ * its memory in *tmp; the caller runs k_tb_image into the plan memory and
+ * frees *tmp.  0: every insertion attempt failed (*tmp freed). */
+static uint32_t device_table(gfs_ctx* ctx, cudaStream_t s, const uint8_t* hdict, uint32_t* flag, int n_words,
+                             TbDev* T, void** tmp) {
+    const size_t n = (size_t)(n_words > 0 ? n_words : 1);
+    uint32_t cap = 16;
+    while (cap < 2 * n) cap <<= 1;
+    uint32_t nb = (uint32_t)((double)n_words / (GREP_WAYS * 0.92)) + 16u;
+    uint32_t nb_max = nb;
+    for (int a = 0; a < 4; a++) nb_max = nb_max + nb_max / 8u + 1u;
+    const size_t o_dict = 0, o_klo = align_up(n * 32, 256), o_khi = align_up(o_klo + n * 16, 256),
+                 o_h1 = align_up(o_khi + n * 16, 256), o_len = align_up(o_h1 + n * 4, 256),
+                 o_rep = align_up(o_len + n * 4, 256), o_head = align_up(o_rep + n * 4, 256),
+                 o_nd = align_up(o_head + n * 4, 256), o_set = align_up(o_nd + n * 4, 256),
+                 o_slots = align_up(o_set + (size_t)cap * 4, 256), o_fail = align_up(o_slots + (size_t)nb_max * 16, 256),
+                 total = o_fail + 256;
+    uint8_t* m = (uint8_t*)gfs__dev_alloc(ctx, total, s);
+    *tmp = m;
+    if (!m) return 0;
+    TbDev& D = *T;
+    D.dict = m + o_dict;
+    D.n = n_words;
+    D.klo = (uint4*)(m + o_klo);
+    D.khi = (uint4*)(m + o_khi);
+    D.h1 = (uint32_t*)(m + o_h1);
+    D.len = (int*)(m + o_len);
+    D.rep = (int*)(m + o_rep);
+    D.head = (int*)(m + o_head);
+    D.set = (int*)(m + o_set);
+    D.cap = cap;
+    D.slot_of = (int*)(m + o_slots);
+    D.fail = (uint32_t*)(m + o_fail);
+    D.chain = (int*)(m + o_nd);
+    const int nt = 256, gw = (n_words + nt - 1) / nt;
+    if (n_words > 0) {
+        cudaMemcpyAsync(m + o_dict, hdict, (size_t)n_words * 32, cudaMemcpyHostToDevice, s);
+        cudaMemsetAsync(D.set, 0xFF, (size_t)cap * 4, s);
+        k_tb_keys<<<gw, nt, 0, s>>>(D);
+        k_tb_dedupe<<<gw, nt, 0, s>>>(D);
+        k_tb_chains<<<gw, nt, 0, s>>>(D);
+    }
+    for (int a = 0; a < 5; a++, nb = nb + nb / 8u + 1u) {
+        D.nb = nb;
+        cudaMemsetAsync(D.slot_of, 0xFF, (size_t)nb * 16, s);
+        cudaMemsetAsync(D.fail, 0, 4, s);
+        if (n_words > 0) k_tb_insert<<<gw, nt, 0, s>>>(D);
+        cudaMemcpyAsync(flag, D.fail, 4, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) break;
+        if (*flag == 0u) return nb;
+    }
+    cudaGetLastError();
+    gfs__dev_free(ctx, m, s);
+    *tmp = nullptr;
+    return 0;
+}
+
 extern "C" {
 
 void gfs__preload_grep() {
@@ -1604,59 +1845,78 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     for (int i = 0; i < n_files; i++)
         if (!paths[i] || strlen(paths[i]) >= GFS_NAME_MAX) return -GFS_EINVAL;
     if (gfs__activate(ctx)) return -GFS_EIO;
-    BuildWs& W = g_ws;
-    std::unique_lock<std::mutex> lk(W.mu);
     int fd = open(dict_path, O_RDONLY | O_CLOEXEC);
     if (fd < 0) return -errno;
     struct stat st;
     if (fstat(fd, &st) != 0) { const int e = errno; close(fd); return -e; }
-    W.dict.resize((size_t)st.st_size + 32);
-    memset(W.dict.data() + st.st_size, 0, 32);
-    ssize_t got = 0;
-    while (got < st.st_size) {
-        ssize_t r = pread(fd, W.dict.data() + got, (size_t)(st.st_size - got), got);
+    const int n_words = (int)(st.st_size / 32); /* grep_text_gpu.cu:221 */
+    const size_t dict_bytes = (size_t)n_words * 32;
+    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
+    /* the dictionary goes straight into the session's pinned buffer */
+    const size_t names_bytes = (size_t)n_files * GFS_NAME_MAX;
+    uint8_t* hb = (uint8_t*)gfs__host_bounce(ctx, align_up(dict_bytes, 256) + 256 + names_bytes);
+    if (!hb) { close(fd); return -GFS_ENOMEM; }
+    size_t got = 0;
+    while (got < dict_bytes) {
+        ssize_t r = pread(fd, hb + got, dict_bytes - got, (off_t)got);
         if (r <= 0) break;
-        got += r;
+        got += (size_t)r;
     }
     close(fd);
+    if (got < dict_bytes) return -GFS_EIO;
     gfs_grep* g = new gfs_grep();
     g->ctx = ctx;
     g->n_files = n_files;
-    g->n_words = (int)(st.st_size / 32); /* grep_text_gpu.cu:221 */
+    g->n_words = n_words;
     int dev = 0, sms = 0, maxsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     const size_t fixed = (size_t)GR_STAGES * GR_STAGE + (size_t)GR_CONS * GR_WSCR + 256;
     const uint64_t t_build = host_us();
-    if (!build_table(W.dict.data(), g->n_words, W)) { delete g; return -GFS_ENOMEM; }
-    g->build_us = (long long)(host_us() - t_build);
-    const uint32_t nb = W.nb;
+    TbDev T{};
+    void* tmp = nullptr;
+    uint32_t nb = device_table(ctx, s, hb, (uint32_t*)(hb + align_up(dict_bytes, 256)), n_words, &T, &tmp);
+    std::unique_lock<std::mutex> lk(g_ws.mu, std::defer_lock);
+    if (!nb) {
+        /* the device insertion gave up: build on the host */
+        lk.lock();
+        if (!build_table(hb, n_words, g_ws)) { delete g; return -GFS_ENOMEM; }
+        nb = g_ws.nb;
+    }
     g->nb = nb;
     const size_t ns = (size_t)nb * 4; /* slots */
-    /* device layout: the table image and the file names first (uploaded in
-     * one copy), then what the device fills or the host adds later */
-    size_t o_tbl = 0, o_recs = align_up(o_tbl + (size_t)nb * 8, 256), o_sw = align_up(o_recs + ns * 32, 256),
-           o_nd = align_up(o_sw + ns * 4, 256), o_names = align_up(o_nd + (size_t)g->n_words * 4 + 4, 256),
-           o_cnt = align_up(o_names + (size_t)n_files * GFS_NAME_MAX, 256),
-           o_fds = align_up(o_cnt + (size_t)g->n_words * n_files * 4 + 4, 256), o_sz = align_up(o_fds + (size_t)n_files * 4, 256),
-           o_pf = align_up(o_sz + (size_t)n_files * 8, 256), o_fl = align_up(o_pf + (size_t)(n_files + 1) * 8, 256),
-           o_st = align_up(o_fl + (size_t)n_files * 4, 256), o_fo = align_up(o_st + 64, 256),
-           o_fn = align_up(o_fo + (size_t)n_files * 4, 256), o_xxh = align_up(o_fn + 64, 256),
-           o_maps = align_up(o_xxh + (size_t)n_files * 8, 256), total = align_up(o_maps + (size_t)n_files * 8, 256);
-    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
+    const PlanLayout L = plan_layout(nb, n_words, n_files);
+    const size_t o_tbl = L.o_tbl, o_recs = L.o_recs, o_sw = L.o_sw, o_nd = L.o_nd, o_names = L.o_names,
+                 o_cnt = L.o_cnt, o_fds = L.o_fds, o_sz = L.o_sz, o_pf = L.o_pf, o_fl = L.o_fl, o_st = L.o_st,
+                 o_fo = L.o_fo, o_fn = L.o_fn, o_xxh = L.o_xxh, o_maps = L.o_maps, total = L.total;
     g->dmem = gfs__dev_alloc(ctx, total, s);
-    uint8_t* hb = (uint8_t*)gfs__host_bounce(ctx, o_cnt);
-    if (!g->dmem || !hb) {
+    if (!g->dmem || !(hb = (uint8_t*)gfs__host_bounce(ctx, tmp ? names_bytes : o_cnt))) {
+        gfs__dev_free(ctx, tmp, s);
         gfs__dev_free(ctx, g->dmem, s);
         delete g;
         return -GFS_ENOMEM;
     }
     uint8_t* b = (uint8_t*)g->dmem;
     cudaMemsetAsync(b + o_cnt, 0, total - o_cnt, s);
-    {
-        /* the table image: slot tags, record bytes 0..15 of every slot, then
-         * bytes 16..31, first record of each slot, duplicate chains; names */
+    if (tmp) {
+        /* the device-built image, then the names */
+        T.tags = (uint16_t*)(b + o_tbl);
+        T.rec_lo = (uint4*)(b + o_recs);
+        T.rec_hi = T.rec_lo + ns;
+        T.slot_word = (uint32_t*)(b + o_sw);
+        T.next_dup = (int32_t*)(b + o_nd);
+        const uint32_t items = (uint32_t)(ns > (size_t)n_words ? ns : (size_t)n_words);
+        k_tb_image<<<(items + 255) / 256, 256, 0, s>>>(T);
+        gfs__dev_free(ctx, tmp, s);
+        memset(hb, 0, names_bytes);
+        for (int i = 0; i < n_files; i++) memcpy(hb + (size_t)i * GFS_NAME_MAX, paths[i], strlen(paths[i]));
+        cudaMemcpyAsync(b + o_names, hb, names_bytes, cudaMemcpyHostToDevice, s);
+    } else {
+        /* the host-built image: slot tags, record bytes 0..15 of every
+         * slot, then bytes 16..31, first record of each slot, duplicate
+         * chains; names */
+        BuildWs& W = g_ws;
         memset(hb, 0, o_cnt);
         uint16_t* tags = (uint16_t*)(hb + o_tbl);
         uint32_t* lo = (uint32_t*)(hb + o_recs);
@@ -1674,11 +1934,12 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
             memcpy(hi + sl * 4, kw.k + 4, 16);
             sw[sl] = (uint32_t)w;
         }
-        if (g->n_words) memcpy(hb + o_nd, W.next_dup.data(), (size_t)g->n_words * 4);
+        if (n_words) memcpy(hb + o_nd, W.next_dup.data(), (size_t)n_words * 4);
         for (int i = 0; i < n_files; i++) memcpy(hb + o_names + (size_t)i * GFS_NAME_MAX, paths[i], strlen(paths[i]));
         cudaMemcpyAsync(b, hb, o_cnt, cudaMemcpyHostToDevice, s);
+        lk.unlock();
     }
-    lk.unlock();
+    g->build_us = (long long)(host_us() - t_build);
     GrepDev& d = g->dev;
     d.n_files = n_files;
     d.n_words = g->n_words;
