@@ -354,7 +354,14 @@ def main():
         "cpu_baseline": cpu,
         "e2e": {"value": ws * corpus / e2e_t / 1e9, "unit": "GB/s",
                 "h2d_bytes_per_step": corpus + os.path.getsize(dpath), "d2h_bytes_per_step": counts_bytes,
-                "ms_per_step": e2e_t * 1e3, "call": "gfs_grep_text (cold buffer cache)"},
+                "ms_per_step": e2e_t * 1e3,
+                "call": "gfs_grep_text: open 32 files + build the dictionary table + direct scan (files read by "
+                        "the GPU from their registered host mappings) + counts to host + close; cold buffer cache",
+                "roofline": {"bound": "host link", "achieved": corpus / e2e_t / 1e9,
+                             "peak": extra.get("link_h2d_gbs"), "unit": "GB/s",
+                             "frac": (corpus / e2e_t / 1e9) / extra["link_h2d_gbs"]
+                             if extra.get("link_h2d_gbs") else None,
+                             "peak_source": "measured pinned H2D copy (cudaMemcpyAsync, 1 GiB)"}},
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,
         "parity": parity,
