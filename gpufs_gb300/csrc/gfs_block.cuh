@@ -41,9 +41,12 @@ __device__ __forceinline__ void grp_zero(uint8_t* dst, size_t n, int rank, int g
     for (size_t k = (size_t)rank; k < n; k += (size_t)gsize) dst[k] = 0;
 }
 
-/* Copy a round of `npages` page segments between frames and a linear user
- * buffer.  Segment j covers file bytes [max(pos, page_j), min(end, page_j+1)).
- * to_frame selects the direction. */
+/* Copy a round of `npages` pages' bytes [pos, end) between frames and a
+ * linear user buffer (frames[j] holds page first + j); to_frame selects the
+ * direction.  Every warp takes an equal contiguous slice of the round (cut
+ * at 512-byte multiples, so frame and buffer keep their relative alignment)
+ * and walks the page boundaries inside it: a round whose first and last
+ * pages are partial keeps all warps equally busy. */
 __device__ __forceinline__ void blk_copy_round(gfs_state* S, const int* frames, uint32_t first, int npages,
                                                uint64_t pos, uint64_t end, uint8_t* ubuf, uint64_t ubase,
                                                bool to_frame) {
@@ -52,25 +55,83 @@ __device__ __forceinline__ void blk_copy_round(gfs_state* S, const int* frames, 
     const int nwarps = (nthr + 31) >> 5;
     const int gsize = (warp == nwarps - 1) ? (nthr - 32 * warp) : 32;
     const uint32_t lp = S->log_page;
-    const uint64_t page = 1ull << lp;
-    int parts = nwarps / npages;
-    if (parts < 1) parts = 1;
-    const int items = npages * parts;
-    for (int k = warp; k < items; k += nwarps) {
-        int j = k / parts, p = k % parts;
-        uint64_t pstart = ((uint64_t)(first + (uint32_t)j)) << lp;
-        uint64_t s0 = pos > pstart ? pos : pstart;
-        uint64_t e0 = end < pstart + page ? end : pstart + page;
-        if (e0 <= s0) continue;
-        uint64_t len = e0 - s0;
-        uint64_t plen = ((len + (uint64_t)parts - 1) / (uint64_t)parts + 511u) & ~511ull;
-        uint64_t a = (uint64_t)p * plen;
-        if (a >= len) continue;
-        uint64_t b = a + plen < len ? a + plen : len;
-        uint8_t* fptr = frame_data(S, (uint32_t)frames[j]) + (s0 - pstart) + a;
-        uint8_t* uptr = ubuf + (s0 - ubase) + a;
-        if (to_frame) grp_copy(fptr, uptr, b - a, lane, gsize);
-        else grp_copy(uptr, fptr, b - a, lane, gsize);
+    (void)npages;
+    if (end <= pos) return;
+    const uint64_t pmask = (1ull << lp) - 1u;
+    const uintptr_t delta = (uintptr_t)ubuf - (uintptr_t)ubase; /* user address of file offset x: delta + x */
+    if ((delta & 15u) == 0u) {
+        /* frame and buffer agree mod 16 (frames are page-aligned): the whole
+         * block sweeps the round as one stream of 16-byte units, consecutive
+         * threads on consecutive units, four in flight per thread -- one
+         * DRAM stream per block instead of one per warp */
+        const uint64_t u0 = (pos + 15u) >> 4, u1 = end >> 4;
+        if (u0 >= u1) {
+            for (uint64_t x = pos + (uint64_t)tid; x < end; x += (uint64_t)nthr) {
+                uint8_t* f = frame_data(S, (uint32_t)frames[(uint32_t)(x >> lp) - first]) + (x & pmask);
+                uint8_t* u = (uint8_t*)(delta + x);
+                if (to_frame) *f = *u;
+                else *u = *f;
+            }
+            return;
+        }
+        /* bytes before the first and after the last whole unit */
+        for (uint64_t x = pos + (uint64_t)tid; x < (u0 << 4); x += (uint64_t)nthr) {
+            uint8_t* f = frame_data(S, (uint32_t)frames[(uint32_t)(x >> lp) - first]) + (x & pmask);
+            uint8_t* u = (uint8_t*)(delta + x);
+            if (to_frame) *f = *u;
+            else *u = *f;
+        }
+        for (uint64_t x = (u1 << 4) + (uint64_t)tid; x < end; x += (uint64_t)nthr) {
+            uint8_t* f = frame_data(S, (uint32_t)frames[(uint32_t)(x >> lp) - first]) + (x & pmask);
+            uint8_t* u = (uint8_t*)(delta + x);
+            if (to_frame) *f = *u;
+            else *u = *f;
+        }
+        const uint64_t step = (uint64_t)nthr;
+        uint64_t u = u0 + (uint64_t)tid;
+        for (; u + 3 * step < u1; u += 4 * step) {
+            uint4* fp[4];
+            uint4* up[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const uint64_t x = (u + (uint64_t)k * step) << 4;
+                fp[k] = (uint4*)(frame_data(S, (uint32_t)frames[(uint32_t)(x >> lp) - first]) + (x & pmask));
+                up[k] = (uint4*)(delta + x);
+            }
+            uint4 v[4];
+            if (to_frame) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) v[k] = ld_cg4(up[k]);
+#pragma unroll
+                for (int k = 0; k < 4; k++) *fp[k] = v[k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++) v[k] = ld_cg4(fp[k]);
+#pragma unroll
+                for (int k = 0; k < 4; k++) *up[k] = v[k];
+            }
+        }
+        for (; u < u1; u += step) {
+            const uint64_t x = u << 4;
+            uint4* f = (uint4*)(frame_data(S, (uint32_t)frames[(uint32_t)(x >> lp) - first]) + (x & pmask));
+            uint4* up = (uint4*)(delta + x);
+            if (to_frame) *f = ld_cg4(up);
+            else *up = ld_cg4(f);
+        }
+        return;
+    }
+    const uint64_t per = ((end - pos + (uint64_t)nwarps - 1) / (uint64_t)nwarps + 511u) & ~511ull;
+    uint64_t a = pos + (uint64_t)warp * per;
+    const uint64_t b = a + per < end ? a + per : end;
+    while (a < b) {
+        const uint32_t j = (uint32_t)(a >> lp) - first;
+        const uint64_t pstart = (uint64_t)(first + j) << lp;
+        const uint64_t e = b < pstart + (1ull << lp) ? b : pstart + (1ull << lp);
+        uint8_t* fptr = frame_data(S, (uint32_t)frames[j]) + (a - pstart);
+        uint8_t* uptr = ubuf + (a - ubase);
+        if (to_frame) grp_copy(fptr, uptr, e - a, lane, gsize);
+        else grp_copy(uptr, fptr, e - a, lane, gsize);
+        a = e;
     }
 }
 

@@ -36,6 +36,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <sys/mman.h>
+#include <sys/prctl.h>
 #include <sys/resource.h>
 #include <sys/stat.h>
 #include <sys/time.h>
@@ -632,14 +633,30 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
     }
 }
 
+static uint64_t mono_ns() {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (uint64_t)ts.tv_sec * 1000000000ull + (uint64_t)ts.tv_nsec;
+}
+
+/* A worker waits for the request of its own ring ticket.  It spins, then
+ * yields the CPU while requests came recently (GFS_HOT_NS after the last
+ * one it served: a kernel's next request, such as the close after its
+ * reads, is then picked up within microseconds), then naps 10 us at a time
+ * with a 1 us timer slack (the default 50 us slack would stretch every
+ * nap, and with it the latency of the first request after a quiet spell). */
+#define GFS_HOT_NS 2000000ull
 static void worker_main(gfs_ctx* c, Worker* w) {
     cudaSetDevice(c->cfg.device);
     cudaFree(nullptr);
+    prctl(PR_SET_TIMERSLACK, 1000UL, 0, 0, 0);
     const uint32_t R = c->cfg.ring_slots, mask = R - 1;
+    uint64_t last_busy = mono_ns();
     while (!c->stop.load(std::memory_order_relaxed)) {
         uint32_t t = c->head.fetch_add(1);
         gfs_req* slot = &c->ring_h[t & mask];
         unsigned spins = 0;
+        bool hot = mono_ns() - last_busy < GFS_HOT_NS;
         while (__atomic_load_n(&slot->seq, __ATOMIC_ACQUIRE) != t + 1u) {
             if (c->stop.load(std::memory_order_relaxed)) return;
             if (w->nbusy) {
@@ -650,13 +667,15 @@ static void worker_main(gfs_ctx* c, Worker* w) {
                 continue;
             }
             if (spins++ < 4096u) continue;
-            if (spins < 8192u) {
+            if (hot) {
                 sched_yield();
+                if ((spins & 255u) == 0u && mono_ns() - last_busy >= GFS_HOT_NS) hot = false;
                 continue;
             }
-            struct timespec ts = {0, 20000};
+            struct timespec ts = {0, 10000};
             nanosleep(&ts, nullptr);
         }
+        last_busy = mono_ns();
         while (c->paused.load(std::memory_order_relaxed) && !c->stop.load(std::memory_order_relaxed)) {
             struct timespec ts = {0, 200000};
             nanosleep(&ts, nullptr);
