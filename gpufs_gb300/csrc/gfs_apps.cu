@@ -80,10 +80,50 @@ __device__ float dot_part(const float* a, const float* b, uint32_t n) {
     return (s0 + s1) + (s2 + s3);
 }
 
+/* Eight rows at once: a (16-byte aligned) holds rows of stride4 float4s,
+ * b the vector; each thread loads a float4 of b once per column step and
+ * the eight rows' float4s beside it (eight loads in flight), and the eight
+ * sums are reduced together.  y[0..7] (shared) are valid after return. */
+__device__ __noinline__ void dot_rows8(const float* a, size_t stride4, const float* b, uint32_t n4, float* red, float* y) {
+    float s[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) s[k] = 0.f;
+    const float4* a4 = (const float4*)a;
+    const float4* b4 = (const float4*)b;
+    for (uint32_t i = threadIdx.x; i < n4; i += blockDim.x) {
+        const float4 q = __ldg(b4 + i);
+        float4 p[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) p[k] = __ldcg(a4 + (size_t)k * stride4 + i);
+#pragma unroll
+        for (int k = 0; k < 8; k++) s[k] = fmaf(p[k].w, q.w, fmaf(p[k].z, q.z, fmaf(p[k].y, q.y, fmaf(p[k].x, q.x, s[k]))));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xFFFFFFFFu, s[k], o);
+    }
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 8; k++) red[k * 32 + warp] = s[k];
+    __syncthreads();
+    if (warp == 0)
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            float r = lane < nw ? red[k * 32 + lane] : 0.f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xFFFFFFFFu, r, o);
+            if (lane == 0) y[k] = r;
+        }
+    __syncthreads();
+}
+
 /* y = A x.  vec/mat/out: device file names; x_buf: cols floats of scratch
  * per block when x does not fit in one page. */
 __global__ void k_bigmatrix(const char* f_v, const char* f_m, const char* f_o, float* x_scratch, long long* res) {
-    __shared__ float red[32];
+    __shared__ float red[8 * 32];
+    __shared__ float ys[8];
     __shared__ int s_fail;
     const uint32_t page = g_gfs->page_size;
     int zfd_m = gopen(f_m, O_GRDONLY);
@@ -137,36 +177,56 @@ __global__ void k_bigmatrix(const char* f_v, const char* f_m, const char* f_o, f
     uint64_t mbase = ~0ull;
     volatile uint8_t* opage = (volatile uint8_t*)-1;
     uint64_t obase = ~0ull;
-    for (uint64_t r = r0; r < r1 && !result; r++) {
-        /* the row may span pages: walk its segments */
+    /* map the output page holding y[r] (block-collective) and store y there
+     * (thread 0; gmunmap of that page later is block-collective, so the
+     * store is ordered before it without a barrier of its own) */
+    auto put_y = [&](uint64_t r, float y) {
+        const uint64_t oo = r * 4, ob = oo / page * page;
+        if (ob != obase) {
+            if (opage != (volatile uint8_t*)-1) gmunmap(opage, 0);
+            uint64_t olen = rows * 4 - ob < page ? rows * 4 - ob : page;
+            opage = (volatile uint8_t*)gmmap(NULL, olen, 0, O_GWRONCE, zfd_o, (off_t)ob);
+            if (opage == (volatile uint8_t*)-1) { result = -GFS_EIO; obase = ~0ull; return; }
+            obase = ob;
+        }
+        if (threadIdx.x == 0) *(volatile float*)(opage + (oo - ob)) = y;
+    };
+    /* the matrix page holding byte pb, mapped (block-collective) */
+    auto map_m = [&](uint64_t pb) {
+        if (pb == mbase) return;
+        if (mpage != (volatile uint8_t*)-1) gmunmap(mpage, 0);
+        uint64_t mlen = size_m * 4 - pb < page ? size_m * 4 - pb : page;
+        mpage = (volatile uint8_t*)gmmap(NULL, mlen, 0, O_GRDONLY, zfd_m, (off_t)pb);
+        if (mpage == (volatile uint8_t*)-1) { result = -GFS_EIO; mbase = ~0ull; return; }
+        mbase = pb;
+    };
+    const bool vec4 = (cols & 3u) == 0u && (((uintptr_t)x) & 15u) == 0u;
+    for (uint64_t r = r0; r < r1 && !result;) {
         const uint64_t rbeg = r * cols * 4, rend = rbeg + cols * 4;
+        const uint64_t pb0 = rbeg / page * page;
+        if (vec4 && r + 8 <= r1 && rbeg + 8 * cols * 4 <= pb0 + page) {
+            /* eight whole rows inside one page */
+            map_m(pb0);
+            if (result) break;
+            dot_rows8((const float*)(mpage + (rbeg - pb0)), cols / 4, x, (uint32_t)(cols / 4), red, ys);
+            for (int k = 0; k < 8 && !result; k++) put_y(r + (uint64_t)k, ys[k]);
+            r += 8;
+            continue;
+        }
+        /* one row; it may span pages: walk its segments */
         float acc = 0.f;
         for (uint64_t pos = rbeg; pos < rend && !result;) {
             const uint64_t pb = pos / page * page;
-            if (pb != mbase) {
-                if (mpage != (volatile uint8_t*)-1) gmunmap(mpage, 0);
-                uint64_t mlen = size_m * 4 - pb < page ? size_m * 4 - pb : page;
-                mpage = (volatile uint8_t*)gmmap(NULL, mlen, 0, O_GRDONLY, zfd_m, (off_t)pb);
-                if (mpage == (volatile uint8_t*)-1) { result = -GFS_EIO; mbase = ~0ull; break; }
-                mbase = pb;
-            }
+            map_m(pb);
+            if (result) break;
             const uint64_t seg_end = pb + page < rend ? pb + page : rend;
             acc += dot_part((const float*)(mpage + (pos - pb)), x + (pos - rbeg) / 4, (uint32_t)((seg_end - pos) / 4));
             pos = seg_end;
         }
         if (result) break;
         float y = block_sum(acc, red);
-        /* output: map the page holding y[r] */
-        const uint64_t oo = r * 4, ob = oo / page * page;
-        if (ob != obase) {
-            if (opage != (volatile uint8_t*)-1) gmunmap(opage, 0);
-            uint64_t olen = rows * 4 - ob < page ? rows * 4 - ob : page;
-            opage = (volatile uint8_t*)gmmap(NULL, olen, 0, O_GWRONCE, zfd_o, (off_t)ob);
-            if (opage == (volatile uint8_t*)-1) { result = -GFS_EIO; obase = ~0ull; break; }
-            obase = ob;
-        }
-        if (threadIdx.x == 0) *(volatile float*)(opage + (oo - ob)) = y;
-        __syncthreads();
+        put_y(r, y);
+        r++;
     }
     if (mpage != (volatile uint8_t*)-1) gmunmap(mpage, 0);
     if (opage != (volatile uint8_t*)-1) gmunmap(opage, 0);
