@@ -144,6 +144,53 @@ __device__ size_t fstat(int fd) {
 }
 
 /* device side of the samples' INIT_LOCK / LAST_SEMAPHORE / ERROR helpers */
+/* ---- fat pointers (include/fat_pointer.cu.h) ----
+ * Single-thread page steps the header-only FatPointer template calls; a
+ * warp's lanes that want the same page of a file share one call, taking
+ * `ref` pins. */
+
+/* pin the page holding byte `off` of fd with `ref` pins; returns the frame
+ * or -errno; *fresh: a write-once page the caller must zero and publish */
+__device__ int gfs_fp_acquire(int fd, unsigned long long off, int ref, int* fresh) {
+    gfs_state* S = g_gfs;
+    bool fr = false;
+    const unsigned long long page_start = off & ~((unsigned long long)S->page_size - 1ull);
+    const int r = map_pin(S, fd, page_start, 0, &fr, ref < 1 ? 1 : ref);
+    *fresh = fr ? 1 : 0;
+    return r;
+}
+
+__device__ unsigned char* gfs_fp_data(int frame) { return frame_data(g_gfs, (uint32_t)frame); }
+
+__device__ void gfs_fp_publish(int frame) { publish_valid(g_gfs, (uint32_t)frame); }
+
+__device__ unsigned int gfs_fp_log_page() { return g_gfs->log_page; }
+
+/* drop `ref` pins of a frame; for a writable file the page is marked dirty
+ * and its content and the file's size grow to cover the `touched` bytes of
+ * the page (page_start: the page's file offset) */
+__device__ void gfs_fp_release(int frame, int ref, unsigned int touched, unsigned long long page_start) {
+    gfs_state* S = g_gfs;
+    if (frame < 0) return;
+    const uint64_t key = ld_rlx64(&S->frames[frame].key);
+    const uint32_t f = key_file(key);
+    if (f < S->n_files && ld_rlx((const uint32_t*)&S->files[f].flags) != (uint32_t)O_GRDONLY) {
+        __threadfence();
+        if (touched) {
+            atomicMax(&S->frames[frame].content, touched);
+            atomicMax((unsigned long long*)&S->files[f].size, page_start + touched);
+        }
+        mark_dirty(S, (uint32_t)frame);
+    }
+    unpin(S, (uint32_t)frame, (uint32_t)(ref < 1 ? 1 : ref));
+}
+
+/* where a failed translation's accesses go (16 bytes per lane; the
+ * session's error bits record the failure) */
+__device__ uint4 g_fp_sink[32 * 8];
+
+__device__ unsigned char* gfs_fp_sink() { return (unsigned char*)&g_fp_sink[(threadIdx.x & 31u) * 8u]; }
+
 __device__ unsigned int g_gfs_user_error;
 __device__ void gfs_report_user_error(const char* msg, const char* file, int line) {
     atomicOr(&g_gfs_user_error, 1u);

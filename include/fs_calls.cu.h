@@ -5,8 +5,8 @@
  * per-thread.  Link with libgpufs.a using relocatable device code
  * (nvcc -rdc=true), as with the reference.
  *
- * Not provided: gvmmap/FatPointer/TLB (libgpufs/fat_pointer.cu.h), used only
- * by the mosaic sample.
+ * gvmmap/FatPointer/TLB (libgpufs/fat_pointer.cu.h) are in fat_pointer.cu.h,
+ * included here as in the reference.
  */
 #ifndef FS_CALLS_CU
 #define FS_CALLS_CU
@@ -16,6 +16,7 @@
 #include "util.cu.h"
 #include "timer.h"
 #include "fs_globals.cu.h"
+#include "fat_pointer.cu.h"
 
 __device__ int single_thread_fsync(int fd);
 __device__ int single_thread_ftruncate(int fd, int size);
