@@ -94,6 +94,7 @@ _SIGS = {
     "gfs_grep_bench": (_int, [_c_p, _int, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "gfs_drop_cache": (_i64, [_c_p]),
     "gfs_bigmatrix": (_int, [_c_p, _c_s, _c_s, _c_s, _int, _int, ctypes.POINTER(ctypes.c_float)]),
+    "gfs_bigmatrix_direct": (_int, [_c_p, _c_s, _c_s, _c_s, _int, _int, ctypes.POINTER(ctypes.c_float)]),
     "gfs_xxh64_files": (_int, [_c_p, ctypes.POINTER(_c_s), _int, ctypes.POINTER(ctypes.c_ulonglong),
                                ctypes.POINTER(ctypes.c_float)]),
     "gfs_xxh64_files_noalloc": (_int, [_c_p, ctypes.POINTER(_c_s), _int, ctypes.POINTER(ctypes.c_ulonglong)]),
@@ -232,11 +233,14 @@ class Session:
                "gfs_memcopy")
         return ms.value
 
-    def bigmatrix(self, vec_path, mat_path, out_path, nblocks=152, nthreads=256):
-        """y = A x through gmmap (samples/bigmatrix_mmap); returns kernel ms."""
+    def bigmatrix(self, vec_path, mat_path, out_path, nblocks=152, nthreads=256, direct=False):
+        """y = A x through gmmap (samples/bigmatrix_mmap); returns kernel ms.
+        direct=True reads the matrix straight from its host mapping (one pass
+        over a cold matrix)."""
         ms = ctypes.c_float(0)
-        _check(self.L.gfs_bigmatrix(self._h, _p(vec_path), _p(mat_path), _p(out_path), nblocks, nthreads,
-                                    ctypes.byref(ms)), "gfs_bigmatrix")
+        fn = self.L.gfs_bigmatrix_direct if direct else self.L.gfs_bigmatrix
+        _check(fn(self._h, _p(vec_path), _p(mat_path), _p(out_path), nblocks, nthreads, ctypes.byref(ms)),
+               "gfs_bigmatrix")
         return ms.value
 
     def xxh64_files(self, paths):

@@ -32,6 +32,9 @@
 
 extern __device__ gfs_state* g_gfs;
 
+/* gfs_calls.cu: a read-only file's bytes in its registered host mapping */
+__device__ const void* gfs_direct_addr(int fd, unsigned long long off, unsigned long long size);
+
 namespace {
 
 __device__ unsigned int g_init_lock; /* INIT_LOCK of the reference sample */
@@ -121,7 +124,11 @@ __device__ __noinline__ void dot_rows8(const float* a, size_t stride4, const flo
 
 /* y = A x.  vec/mat/out: device file names; x_buf: cols floats of scratch
  * per block when x does not fit in one page. */
-__global__ void k_bigmatrix(const char* f_v, const char* f_m, const char* f_o, float* x_scratch, long long* res) {
+/* direct: read the matrix straight from its registered host mapping when it
+ * has one (one pass over a cold matrix: no cache pages, SM loads over the
+ * host link) */
+__global__ void k_bigmatrix(const char* f_v, const char* f_m, const char* f_o, float* x_scratch, long long* res,
+                            int direct) {
     __shared__ float red[8 * 32];
     __shared__ float ys[8];
     __shared__ int s_fail;
@@ -201,7 +208,22 @@ __global__ void k_bigmatrix(const char* f_v, const char* f_m, const char* f_o, f
         mbase = pb;
     };
     const bool vec4 = (cols & 3u) == 0u && (((uintptr_t)x) & 15u) == 0u;
-    for (uint64_t r = r0; r < r1 && !result;) {
+    const uint8_t* dm = (direct && !result) ? (const uint8_t*)gfs_direct_addr(zfd_m, 0, size_m * 4) : nullptr;
+    if (dm) {
+        /* the whole matrix in one mapping: eight-row passes anywhere */
+        for (uint64_t r = r0; r < r1 && !result;) {
+            if (vec4 && r + 8 <= r1) {
+                dot_rows8((const float*)(dm + r * cols * 4), cols / 4, x, (uint32_t)(cols / 4), red, ys);
+                for (int k = 0; k < 8 && !result; k++) put_y(r + (uint64_t)k, ys[k]);
+                r += 8;
+            } else {
+                float y = block_sum(dot_part((const float*)(dm + r * cols * 4), x, (uint32_t)cols), red);
+                put_y(r, y);
+                r++;
+            }
+        }
+    }
+    for (uint64_t r = dm ? r1 : r0; r < r1 && !result;) {
         const uint64_t rbeg = r * cols * 4, rend = rbeg + cols * 4;
         const uint64_t pb0 = rbeg / page * page;
         if (vec4 && r + 8 <= r1 && rbeg + 8 * cols * 4 <= pb0 + page) {
@@ -351,8 +373,8 @@ void gfs__preload_apps() {
     cudaFuncGetAttributes(&a, k_close_many);
 }
 
-int gfs_bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
-                  int nthreads, float* kernel_ms) {
+static int bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
+                     int nthreads, float* kernel_ms, int direct) {
     if (!vec_path || !mat_path || !out_path || nblocks < 1 || nthreads < 32 || nthreads > 1024) return -GFS_EINVAL;
     if (strlen(vec_path) >= GFS_NAME_MAX || strlen(mat_path) >= GFS_NAME_MAX || strlen(out_path) >= GFS_NAME_MAX)
         return -GFS_EINVAL;
@@ -385,7 +407,7 @@ int gfs_bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, cons
         cudaEventCreate(&b);
         cudaEventRecord(a, s);
     }
-    k_bigmatrix<<<nblocks, nthreads, 0, s>>>(d, d + GFS_NAME_MAX, d + 2 * GFS_NAME_MAX, xs, res);
+    k_bigmatrix<<<nblocks, nthreads, 0, s>>>(d, d + GFS_NAME_MAX, d + 2 * GFS_NAME_MAX, xs, res, direct);
     cudaError_t le = cudaGetLastError();
     if (kernel_ms) {
         cudaEventRecord(b, s);
@@ -397,6 +419,16 @@ int gfs_bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, cons
     long long r = le == cudaSuccess ? sum_results(res, nblocks, s) : -GFS_EINVAL;
     if (xs) cudaFree(xs);
     return r < 0 ? (int)r : 0;
+}
+
+int gfs_bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
+                  int nthreads, float* kernel_ms) {
+    return bigmatrix(ctx, vec_path, mat_path, out_path, nblocks, nthreads, kernel_ms, 0);
+}
+
+int gfs_bigmatrix_direct(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
+                         int nthreads, float* kernel_ms) {
+    return bigmatrix(ctx, vec_path, mat_path, out_path, nblocks, nthreads, kernel_ms, 1);
 }
 
 /* XXH64 of each file (read through the buffer cache), seed 0. */

@@ -144,6 +144,21 @@ __device__ size_t fstat(int fd) {
 }
 
 /* device side of the samples' INIT_LOCK / LAST_SEMAPHORE / ERROR helpers */
+/* Bytes [off, off + size) of a file opened read-only, addressed straight
+ * in its registered host mapping (SM loads over the host link, no cache
+ * page); nullptr when the file has no mapping or the range passes its size
+ * at open.  Valid while the file stays open. */
+__device__ const void* gfs_direct_addr(int fd, unsigned long long off, unsigned long long size) {
+    gfs_state* S = g_gfs;
+    if (fd < 0 || (uint32_t)fd >= S->n_files) return nullptr;
+    gfs_file* fe = &S->files[fd];
+    if (sstatus(ld_acq(&fe->st)) != GFS_SS_OPEN) return nullptr;
+    if (ld_rlx((const uint32_t*)&fe->flags) != (uint32_t)O_GRDONLY) return nullptr;
+    const uint64_t m = ld_rlx64(&fe->map_dev);
+    if (!m || off + size > ld_rlx64(&fe->size) || off + size < off) return nullptr;
+    return (const void*)(uintptr_t)(m + off);
+}
+
 /* ---- fat pointers (include/fat_pointer.cu.h) ----
  * Single-thread page steps the header-only FatPointer template calls; a
  * warp's lanes that want the same page of a file share one call, taking

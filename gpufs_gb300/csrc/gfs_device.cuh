@@ -765,6 +765,7 @@ __device__ __noinline__ int file_open(gfs_state* S, const char* name, int oflags
                     st_rlx((uint32_t*)&fe->err, 0u);
                     st_rlx64(&fe->size, ld_rlx_sys64(&rep->size));
                     st_rlx64((uint64_t*)&fe->ctime_ns, ld_rlx_sys64((const uint64_t*)&rep->ctime_ns));
+                    st_rlx64(&fe->map_dev, ld_rlx_sys64(&rep->map_dev));
                     __threadfence();
                 }
                 if (rc < 0) {

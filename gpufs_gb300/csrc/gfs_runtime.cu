@@ -467,6 +467,7 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
             rep.size = (uint64_t)st.st_size;
             rep.ctime_ns = (int64_t)st.st_ctim.tv_sec * 1000000000LL + st.st_ctim.tv_nsec;
             FileMap* fm = (hflags & O_ACCMODE) == O_RDONLY ? map_attach(c, fd, st) : nullptr;
+            rep.map_dev = fm ? fm->dev_addr : 0u;
             HostSlot& h = c->slots[r.file];
             {
                 std::lock_guard<std::mutex> lk(h.mu);

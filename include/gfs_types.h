@@ -110,6 +110,7 @@ typedef struct gfs_open_reply {
     int32_t err;
     uint64_t size;
     int64_t ctime_ns;
+    uint64_t map_dev; /* device address of the file's registered host mapping (read-only opens), 0 if none */
 } gfs_open_reply;
 
 typedef struct gfs_file {
@@ -127,7 +128,8 @@ typedef struct gfs_file {
     uint64_t cached_ctime; /* ctime the cached pages belong to */
     uint64_t cached_size;
     uint32_t lock;
-    uint32_t pad[3];
+    uint32_t pad;
+    uint64_t map_dev; /* from the reply: the registered host mapping, 0 if none */
     char name[GFS_NAME_MAX];
 } gfs_file;
 
@@ -195,6 +197,6 @@ typedef struct gfs_state {
 }
 static_assert(sizeof(gfs_req) == 136, "gfs_req layout");
 static_assert(sizeof(gfs_frame) == 32, "gfs_frame layout");
-static_assert(sizeof(gfs_open_reply) == 24, "gfs_open_reply layout");
+static_assert(sizeof(gfs_open_reply) == 32, "gfs_open_reply layout");
 #endif
 #endif

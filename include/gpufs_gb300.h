@@ -142,6 +142,12 @@ int gfs_memcopy(gfs_ctx* ctx, const char* src, const char* dst, int nblocks, int
  * FP32 accumulation, deterministic reduction order. */
 int gfs_bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
                   int nthreads, float* kernel_ms);
+/* The same GEMV read once: when the matrix file has a registered host
+ * mapping, the kernel reads it straight from there (SM loads over the host
+ * link, no cache pages, as O_DIRECT); x and y go through the cache.  No
+ * reference counterpart. */
+int gfs_bigmatrix_direct(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
+                         int nthreads, float* kernel_ms);
 /* XXH64 (seed 0) of each file, read through the buffer cache; one warp per file */
 int gfs_xxh64_files(gfs_ctx* ctx, const char* const* paths, int n, unsigned long long* host_out, float* kernel_ms);
 

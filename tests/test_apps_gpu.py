@@ -32,6 +32,29 @@ def test_bigmatrix_matches_fp64(built, shm_dir, rows, cols, log_page):
     assert np.all(np.abs(y - y64) <= 1e-5 * ay)
 
 
+@pytest.mark.parametrize("rows,cols", [(96, 65536), (37, 8192 + 4), (11, 1023)])
+def test_bigmatrix_direct_matches_fp64(built, shm_dir, rows, cols):
+    """The one-pass form reads the matrix straight from its host mapping (or
+    through the cache when it has none) within the same bounds."""
+    vp, mp, op = (os.path.join(shm_dir, n) for n in ("v.f32", "m.f32", "o.f32"))
+    datagen.normal_f32(vp, cols, seed=7)
+    datagen.normal_f32(mp, rows * cols, seed=8)
+    with g.Session(log_page=16, pool_bytes=256 << 20, timeout_s=20) as s:
+        s.reset_stats()
+        s.bigmatrix(vp, mp, op, nblocks=7, nthreads=256, direct=True)
+        assert s.last_error() == 0, s.error_report()
+        mat_pages = (rows * cols * 4 + 65535) // 65536
+        if rows * cols * 4 >= 65536:  # mapped: the matrix never enters the cache
+            assert s.stats()["misses"] < mat_pages
+    A = np.fromfile(mp, dtype=np.float32).reshape(rows, cols)
+    x = np.fromfile(vp, dtype=np.float32)
+    y = np.fromfile(op, dtype=np.float32)
+    assert y.size == rows
+    y64, ay = oracle.gemv_f64(A, x)
+    assert np.linalg.norm(y - y64) / np.linalg.norm(y64) <= 1e-5
+    assert np.all(np.abs(y - y64) <= 1e-5 * ay)
+
+
 def test_bigmatrix_deterministic(built, shm_dir):
     vp, mp = os.path.join(shm_dir, "v.f32"), os.path.join(shm_dir, "m.f32")
     datagen.normal_f32(vp, 8192, seed=5)
