@@ -184,6 +184,7 @@ struct gfs_ctx {
     void* h_bounce = nullptr;  /* pinned host buffer for results copied back to callers' memory */
     size_t h_bounce_cap = 0;
     cudaMemPool_t mem_pool = nullptr; /* stream-ordered device memory of per-call objects (plans, servers) */
+    int pageable = 0; /* kernels may address pageable host memory (host page tables) */
     /* driver entry point, resolved through the runtime so the library does
      * not link libcuda directly (it loads on machines without a driver) */
     uint8_t* hmap = nullptr;   /* mapped block: completion words + open replies (host view) */
@@ -847,6 +848,10 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
         CK(cudaMemcpyToSymbol(g_gfs, &c->ds, sizeof(gfs_state*)));
         g_current = c;
         CK(cudaStreamCreateWithFlags(&c->kstream, cudaStreamNonBlocking));
+        if (cudaDeviceGetAttribute(&c->pageable, cudaDevAttrPageableMemoryAccess, cfg.device) != cudaSuccess) {
+            cudaGetLastError();
+            c->pageable = 0;
+        }
         {
             /* the session's own pool, kept warm (nothing returned to the
              * driver at synchronisation points) */
@@ -1015,6 +1020,8 @@ void* gfs__scratch(gfs_ctx* c, size_t bytes) {
     }
     return c->d_scratch;
 }
+
+int gfs__pageable_access(gfs_ctx* c) { return c && c->pageable; }
 
 void* gfs__dev_alloc(gfs_ctx* c, size_t bytes, cudaStream_t s) {
     void* p = nullptr;

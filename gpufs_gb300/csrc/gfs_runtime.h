@@ -16,6 +16,9 @@ void* gfs__host_bounce(gfs_ctx* c, size_t bytes);
 /* device memory from the session's stream-ordered pool (cudaMalloc when
  * the pool is unavailable), usable on stream s and after; freed on stream s */
 void* gfs__dev_alloc(gfs_ctx* c, size_t bytes, cudaStream_t s);
+/* kernels of the session's device may address pageable host memory
+ * (cudaDevAttrPageableMemoryAccess: host page tables, as on Grace) */
+int gfs__pageable_access(gfs_ctx* c);
 void gfs__dev_free(gfs_ctx* c, void* p, cudaStream_t s);
 /* the registered host mapping of an open file slot, as a device address and
  * its length (0 when the slot has none); valid while the slot stays open */

@@ -287,13 +287,19 @@ long long gfs_pread_dev(gfs_ctx* c, const char* path, uint64_t off, uint64_t siz
     return collect(c, n, nblocks);
 }
 
+/* Host buffers: where the device reads pageable host memory through the
+ * host's page tables, the kernel takes the caller's buffer as it is (its
+ * copies cross the host link as they go, both directions at once);
+ * otherwise a device buffer from the session pool is copied in or out. */
 long long gfs_pread(gfs_ctx* c, const char* path, uint64_t off, uint64_t size, void* host_out, int nblocks,
                     int nthreads) {
-    void* d = nullptr;
-    if (size && cudaMalloc(&d, size) != cudaSuccess) return -GFS_ENOMEM;
+    if (gfs__pageable_access(c)) return gfs_pread_dev(c, path, off, size, host_out, nblocks, nthreads, nullptr);
+    cudaStream_t st = (cudaStream_t)gfs_kernel_stream(c);
+    void* d = size ? gfs__dev_alloc(c, size, st) : nullptr;
+    if (size && !d) return -GFS_ENOMEM;
     long long r = gfs_pread_dev(c, path, off, size, d, nblocks, nthreads, nullptr);
     if (r > 0 && cudaMemcpy(host_out, d, (size_t)r, cudaMemcpyDeviceToHost) != cudaSuccess) r = -GFS_EIO;
-    cudaFree(d);
+    gfs__dev_free(c, d, st);
     return r;
 }
 
@@ -302,16 +308,17 @@ static long long pwrite_impl(gfs_ctx* c, const char* path, int oflags, uint64_t 
     Names n;
     int rc = stage(c, path, nullptr, nblocks, &n);
     if (rc) return rc;
-    void* d = nullptr;
-    if (size && cudaMalloc(&d, size) != cudaSuccess) return -GFS_ENOMEM;
-    if (size && cudaMemcpy(d, host_in, size, cudaMemcpyHostToDevice) != cudaSuccess) {
-        cudaFree(d);
+    cudaStream_t st = (cudaStream_t)gfs_kernel_stream(c);
+    const bool direct = gfs__pageable_access(c) != 0;
+    void* d = direct ? (void*)host_in : (size ? gfs__dev_alloc(c, size, st) : nullptr);
+    if (size && !d) return -GFS_ENOMEM;
+    if (!direct && size && cudaMemcpyAsync(d, host_in, size, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        gfs__dev_free(c, d, st);
         return -GFS_EIO;
     }
-    cudaStream_t st = (cudaStream_t)gfs_kernel_stream(c);
     k_pwrite<<<nblocks, nthreads, 0, st>>>(n.a, oflags, off, size, (const uint8_t*)d, n.results, do_fsync);
     long long r = cudaGetLastError() == cudaSuccess ? collect(c, n, nblocks) : -GFS_EINVAL;
-    cudaFree(d);
+    if (!direct) gfs__dev_free(c, d, st);
     return r;
 }
 
@@ -329,13 +336,16 @@ long long gfs_mmap_read(gfs_ctx* c, const char* path, uint64_t off, uint64_t siz
     Names n;
     int rc = stage(c, path, nullptr, nblocks, &n);
     if (rc) return rc;
-    void* d = nullptr;
-    if (size && cudaMalloc(&d, size) != cudaSuccess) return -GFS_ENOMEM;
     cudaStream_t st = (cudaStream_t)gfs_kernel_stream(c);
+    const bool direct = gfs__pageable_access(c) != 0;
+    void* d = direct ? host_out : (size ? gfs__dev_alloc(c, size, st) : nullptr);
+    if (size && !d) return -GFS_ENOMEM;
     k_mmap_read<<<nblocks, nthreads, 0, st>>>(n.a, off, size, (uint8_t*)d, n.results, use_warp_api);
     long long r = cudaGetLastError() == cudaSuccess ? collect(c, n, nblocks) : -GFS_EINVAL;
-    if (r > 0 && cudaMemcpy(host_out, d, (size_t)r, cudaMemcpyDeviceToHost) != cudaSuccess) r = -GFS_EIO;
-    cudaFree(d);
+    if (!direct) {
+        if (r > 0 && cudaMemcpy(host_out, d, (size_t)r, cudaMemcpyDeviceToHost) != cudaSuccess) r = -GFS_EIO;
+        gfs__dev_free(c, d, st);
+    }
     return r;
 }
 
