@@ -2168,9 +2168,32 @@ int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts) {
     if (!g) return -GFS_EINVAL;
     cudaStream_t s = (cudaStream_t)gfs_kernel_stream(g->ctx);
     const size_t bytes = (size_t)g->n_words * g->n_files * 4;
-    /* through the session's pinned buffer, at most 16 MiB at a time: DMA at
-     * link speed, then a host copy (a pageable copy is staged by the driver
-     * and much slower) */
+    /* through the session's pinned buffer: DMA at link speed, then a host
+     * copy (a pageable copy is staged by the driver and much slower).  Up to
+     * 1 GiB goes in one DMA and is copied out by several host threads (a
+     * count matrix of thousands of files is hundreds of MB); larger ones go
+     * 16 MiB at a time. */
+    if (bytes > ((size_t)16 << 20) && bytes <= ((size_t)1 << 30)) {
+        uint8_t* big = (uint8_t*)gfs__host_bounce(g->ctx, bytes);
+        if (big) {
+            if (cudaMemcpyAsync(big, g->dev.counts, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess)
+                return -GFS_EIO;
+            unsigned nt = std::thread::hardware_concurrency();
+            nt = nt < 1u ? 1u : (nt > 16u ? 16u : nt);
+            if ((size_t)nt > bytes / ((size_t)8 << 20)) nt = (unsigned)(bytes / ((size_t)8 << 20));
+            if (nt < 1u) nt = 1u;
+            const size_t per = (bytes / nt + 4095u) & ~(size_t)4095u;
+            std::vector<std::thread> th;
+            for (unsigned i = 1; i < nt; i++) {
+                const size_t a = per * i, e = a + per < bytes ? a + per : bytes;
+                if (a < e) th.emplace_back([=] { memcpy((uint8_t*)host_counts + a, big + a, e - a); });
+            }
+            memcpy(host_counts, big, per < bytes ? per : bytes);
+            for (auto& x : th) x.join();
+            return 0;
+        }
+    }
     const size_t piece = bytes < ((size_t)16 << 20) ? bytes : ((size_t)16 << 20);
     void* hb = gfs__host_bounce(g->ctx, piece);
     if (hb) {

@@ -154,6 +154,23 @@ def test_direct_scan_reads_the_mappings(built, shm_dir, n_ctas):
     assert bad.size == 0, (bad[:5], got[tuple(bad[0])], want[tuple(bad[0])])
 
 
+def test_large_count_matrix(built, shm_dir):
+    """A count matrix over 16 MB (20,000 words x 220 files) comes back in one
+    DMA and a multi-threaded host copy, equal to the oracle."""
+    voc = datagen.vocab(30000, seed=31)
+    dpath = os.path.join(shm_dir, "big.gpu")
+    datagen.dictionary(dpath, voc, 20000, seed=32)
+    paths = [os.path.join(shm_dir, "m%03d.txt" % i) for i in range(220)]
+    datagen.zipf_files(paths, [3000 + 97 * i for i in range(220)], voc, s=1.1, seed=33)
+    want = oracle.grep_counts(open(dpath, "rb").read(), [open(p, "rb").read() for p in paths], mode="fast")
+    assert want.nbytes > 16 << 20
+    with g.Session(log_page=16, pool_bytes=128 << 20, max_files=512, timeout_s=20) as s:
+        with g.Grep(s, dpath, paths) as gr:
+            gr.run()
+            got = gr.counts()
+    assert np.array_equal(got, want)
+
+
 def test_one_shot_grep_text(sess, shm_dir):
     paths, dpath = datagen.grep_corpus(shm_dir, n_files=2, total_bytes=1 << 20, n_vocab=1000, n_dict=300, seed=10)
     got = g.grep_text(sess, dpath, paths)
