@@ -1,0 +1,69 @@
+"""Host logic of the benchmark (CPU only): the served workload's request
+trace has the stated op mix, popularity skew and alignment, writes go to
+disjoint regions of the output files, the byte accounting clamps at end of
+file, and the max-over-ranks helper is the identity on one rank."""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+import gpufs_gb300 as g  # noqa: E402
+
+
+def _trace(n_files=2000, n_req=20000, n_out=8, seed=1):
+    rng = np.random.default_rng(seed)
+    sizes = [int(x) for x in rng.integers(4096, 4 << 20, n_files)]
+    return sizes, bench._served_trace(sizes, n_req, n_out, np.random.default_rng(seed + 1))
+
+
+def test_served_trace_op_mix_and_alignment():
+    sizes, reqs = _trace()
+    ops = reqs["op"]
+    mix = [float(np.mean(ops == op)) for op in (g.SV_READ, g.SV_GREP, g.SV_WRITE)]
+    assert abs(mix[0] - 0.80) < 0.02 and abs(mix[1] - 0.15) < 0.02 and abs(mix[2] - 0.05) < 0.01
+    rd = reqs[ops != g.SV_WRITE]
+    assert np.all(rd["offset"] % 4096 == 0)
+    sz = np.asarray(sizes, dtype=np.uint64)
+    assert np.all(rd["offset"] <= sz[rd["file"]])
+    lengths = reqs["length"].astype(np.float64)
+    assert lengths.min() >= 4096 and lengths.max() <= 16 << 20
+    # log-uniform lengths: the median sits near the geometric mean of the range
+    assert abs(np.log(np.median(lengths)) - 0.5 * (np.log(4096) + np.log(16 << 20))) < 0.2
+
+
+def test_served_trace_popularity_is_skewed():
+    sizes, reqs = _trace()
+    rd = reqs[reqs["op"] != g.SV_WRITE]
+    counts = np.sort(np.bincount(rd["file"], minlength=len(sizes)))[::-1]
+    # Zipf(0.9) over 2000 files: the top 1 % of files draw a large share
+    assert counts[:20].sum() > 0.15 * counts.sum()
+    assert counts[0] > 10 * max(1, int(np.median(counts)))
+
+
+def test_served_writes_are_disjoint_and_aligned():
+    _, reqs = _trace()
+    wr = reqs[reqs["op"] == g.SV_WRITE]
+    assert np.all(wr["offset"] % 16 == 0)
+    for f in np.unique(wr["file"]):
+        w = np.sort(wr[wr["file"] == f], order="offset")
+        ends = w["offset"] + w["length"]
+        assert np.all(ends[:-1] <= w["offset"][1:])
+
+
+def test_served_bytes_clamp_at_end_of_file():
+    sizes = [10000, 5000]
+    reqs = np.zeros(4, dtype=g.SERVE_REQ)
+    reqs[0] = (g.SV_READ, 0, 8192, 100000, 0)   # clamps to 1808
+    reqs[1] = (g.SV_GREP, 1, 0, 1000, 0)       # 1000
+    reqs[2] = (g.SV_READ, 1, 8192, 4096, 0)    # past the end: 0
+    reqs[3] = (g.SV_WRITE, 0, 0, 777, 0)       # writes count their length
+    assert bench._served_bytes(reqs, sizes) == 1808 + 1000 + 0 + 777
+
+
+def test_allmax_single_rank():
+    assert bench.allmax(None, 3.5) == 3.5
