@@ -171,6 +171,24 @@ def test_large_count_matrix(built, shm_dir):
     assert np.array_equal(got, want)
 
 
+def test_empty_and_degenerate_dictionaries(built, shm_dir):
+    """No records, only empty records, and one word repeated: the table
+    built on the device handles each, and counts equal the oracle."""
+    paths, _ = datagen.grep_corpus(shm_dir, n_files=2, total_bytes=300000, n_vocab=500, n_dict=100, seed=41)
+    text = open(paths[0], "rb").read()
+    word = text.split()[3][:12]
+    cases = {"none.gpu": b"", "empties.gpu": b"\0" * 32 * 5,
+             "repeated.gpu": (word + b"\0" * (32 - len(word))) * 7 + b"\0" * 32}
+    with g.Session(log_page=16, pool_bytes=64 << 20, timeout_s=20) as s:
+        for name, recs in cases.items():
+            dpath = os.path.join(shm_dir, name)
+            _write(dpath, recs)
+            want = oracle.grep_counts(recs, [open(p, "rb").read() for p in paths], mode="fast")
+            got = g.grep_text(s, dpath, paths)
+            assert got.shape == want.shape and np.array_equal(got, want), name
+        assert s.last_error() == 0
+
+
 def test_one_shot_grep_text(sess, shm_dir):
     paths, dpath = datagen.grep_corpus(shm_dir, n_files=2, total_bytes=1 << 20, n_vocab=1000, n_dict=300, seed=10)
     got = g.grep_text(sess, dpath, paths)
