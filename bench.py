@@ -905,8 +905,8 @@ def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
     t_open = time.perf_counter() - t0
     # saturation: a burst of requests all due at once
     burst = _served_trace(sizes, 30000, n_out, rng)
-    sv.run(burst[:2000], inflight_pages=budget, warps_per_sm=16)  # warm-up
-    res = sv.run(burst, inflight_pages=budget, warps_per_sm=16)
+    sv.run(burst[:2000], inflight_pages=budget, warps_per_sm=32)  # warm-up
+    res = sv.run(burst, inflight_pages=budget, warps_per_sm=32)
     # saturation: the whole burst (long enough that its last large requests
     # are a small part of it), every request due at once
     span = float(res["complete_ns"].max()) / 1e9
@@ -922,7 +922,7 @@ def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
         reqs = _served_trace(sizes, n_req, n_out, rng)
         rate = frac * sat_rps
         reqs["arrival_ns"] = np.cumsum(rng.exponential(1e9 / rate, n_req)).astype(np.uint64)
-        r = sv.run(reqs, inflight_pages=budget, warps_per_sm=16)
+        r = sv.run(reqs, inflight_pages=budget, warps_per_sm=32)
         lat = (r["complete_ns"].astype(np.int64) - reqs["arrival_ns"].astype(np.int64)) / 1e3
         dur = (int(r["complete_ns"].max()) - int(reqs["arrival_ns"].min())) / 1e9
         loads.append({"offered_frac": frac, "offered_rps": rate, "achieved_rps": n_req / dur,
@@ -1009,7 +1009,7 @@ def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
                                    "Zipf(0.9), lengths log-uniform 4 KiB-16 MiB, 80%% read+XXH64 / 15%% grep / 5%% "
                                    "write, 24 GiB buffer cache, memory-gated admission, open-loop Poisson arrivals at "
                                    "10-90%% of saturation" % (len(paths), total / 2 ** 30),
-                       "page_bytes": 1 << page_log, "warps_per_sm": 16, "admission_pages": budget,
+                       "page_bytes": 1 << page_log, "warps_per_sm": 32, "admission_pages": budget,
                        "value_at": "90%% of saturation load, p99 %.0f us" % top["p99_us"]},
             "roofline": {"bound": "link", "achieved": top["gbs"], "peak": link[0] if link else None, "unit": "GB/s",
                          "frac": top["gbs"] / link[0] if link else None, "peak_source": "measured pinned H2D",
