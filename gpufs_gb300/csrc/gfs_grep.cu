@@ -1606,7 +1606,6 @@ struct BuildWs {
         int len;
     };
     std::mutex mu;
-    std::vector<uint8_t> dict;
     std::vector<Key> key;
     std::vector<int> uniq, last, seen, slot_of;
     std::vector<uint32_t> ba, bb;
