@@ -185,8 +185,6 @@ struct gfs_ctx {
     size_t h_bounce_cap = 0;
     cudaMemPool_t mem_pool = nullptr; /* stream-ordered device memory of per-call objects (plans, servers) */
     int pageable = 0; /* kernels may address pageable host memory (host page tables) */
-    /* driver entry point, resolved through the runtime so the library does
-     * not link libcuda directly (it loads on machines without a driver) */
     uint8_t* hmap = nullptr;   /* mapped block: completion words + open replies (host view) */
     uint8_t* hmap_d = nullptr; /* same, device view */
     size_t hmap_bytes = 0;
