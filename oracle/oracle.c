@@ -19,7 +19,7 @@
  *   - orc_grep_counts_fast is the single-pass restatement (tokenise once, hash
  *     lookup); it is checked against orc_grep_file_faithful on random and
  *     adversarial inputs.
- *   - orc_gemv_f64 is the FP64 host GEMV the bigmatrix sample is judged by
+ *   - orc_gemv_f64 is the FP64 host GEMV the bigmatrix sample is checked against
  *     (samples/bigmatrix_mmap/bigmatrix_mmap.cu:24-41 computes the FP32 dot).
  */
 #include <stdint.h>
