@@ -38,6 +38,7 @@ STAT_NAMES = ["hits", "misses", "evictions", "writebacks", "read_rpcs", "bytes_r
 ERR_TIMEOUT, ERR_IO, ERR_NOMEM, ERR_TABLE, ERR_ARG = 1, 2, 4, 8, 16
 XXH64_NOALLOC_MAX_FILES = 1024  # GFS_XXH64_NOALLOC_MAX_FILES
 CFG_NO_FILE_MAP = 1  # GFS_CFG_NO_FILE_MAP
+CFG_RETAIN_CACHE = 2  # GFS_CFG_RETAIN_CACHE
 
 
 class Config(ctypes.Structure):
@@ -93,6 +94,8 @@ _SIGS = {
     "gfs_serve_close": (_int, [_c_p]),
     "gfs_grep_bench": (_int, [_c_p, _int, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "gfs_drop_cache": (_i64, [_c_p]),
+    "gfs_retained_pages": (_i64, [_c_p]),
+    "gfs_release_retained": (_int, []),
     "gfs_bigmatrix": (_int, [_c_p, _c_s, _c_s, _c_s, _int, _int, ctypes.POINTER(ctypes.c_float)]),
     "gfs_bigmatrix_direct": (_int, [_c_p, _c_s, _c_s, _c_s, _int, _int, ctypes.POINTER(ctypes.c_float)]),
     "gfs_xxh64_files": (_int, [_c_p, ctypes.POINTER(_c_s), _int, ctypes.POINTER(ctypes.c_ulonglong),
@@ -140,6 +143,12 @@ class GfsError(OSError):
     pass
 
 
+def release_retained_cache():
+    """Free a buffer cache that a closed Session(retain_cache=True) kept and
+    no later session took over; True if one was freed."""
+    return bool(lib().gfs_release_retained())
+
+
 def _check(rc, what):
     if rc < 0:
         raise GfsError(-rc, "%s failed: %s" % (what, os.strerror(-rc) if -rc < 200 else str(rc)))
@@ -150,7 +159,11 @@ class Session:
     """One file-system session on one GPU (initializer() .. delete GPUGlobals)."""
 
     def __init__(self, log_page=16, pool_bytes=2 << 30, max_files=1024, ring_slots=4096, host_workers=8,
-                 staging_depth=8, timeout_s=30.0, device=0, file_map=True):
+                 staging_depth=8, timeout_s=30.0, device=0, file_map=True, retain_cache=False):
+        """retain_cache: keep the buffer cache in HBM when the session closes,
+        for the next session of this process with the same log_page,
+        pool_bytes, max_files and device (kept only if every file is closed
+        and every page clean); see retained_pages."""
         L = lib()
         c = Config()
         L.gfs_default_config(ctypes.byref(c))
@@ -160,7 +173,7 @@ class Session:
         c.ring_slots = ring_slots
         c.host_workers = host_workers
         c.staging_depth = staging_depth
-        c.flags = 0 if file_map else CFG_NO_FILE_MAP
+        c.flags = (0 if file_map else CFG_NO_FILE_MAP) | (CFG_RETAIN_CACHE if retain_cache else 0)
         c.timeout_ns = int(timeout_s * 1e9)
         c.device = device
         h = ctypes.c_void_p()
@@ -169,6 +182,8 @@ class Session:
         self.L = L
         self.page_size = L.gfs_page_size(h)
         self.n_frames = L.gfs_num_frames(h)
+        # valid pages taken over from a cache an earlier session retained
+        self.retained_pages = int(L.gfs_retained_pages(h))
 
     @property
     def handle(self):

@@ -203,6 +203,7 @@ struct gfs_ctx {
     size_t mapped_bytes = 0, map_cap = 0;
     uint64_t map_clock = 0;
     std::atomic<unsigned long long> h_map_reads{0};
+    unsigned long long retained_pages = 0; /* valid pages taken over from a retained cache */
 };
 
 static uint32_t* host_word(gfs_ctx* c, uint64_t dev_addr) {
@@ -714,6 +715,112 @@ __attribute__((constructor)) static void gfs_set_connections() { setenv("CUDA_DE
 
 void gfs__preload_runtime();
 
+/* A buffer cache kept in HBM after its session ended (GFS_CFG_RETAIN_CACHE)
+ * for the next session of this process with the same geometry: page pool,
+ * frames, page index and file table, every page clean and unpinned and
+ * every file closed.  File slots keep their names, generations and the
+ * ctime and size their pages belong to, so the next session's first open of
+ * a file compares those with the host's reply, as a reopen within a session
+ * does (the version check of fs_calls.cu:197-218), and drops the pages of a
+ * file that changed in between. */
+struct RetainedCache {
+    int device = -1;
+    uint32_t log_page = 0, n_frames = 0, n_buckets = 0, n_files = 0;
+    uint8_t* pool = nullptr;
+    gfs_frame* frames = nullptr;
+    uint32_t* index = nullptr;
+    uint32_t* bucket_lock = nullptr;
+    gfs_file* files = nullptr;
+    uint32_t* dirty_bits = nullptr;
+    unsigned long long pages = 0; /* valid pages */
+};
+static std::mutex g_retained_mu;
+static RetainedCache* g_retained = nullptr; /* under g_retained_mu */
+
+static void retained_free(RetainedCache* r) {
+    if (!r) return;
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) cur = -1;
+    cudaSetDevice(r->device);
+    cudaFree(r->pool);
+    cudaFree(r->frames);
+    cudaFree(r->index);
+    cudaFree(r->bucket_lock);
+    cudaFree(r->files);
+    cudaFree(r->dirty_bits);
+    if (cur >= 0) cudaSetDevice(cur);
+    cudaGetLastError();
+    delete r;
+}
+
+/* What keeps a cache from being retained: frames pinned, dirty, or in a
+ * state other than FREE and VALID (a DEAD frame had a request time out);
+ * files other than EMPTY or CLOSED without openers; held locks.
+ * out[0] += such objects, out[1] += valid pages. */
+__global__ void k_retain_check(const gfs_state* S, unsigned long long* out) {
+    unsigned long long bad = 0, valid = 0;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, T = gridDim.x * blockDim.x;
+    for (uint32_t i = tid; i < S->n_frames; i += T) {
+        const uint32_t st = S->frames[i].st, s = (st >> GFS_F_SHIFT) & 0xFu;
+        if (st & (GFS_F_PINS | GFS_F_DIRTY)) bad++;
+        else if (s == GFS_FS_VALID) valid++;
+        else if (s != GFS_FS_FREE) bad++;
+    }
+    for (uint32_t i = tid; i < S->n_files; i += T) {
+        const uint32_t st = S->files[i].st, s = st >> GFS_S_SHIFT;
+        if (!(s == GFS_SS_EMPTY || (s == GFS_SS_CLOSED && (st & GFS_S_CNT) == 0u))) bad++;
+    }
+    for (uint32_t i = tid; i < S->n_buckets; i += T)
+        if (S->bucket_lock[i]) bad++;
+    if (tid == 0 && S->table_lock) bad++;
+    if (bad) atomicAdd(&out[0], bad);
+    if (valid) atomicAdd(&out[1], valid);
+}
+
+/* At the end of a session (device idle, host workers stopped): keep its
+ * cache for a later session if nothing in it is owned or in flight.  The
+ * kept objects leave the session and are not freed with it; a cache kept
+ * earlier and not taken over is freed. */
+static void retain_cache(gfs_ctx* c) {
+    gfs_state& s = c->hs;
+    unsigned long long* d = nullptr;
+    unsigned long long h[2] = {1ull, 0ull};
+    if (cudaMalloc(&d, sizeof h) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    bool ok = cudaMemset(d, 0, sizeof h) == cudaSuccess;
+    if (ok) {
+        k_retain_check<<<152, 256>>>(c->ds, d);
+        ok = cudaGetLastError() == cudaSuccess && cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost) == cudaSuccess;
+    }
+    cudaFree(d);
+    cudaGetLastError();
+    if (!ok || h[0] != 0) return;
+    RetainedCache* r = new RetainedCache();
+    r->device = c->cfg.device;
+    r->log_page = s.log_page;
+    r->n_frames = s.n_frames;
+    r->n_buckets = s.n_buckets;
+    r->n_files = s.n_files;
+    r->pool = s.pool;
+    r->frames = s.frames;
+    r->index = s.index;
+    r->bucket_lock = s.bucket_lock;
+    r->files = s.files;
+    r->dirty_bits = s.dirty_bits;
+    r->pages = h[1];
+    s.pool = nullptr;
+    s.frames = nullptr;
+    s.index = nullptr;
+    s.bucket_lock = nullptr;
+    s.files = nullptr;
+    s.dirty_bits = nullptr;
+    std::lock_guard<std::mutex> lk(g_retained_mu);
+    retained_free(g_retained);
+    g_retained = r;
+}
+
 /* drop clean, unpinned, valid frames: first their index ways, then the frames */
 __global__ void k_drop_ways(gfs_state* S) {
     size_t n = (size_t)S->n_buckets * GFS_WAYS;
@@ -816,18 +923,43 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
          * launched while a file-system kernel waits on the host would stall
          * the driver calls the host workers make */
         gfs__preload_kernels();
-        CK(cudaMalloc(&s.pool, nf * page));
-        CK(cudaMalloc(&s.frames, nf * sizeof(gfs_frame)));
-        CK(cudaMalloc(&s.index, (size_t)s.n_buckets * GFS_WAYS * sizeof(uint32_t)));
-        CK(cudaMemset(s.index, 0, (size_t)s.n_buckets * GFS_WAYS * sizeof(uint32_t)));
-        CK(cudaMalloc(&s.bucket_lock, (size_t)s.n_buckets * sizeof(uint32_t)));
-        CK(cudaMemset(s.bucket_lock, 0, (size_t)s.n_buckets * sizeof(uint32_t)));
-        CK(cudaMalloc(&s.files, (size_t)s.n_files * sizeof(gfs_file)));
-        CK(cudaMemset(s.files, 0, (size_t)s.n_files * sizeof(gfs_file)));
-        CK(cudaMalloc(&s.dirty_bits, ((nf + 31) / 32) * sizeof(uint32_t)));
-        CK(cudaMemset(s.dirty_bits, 0, ((nf + 31) / 32) * sizeof(uint32_t)));
-        k_init_frames<<<256, 256>>>(s.frames, (uint32_t)nf);
-        CK(cudaGetLastError());
+        /* a retained cache of the same geometry is taken over; any other is
+         * freed (a session without GFS_CFG_RETAIN_CACHE frees it too) */
+        RetainedCache* adopt = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(g_retained_mu);
+            if (RetainedCache* r = g_retained) {
+                g_retained = nullptr;
+                if ((cfg.flags & GFS_CFG_RETAIN_CACHE) && r->device == cfg.device && r->log_page == s.log_page &&
+                    r->n_frames == s.n_frames && r->n_buckets == s.n_buckets && r->n_files == s.n_files)
+                    adopt = r;
+                else
+                    retained_free(r);
+            }
+        }
+        if (adopt) {
+            s.pool = adopt->pool;
+            s.frames = adopt->frames;
+            s.index = adopt->index;
+            s.bucket_lock = adopt->bucket_lock;
+            s.files = adopt->files;
+            s.dirty_bits = adopt->dirty_bits;
+            c->retained_pages = adopt->pages;
+            delete adopt;
+        } else {
+            CK(cudaMalloc(&s.pool, nf * page));
+            CK(cudaMalloc(&s.frames, nf * sizeof(gfs_frame)));
+            CK(cudaMalloc(&s.index, (size_t)s.n_buckets * GFS_WAYS * sizeof(uint32_t)));
+            CK(cudaMemset(s.index, 0, (size_t)s.n_buckets * GFS_WAYS * sizeof(uint32_t)));
+            CK(cudaMalloc(&s.bucket_lock, (size_t)s.n_buckets * sizeof(uint32_t)));
+            CK(cudaMemset(s.bucket_lock, 0, (size_t)s.n_buckets * sizeof(uint32_t)));
+            CK(cudaMalloc(&s.files, (size_t)s.n_files * sizeof(gfs_file)));
+            CK(cudaMemset(s.files, 0, (size_t)s.n_files * sizeof(gfs_file)));
+            CK(cudaMalloc(&s.dirty_bits, ((nf + 31) / 32) * sizeof(uint32_t)));
+            CK(cudaMemset(s.dirty_bits, 0, ((nf + 31) / 32) * sizeof(uint32_t)));
+            k_init_frames<<<256, 256>>>(s.frames, (uint32_t)nf);
+            CK(cudaGetLastError());
+        }
         CK(cudaHostAlloc((void**)&c->ring_h, (size_t)cfg.ring_slots * sizeof(gfs_req),
                          cudaHostAllocMapped | cudaHostAllocPortable));
         memset(c->ring_h, 0, (size_t)cfg.ring_slots * sizeof(gfs_req));
@@ -899,6 +1031,7 @@ int gfs_destroy(gfs_ctx* c) {
     for (Worker* w : c->workers)
         if (w->th.joinable()) w->th.join();
     cudaDeviceSynchronize();
+    if ((c->cfg.flags & GFS_CFG_RETAIN_CACHE) && c->ds && c->hs.pool) retain_cache(c);
     for (Worker* w : c->workers) {
         for (cudaEvent_t e : w->ev)
             if (e) cudaEventDestroy(e);
@@ -1072,6 +1205,7 @@ void gfs__preload_runtime() {
     cudaFuncGetAttributes(&a, k_init_frames);
     cudaFuncGetAttributes(&a, k_drop_ways);
     cudaFuncGetAttributes(&a, k_drop_frames);
+    cudaFuncGetAttributes(&a, k_retain_check);
 }
 
 void gfs__preload_kernels() {
@@ -1079,6 +1213,20 @@ void gfs__preload_kernels() {
     gfs__preload_workloads();
     gfs__preload_grep();
     gfs__preload_apps();
+}
+
+long long gfs_retained_pages(gfs_ctx* c) { return c ? (long long)c->retained_pages : -GFS_EINVAL; }
+
+int gfs_release_retained(void) {
+    RetainedCache* r;
+    {
+        std::lock_guard<std::mutex> lk(g_retained_mu);
+        r = g_retained;
+        g_retained = nullptr;
+    }
+    if (!r) return 0;
+    retained_free(r);
+    return 1;
 }
 
 /* Empty the buffer cache (clean, unpinned pages); returns frames kept. */

@@ -43,6 +43,14 @@ typedef struct gfs_config {
 /* gfs_config.flags: read files through pread into pinned staging only, never
  * through a registered mapping of the file (see gfs_create) */
 #define GFS_CFG_NO_FILE_MAP 1u
+/* gfs_config.flags: keep the buffer cache in HBM when the session ends, for
+ * the next session of this process with the same page size, pool, file-table
+ * size and device.  Kept only if every file is closed and every page clean
+ * and unpinned at gfs_destroy.  Cross-session counterpart of the reopen
+ * check of libgpufs/fs_calls.cu:197-218: a file's first open in the new
+ * session compares the host's ctime and size with those its cached pages
+ * belong to and drops the pages if they differ. */
+#define GFS_CFG_RETAIN_CACHE 2u
 
 #define GFS_NSTATS 21
 /* gfs_get_stats order: device hits(page accesses), misses, evictions,
@@ -83,6 +91,13 @@ int gfs_reset_stats(gfs_ctx* ctx);
 /* empty the buffer cache of clean, unpinned pages (no kernel may be running);
  * returns the number of frames kept (pinned or dirty) */
 long long gfs_drop_cache(gfs_ctx* ctx);
+/* valid pages this session took over at gfs_create from a cache an earlier
+ * session retained (GFS_CFG_RETAIN_CACHE); 0 if it started empty */
+long long gfs_retained_pages(gfs_ctx* ctx);
+/* free a retained cache that no session has taken over (gfs_create without
+ * GFS_CFG_RETAIN_CACHE, or with another geometry, frees it too); returns 1
+ * if one was freed, 0 if none was kept */
+int gfs_release_retained(void);
 /* pinned host<->device cudaMemcpyAsync bandwidth, best of `reps` (GB/s) */
 int gfs_measure_link(uint64_t bytes, int reps, float* h2d_gbs, float* d2h_gbs);
 /* Cold-read ceilings for one file of at least 1 MiB (GB/s, best of reps; no
