@@ -718,7 +718,7 @@ void gfs__preload_runtime();
 /* A buffer cache kept in HBM after its session ended (GFS_CFG_RETAIN_CACHE)
  * for the next session of this process with the same geometry: page pool,
  * frames, page index and file table, every page clean and unpinned and
- * every file closed.  File slots keep their names, generations and the
+ * every file closed, and the session's registered file mappings.  File slots keep their names, generations and the
  * ctime and size their pages belong to, so the next session's first open of
  * a file compares those with the host's reply, as a reopen within a session
  * does (the version check of fs_calls.cu:197-218), and drops the pages of a
@@ -733,6 +733,11 @@ struct RetainedCache {
     gfs_file* files = nullptr;
     uint32_t* dirty_bits = nullptr;
     unsigned long long pages = 0; /* valid pages */
+    /* the registered file mappings, none in use (keyed by file identity and
+     * ctime, so a changed file is never served from an old one) */
+    std::unordered_multimap<uint64_t, FileMap*> maps;
+    size_t mapped_bytes = 0;
+    uint64_t map_clock = 0;
 };
 static std::mutex g_retained_mu;
 static RetainedCache* g_retained = nullptr; /* under g_retained_mu */
@@ -748,6 +753,7 @@ static void retained_free(RetainedCache* r) {
     cudaFree(r->bucket_lock);
     cudaFree(r->files);
     cudaFree(r->dirty_bits);
+    for (auto& e : r->maps) map_release(e.second);
     if (cur >= 0) cudaSetDevice(cur);
     cudaGetLastError();
     delete r;
@@ -810,6 +816,20 @@ static void retain_cache(gfs_ctx* c) {
     r->files = s.files;
     r->dirty_bits = s.dirty_bits;
     r->pages = h[1];
+    {
+        std::lock_guard<std::mutex> lk(c->map_mu);
+        for (auto& e : c->maps) {
+            if (e.second->refs == 0) {
+                r->maps.emplace(e.first, e.second);
+                r->mapped_bytes += e.second->len;
+            } else {
+                map_release(e.second);
+            }
+        }
+        c->maps.clear();
+        c->mapped_bytes = 0;
+        r->map_clock = c->map_clock;
+    }
     s.pool = nullptr;
     s.frames = nullptr;
     s.index = nullptr;
@@ -945,6 +965,9 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
             s.files = adopt->files;
             s.dirty_bits = adopt->dirty_bits;
             c->retained_pages = adopt->pages;
+            c->maps.swap(adopt->maps);
+            c->mapped_bytes = adopt->mapped_bytes;
+            c->map_clock = adopt->map_clock;
             delete adopt;
         } else {
             CK(cudaMalloc(&s.pool, nf * page));
