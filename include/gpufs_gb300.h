@@ -45,8 +45,9 @@ typedef struct gfs_config {
 #define GFS_CFG_NO_FILE_MAP 1u
 /* gfs_config.flags: keep the buffer cache in HBM when the session ends, for
  * the next session of this process with the same page size, pool, file-table
- * size and device.  Kept only if every file is closed and every page clean
- * and unpinned at gfs_destroy.  Cross-session counterpart of the reopen
+ * size and device, together with the session's registered file mappings.
+ * Kept only if every file is closed and every page clean and unpinned at
+ * gfs_destroy.  Cross-session counterpart of the reopen
  * check of libgpufs/fs_calls.cu:197-218: a file's first open in the new
  * session compares the host's ctime and size with those its cached pages
  * belong to and drops the pages if they differ. */
