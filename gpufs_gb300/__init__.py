@@ -8,6 +8,7 @@ every entry point raises if the native library is missing.
 """
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -180,6 +181,7 @@ class Session:
         _check(L.gfs_create(ctypes.byref(c), ctypes.byref(h)), "gfs_create")
         self._h = h
         self.L = L
+        self._children = weakref.WeakSet()  # open Grep plans and Servers of this session
         self.page_size = L.gfs_page_size(h)
         self.n_frames = L.gfs_num_frames(h)
         # valid pages taken over from a cache an earlier session retained
@@ -190,7 +192,15 @@ class Session:
         return self._h
 
     def close(self):
-        if self._h:
+        """Close the session's open Grep plans and Servers (their files and
+        device memory belong to it), then end the session."""
+        if not self._h:
+            return
+        try:
+            for ch in list(self._children):
+                ch.close()
+        finally:
+            self._children.clear()
             self.L.gfs_destroy(self._h)
             self._h = None
 
@@ -317,6 +327,7 @@ class Grep:
         _check(sess.L.gfs_grep_open(sess.handle, _p(dict_path), _paths(self.paths), len(self.paths),
                                     ctypes.byref(h)), "gfs_grep_open")
         self._h = h
+        sess._children.add(self)
         self._info()
 
     def _info(self):
@@ -368,9 +379,10 @@ class Grep:
 
     def close(self):
         if self._h:
-            rc = self.s.L.gfs_grep_close(self._h)
-            self._h = None
-            _check(rc, "gfs_grep_close")
+            h, self._h = self._h, None
+            self.s._children.discard(self)
+            if self.s.handle:  # after the session has ended there is nothing left to close
+                _check(self.s.L.gfs_grep_close(h), "gfs_grep_close")
 
     def __enter__(self):
         return self
@@ -427,6 +439,7 @@ class Server:
         _check(sess.L.gfs_serve_open(sess.handle, _p(dict_path), _paths(self.paths), len(self.paths), outs,
                                      len(self.out_paths), ctypes.byref(h)), "gfs_serve_open")
         self._h = h
+        sess._children.add(self)
 
     def run(self, reqs, inflight_pages=1 << 62, warps_per_sm=8):
         """reqs: SERVE_REQ array sorted by arrival_ns.  Returns a SERVE_RES array."""
@@ -439,9 +452,10 @@ class Server:
 
     def close(self):
         if self._h:
-            rc = self.s.L.gfs_serve_close(self._h)
-            self._h = None
-            _check(rc, "gfs_serve_close")
+            h, self._h = self._h, None
+            self.s._children.discard(self)
+            if self.s.handle:  # after the session has ended there is nothing left to close
+                _check(self.s.L.gfs_serve_close(h), "gfs_serve_close")
 
     def __enter__(self):
         return self
