@@ -1,7 +1,9 @@
 """Host logic of the benchmark (CPU only): the served workload's request
 trace has the stated op mix, popularity skew and alignment, writes go to
 disjoint regions of the output files, the byte accounting clamps at end of
-file, and the max-over-ranks helper is the identity on one rank."""
+file, the max-over-ranks helper is the identity on one rank, and the
+reference arm (a CPU path) prints the contract's JSON line."""
+import json
 import os
 import sys
 
@@ -67,3 +69,31 @@ def test_served_bytes_clamp_at_end_of_file():
 
 def test_allmax_single_rank():
     assert bench.allmax(None, 3.5) == 3.5
+
+
+def test_reference_arm_prints_the_contract_line(built, tmp_path, monkeypatch, capsys):
+    from gpufs_gb300 import datagen
+
+    def small_corpus(d, total=None):
+        return datagen.grep_corpus(str(tmp_path / "c"), bench.N_FILES, bench.N_FILES * (40 << 10), n_vocab=2000,
+                                   n_dict=300, seed=9)
+
+    monkeypatch.setattr(bench, "make_data", small_corpus)
+
+    class Args:
+        steps, warmup, gpus = 2, 3, 1
+
+    bench.run_reference(Args(), 0, 1, None, str(tmp_path))
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e", "gpu_launches"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == "GB/s"
+    assert line["value"] > 0 and line["steps"] == 2 and line["warmup"] == 3 and line["higher_is_better"] is True
+    assert line["config"]["sample_bytes"] == bench.N_FILES * (32 << 10)
+    cb = line["cpu_baseline"]
+    assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == line["value"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    assert line["gpu_launches"] == 0
+
