@@ -1,8 +1,10 @@
 """Host logic of the benchmark (CPU only): the served workload's request
 trace has the stated op mix, popularity skew and alignment, writes go to
 disjoint regions of the output files, the byte accounting clamps at end of
-file, the max-over-ranks helper is the identity on one rank, and the
-reference arm (a CPU path) prints the contract's JSON line."""
+file, the max-over-ranks helper is the identity on one rank, the reference
+arm (a CPU path) prints the contract's JSON line, and the nvidia-smi clock
+samples reduce to the median SM clock, the maximum and the active throttle
+reasons."""
 import json
 import os
 import sys
@@ -97,3 +99,37 @@ def test_reference_arm_prints_the_contract_line(built, tmp_path, monkeypatch, ca
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert line["gpu_launches"] == 0
 
+
+
+class _DoneProc:
+    def poll(self):
+        return 0
+
+    def terminate(self):
+        pass
+
+    def kill(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+
+def test_clock_samples_give_median_max_and_active_reasons():
+    c = bench.Clocks(0)
+    c.f.write("0, 2070, 2070, 812.1, 0x0, Not Active, Not Active, Not Active, Not Active\n"
+              "0, 1965, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, Active\n"
+              "0, 2025, 2070, 1210.7, 0x0, Not Active, Not Active, Not Active, Not Active\n"
+              "0, [N/A], [N/A], [N/A], [N/A], [N/A], [N/A], [N/A], [N/A]\n"
+              "garbage line\n")
+    c.p = _DoneProc()
+    got = c.stop()
+    assert got == {"sm_mhz": 2025.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 4}
+    assert not os.path.exists(c.f.name)
+
+
+def test_clock_reasons_name_thermal_and_hw_slowdowns():
+    c = bench.Clocks(0)
+    c.f.write("0, 1500, 2070, 900, 0x48, Active, Not Active, Active, Not Active\n")
+    c.p = _DoneProc()
+    assert c.stop()["reasons"] == ["hw_slowdown", "sw_thermal_slowdown"]
