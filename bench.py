@@ -23,7 +23,6 @@ a time, all host threads) on a bounded sample of the same corpus.
 import argparse
 import atexit
 import json
-import re
 import os
 import statistics
 import subprocess
@@ -165,14 +164,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
+# DRAM bytes (read + write) per corpus byte of the resident scan kernel, from
+# one ncu capture of the 256 MiB corpus (profiles/k_grep_scan_grep_text_256MiB.md:
+# dram__bytes_read.sum + dram__bytes_write.sum over the corpus bytes).  Every
+# page is read once, so the traffic scales with the corpus.
+SCAN_DRAM_BYTES_PER_CORPUS_BYTE = 1.0419
+
+
 def traffic_per_byte():
-    """DRAM bytes per corpus byte of the scan kernel, read from the committed
-    ncu summary (the `dram_bytes_per_corpus_byte` row)."""
-    p = os.path.join(ROOT, "profiles", "k_grep_scan_grep_text_256MiB.md")
-    if not os.path.exists(p):
-        return None
-    m = re.search(r"dram_bytes_per_corpus_byte\*\*\s*\|\s*\*\*([0-9.]+)", open(p).read())
-    return float(m.group(1)) if m else None
+    return SCAN_DRAM_BYTES_PER_CORPUS_BYTE
 
 
 def cpu_threads():

@@ -517,11 +517,21 @@ static __device__ __align__(256) unsigned char g_xxh64_scratch[XN_BYTES];
 unsigned char* g_xxh64_scratch_addr[XN_MAX_DEVICES];
 std::mutex g_xxh64_scratch_mu;
 
-/* device address of g_xxh64_scratch on the current device (set-up on first use) */
-int xxh64_scratch(unsigned char** out) {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= XN_MAX_DEVICES) return -GFS_EIO;
+/* device address of g_xxh64_scratch on device `dev`, which the caller has
+ * made current (set-up on first use on a device).  A cached address is
+ * checked against the driver's view of that device's memory on every call
+ * (no allocation), so after a device reset it is looked up again. */
+int xxh64_scratch(int dev, unsigned char** out) {
+    if (dev < 0 || dev >= XN_MAX_DEVICES) return -GFS_EIO;
     std::lock_guard<std::mutex> lk(g_xxh64_scratch_mu);
+    if (g_xxh64_scratch_addr[dev]) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, g_xxh64_scratch_addr[dev]) != cudaSuccess || a.type != cudaMemoryTypeDevice ||
+            a.device != dev) {
+            cudaGetLastError();
+            g_xxh64_scratch_addr[dev] = nullptr;
+        }
+    }
     if (!g_xxh64_scratch_addr[dev]) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_xxh64_scratch);
@@ -538,6 +548,9 @@ int xxh64_scratch(unsigned char** out) {
 
 } /* namespace */
 
+static int xxh64_noalloc_on_device(gfs_ctx* ctx, int dev, const char* const* paths, int n,
+                                   unsigned long long* host_out);
+
 extern "C" int gfs_xxh64_files_noalloc(gfs_ctx* ctx, const char* const* paths, int n, unsigned long long* host_out) {
     if (n < 1 || !paths || !host_out) return -GFS_EINVAL;
     if (n > GFS_XXH64_NOALLOC_MAX_FILES) {
@@ -547,9 +560,22 @@ extern "C" int gfs_xxh64_files_noalloc(gfs_ctx* ctx, const char* const* paths, i
     }
     for (int i = 0; i < n; i++)
         if (!paths[i] || strlen(paths[i]) >= GFS_NAME_MAX) return -GFS_EINVAL;
+    /* the session's device is current for the call (its stream and the
+     * scratch address belong to it); the caller's device comes back after */
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return -GFS_EIO;
+    const int dev = gfs__device(ctx);
+    if (prev != dev && cudaSetDevice(dev) != cudaSuccess) return -GFS_EIO;
+    const int rc = xxh64_noalloc_on_device(ctx, dev, paths, n, host_out);
+    if (prev != dev) cudaSetDevice(prev);
+    return rc;
+}
+
+static int xxh64_noalloc_on_device(gfs_ctx* ctx, int dev, const char* const* paths, int n,
+                                   unsigned long long* host_out) {
     if (gfs__activate(ctx)) return -GFS_EIO;
     unsigned char* base = nullptr;
-    int rc = xxh64_scratch(&base);
+    int rc = xxh64_scratch(dev, &base);
     if (rc) return rc;
     char* names = (char*)base;
     uint64_t* sizes = (uint64_t*)(base + XN_SIZES);

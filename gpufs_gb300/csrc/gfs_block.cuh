@@ -59,6 +59,7 @@ __device__ __forceinline__ void blk_copy_round(gfs_state* S, const int* frames, 
     if (end <= pos) return;
     const uint64_t pmask = (1ull << lp) - 1u;
     const uintptr_t delta = (uintptr_t)ubuf - (uintptr_t)ubase; /* user address of file offset x: delta + x */
+    const bool ug = __isGlobal(ubuf) != 0; /* the user buffer may be a block's shared memory */
     if ((delta & 15u) == 0u) {
         /* frame and buffer agree mod 16 (frames are page-aligned): the whole
          * block sweeps the round as one stream of 16-byte units, consecutive
@@ -101,7 +102,7 @@ __device__ __forceinline__ void blk_copy_round(gfs_state* S, const int* frames, 
             uint4 v[4];
             if (to_frame) {
 #pragma unroll
-                for (int k = 0; k < 4; k++) v[k] = ld_cg4(up[k]);
+                for (int k = 0; k < 4; k++) v[k] = ld_user4(up[k], ug);
 #pragma unroll
                 for (int k = 0; k < 4; k++) *fp[k] = v[k];
             } else {
@@ -115,7 +116,7 @@ __device__ __forceinline__ void blk_copy_round(gfs_state* S, const int* frames, 
             const uint64_t x = u << 4;
             uint4* f = (uint4*)(frame_data(S, (uint32_t)frames[(uint32_t)(x >> lp) - first]) + (x & pmask));
             uint4* up = (uint4*)(delta + x);
-            if (to_frame) *f = ld_cg4(up);
+            if (to_frame) *f = ld_user4(up, ug);
             else *up = ld_cg4(f);
         }
         return;

@@ -127,6 +127,12 @@ __device__ __forceinline__ uint4 ld_cg4(const void* p) {
                  : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
     return v;
 }
+/* 16 bytes of a caller's buffer: cache-global when it is global memory, a
+ * generic load otherwise (a block's shared-memory buffer; global-space
+ * loads of a shared address are an error) */
+__device__ __forceinline__ uint4 ld_user4(const void* p, bool global) {
+    return global ? ld_cg4(p) : *(const uint4*)p;
+}
 
 /* Bounded wait: exponential back-off with __nanosleep, deadline on the
  * global timer.  tick() returns false once the deadline has passed. */
@@ -851,6 +857,7 @@ __device__ __forceinline__ int file_close_finish(gfs_state* S, int fd) {
  * copy_block_16, util.cu.h:161-236, used ld.cv/st.wt for the same job). */
 __device__ __forceinline__ void warp_copy(uint8_t* dst, const uint8_t* src, size_t n, int lane) {
     uintptr_t d = (uintptr_t)dst, s = (uintptr_t)src;
+    const bool sg = __isGlobal(src) != 0; /* a user buffer may be in shared memory */
     if (((d ^ s) & 15u) == 0u) {
         size_t head = (16u - (s & 15u)) & 15u;
         if (head > n) head = n;
@@ -860,10 +867,11 @@ __device__ __forceinline__ void warp_copy(uint8_t* dst, const uint8_t* src, size
         const uint4* s4 = (const uint4*)(src + head);
         size_t i = (size_t)lane;
         for (; i + 96 < n4; i += 128) {
-            uint4 a = ld_cg4(s4 + i), b = ld_cg4(s4 + i + 32), c = ld_cg4(s4 + i + 64), e = ld_cg4(s4 + i + 96);
+            uint4 a = ld_user4(s4 + i, sg), b = ld_user4(s4 + i + 32, sg), c = ld_user4(s4 + i + 64, sg),
+                  e = ld_user4(s4 + i + 96, sg);
             d4[i] = a; d4[i + 32] = b; d4[i + 64] = c; d4[i + 96] = e;
         }
-        for (; i < n4; i += 32) d4[i] = ld_cg4(s4 + i);
+        for (; i < n4; i += 32) d4[i] = ld_user4(s4 + i, sg);
         size_t t0 = head + (n4 << 4);
         for (size_t k = t0 + (size_t)lane; k < n; k += 32) dst[k] = src[k];
     } else if (((d ^ s) & 3u) == 0u) {
@@ -873,7 +881,7 @@ __device__ __forceinline__ void warp_copy(uint8_t* dst, const uint8_t* src, size
         size_t n1 = (n - head) >> 2;
         uint32_t* d1 = (uint32_t*)(dst + head);
         const uint32_t* s1 = (const uint32_t*)(src + head);
-        for (size_t i = (size_t)lane; i < n1; i += 32) d1[i] = __ldcg(s1 + i);
+        for (size_t i = (size_t)lane; i < n1; i += 32) d1[i] = sg ? __ldcg(s1 + i) : s1[i];
         for (size_t k = head + (n1 << 2) + (size_t)lane; k < n; k += 32) dst[k] = src[k];
     } else {
         for (size_t k = (size_t)lane; k < n; k += 32) dst[k] = src[k];

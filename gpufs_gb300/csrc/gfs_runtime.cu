@@ -1099,6 +1099,8 @@ int gfs_destroy(gfs_ctx* c) {
 
 void* gfs_kernel_stream(gfs_ctx* c) { return (void*)c->kstream; }
 unsigned long long gfs__timeout_ns(gfs_ctx* c) { return c->cfg.timeout_ns; }
+uint32_t gfs__config_flags(gfs_ctx* c) { return c->cfg.flags; }
+int gfs__device(gfs_ctx* c) { return c->cfg.device; }
 void* gfs_device_state(gfs_ctx* c) { return (void*)c->ds; }
 uint32_t gfs_page_size(gfs_ctx* c) { return c->hs.page_size; }
 uint32_t gfs_num_frames(gfs_ctx* c) { return c->hs.n_frames; }

@@ -26,6 +26,9 @@ int gfs__slot_map(gfs_ctx* c, uint32_t slot, unsigned long long* dev_addr, unsig
 int gfs__activate(gfs_ctx* c);
 /* the session's bound on device-side waits (ns) */
 unsigned long long gfs__timeout_ns(gfs_ctx* c);
+/* the session's GFS_CFG_* flags and CUDA device */
+uint32_t gfs__config_flags(gfs_ctx* c);
+int gfs__device(gfs_ctx* c);
 void gfs__preload_kernels(void);
 void gfs__preload_runtime(void);
 void gfs__preload_workloads(void);

@@ -175,8 +175,12 @@ int gfs_xxh64_files(gfs_ctx* ctx, const char* const* paths, int n, unsigned long
  * no cudaMalloc/cudaFree or other allocation.  At most
  * GFS_XXH64_NOALLOC_MAX_FILES files per call, else -GFS_E2BIG.  The first
  * call on a device looks the array's address up (cudaGetSymbolAddress): make
- * it before any stream capture.  The array is shared by all callers on a
- * device, so overlapping calls on one device race: serialise them. */
+ * it before any stream capture.  The array is 90,368 bytes on every device
+ * that loads the library, held until exit.  The call runs on the session's
+ * device (made current for its duration, the caller's device restored
+ * after); a device reset makes the next call look the address up again.
+ * The array is shared by all callers on a device, so overlapping calls on
+ * one device race: serialise them. */
 #define GFS_XXH64_NOALLOC_MAX_FILES 1024
 int gfs_xxh64_files_noalloc(gfs_ctx* ctx, const char* const* paths, int n, unsigned long long* host_out);
 

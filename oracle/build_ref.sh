@@ -9,9 +9,17 @@
 #                   C file is kept beside it so a machine without the
 #                   reference tree can recompile it (it stays git-ignored).
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#        oracle/build_ref.sh --print-root    (prints where the tree is looked for)
+# The root is the argument, else $GPUFS_REFERENCE, else /root/reference (the
+# read-only copy of the reference tree on the build machine; it is absent
+# where the tests run on a GPU, which need none of it).
 set -eu
-REF=${1:-/root/reference}
+if [ "${1:-}" = "--print-root" ]; then
+  echo "${GPUFS_REFERENCE:-/root/reference}"
+  exit 0
+fi
+REF=${1:-${GPUFS_REFERENCE:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 SRC="$REF/samples/grep_text/grep_text_gpu.cu"

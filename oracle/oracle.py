@@ -13,7 +13,19 @@ SO = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SRC = os.path.join(REF_DIR, "ref_match_string.c")
 REF_SO = os.path.join(REF_DIR, "libref_grep.so")
-REFERENCE_ROOT = "/root/reference"
+_ROOT = None
+
+
+def reference_root():
+    """Where the reference source tree is looked for: $GPUFS_REFERENCE, else
+    the default of the build recipe (oracle/build_ref.sh).  It may be absent
+    (machines that run the GPU tests have none); callers check."""
+    global _ROOT
+    if _ROOT is None:
+        _ROOT = os.environ.get("GPUFS_REFERENCE") or subprocess.run(
+            ["sh", os.path.join(HERE, "build_ref.sh"), "--print-root"], stdout=subprocess.PIPE,
+            text=True, check=True).stdout.strip()
+    return _ROOT
 
 
 def build():
@@ -21,8 +33,8 @@ def build():
     src = os.path.join(HERE, "oracle.c")
     if not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(src):
         subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-pthread", "-o", SO, src])
-    if not os.path.exists(REF_SRC) and os.path.isdir(REFERENCE_ROOT):
-        subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT])
+    if not os.path.exists(REF_SRC) and os.path.isdir(reference_root()):
+        subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), reference_root()])
     if os.path.exists(REF_SRC) and (not os.path.exists(REF_SO) or os.path.getmtime(REF_SO) < os.path.getmtime(REF_SRC)):
         subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-pthread", "-o", REF_SO, REF_SRC])
 

@@ -5,6 +5,10 @@
       samples/grep_text/input/pg100.txt.small), computed by the faithful
       oracle whose matcher is pinned to the reference's match_string; only the
       total and an XXH64 digest of the count matrix are stored.
+  ref_dict_4000.gpu, ref_pg100_small.txt  those two inputs, copied byte for
+      byte from the reference tree (the dictionary cut to its first 4000
+      records), so the GPU tests can run the scan on them where the
+      reference tree is absent.
   datagen_golden.json  XXH64 digests of small seeded inputs from the
       workload generator, and the faithful grep counts over them.
 
@@ -57,12 +61,16 @@ def main():
         g = datagen_case(d)
     with open(os.path.join(HERE, "datagen_golden.json"), "w") as f:
         json.dump(g, f, indent=1)
-    root = oracle.REFERENCE_ROOT
+    root = oracle.reference_root()
     dpath = os.path.join(root, "samples/grep_text/input/dict.gpu")
     tpath = os.path.join(root, "samples/grep_text/input/pg100.txt.small")
     if os.path.exists(dpath):
         recs = open(dpath, "rb").read()[:32 * 4000]
         text = open(tpath, "rb").read()
+        with open(os.path.join(HERE, "ref_dict_4000.gpu"), "wb") as f:
+            f.write(recs)
+        with open(os.path.join(HERE, "ref_pg100_small.txt"), "wb") as f:
+            f.write(text)
         c = oracle.grep_counts(recs, [text], mode="faithful")
         with open(os.path.join(HERE, "reference_fixture_counts.json"), "w") as f:
             json.dump({"records": 4000, "total": int(c.sum()),

@@ -1,5 +1,5 @@
-"""A plain C host program over the C ABI (the way INTEGRATION.md shows it,
-and the way a cgo / JNI / ctypes binding would call it) compiles as C11
+"""A plain C host program over the C ABI (the way a cgo / JNI / ctypes
+binding would call it) compiles as C11
 against include/gpufs_gb300.h with warnings as errors and links against
 libgpufs_gb300.so.  CPU only: nothing is run."""
 import os

@@ -255,3 +255,28 @@ def test_batched_counts_and_xxh64(built, shm_dir, n_ctas, pool_mb):
         if pool_mb < 8:
             assert s.stats()["evictions"] > 0
         assert s.last_error() == 0
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_reference_fixture_inputs(built):
+    """The reference's own grep inputs (the first 4000 records of
+    samples/grep_text/input/dict.gpu over samples/grep_text/input/pg100.txt.small,
+    copied into tests/golden by make_golden.py): the cold, resident and
+    direct scans give the committed digest of the oracle pinned to the
+    reference's match_string."""
+    import json
+    dpath = os.path.join(GOLDEN, "ref_dict_4000.gpu")
+    tpath = os.path.join(GOLDEN, "ref_pg100_small.txt")
+    with open(os.path.join(GOLDEN, "reference_fixture_counts.json")) as f:
+        want = json.load(f)
+    for lp in (12, 16):
+        with g.Session(log_page=lp, pool_bytes=64 << 20, timeout_s=20) as s:
+            with g.Grep(s, dpath, [tpath]) as gr:
+                for direct in (False, False, True):
+                    gr.run(0, direct=direct)
+                    got = gr.counts()
+                    assert int(got.sum()) == want["total"]
+                    assert oracle.xxh64(got.astype("<u4").tobytes()) == int(want["xxh64"], 16)
+            assert s.last_error() == 0

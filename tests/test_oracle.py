@@ -146,7 +146,7 @@ def test_reference_fixture_counts(built):
     """The reference's own inputs (dict.gpu x pg100.txt.small): the fast
     oracle equals the faithful walk whose matcher is pinned to the reference
     code; the digest is committed so the result cannot drift."""
-    root = oracle.REFERENCE_ROOT
+    root = oracle.reference_root()
     d = os.path.join(root, "samples/grep_text/input/dict.gpu")
     t = os.path.join(root, "samples/grep_text/input/pg100.txt.small")
     if not (os.path.exists(d) and os.path.exists(t)):

@@ -17,7 +17,9 @@ import pytest
 
 from gpufs_gb300 import build as gbuild
 
-REF = os.environ.get("GPUFS_REFERENCE", "/root/reference")
+from oracle import oracle
+
+REF = oracle.reference_root()
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SAMPLES = ["memcopy/cp.cu", "grep_text/fs.cu", "bigmatrix_mmap/fs.cu"]
 
