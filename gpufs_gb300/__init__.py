@@ -40,6 +40,7 @@ ERR_TIMEOUT, ERR_IO, ERR_NOMEM, ERR_TABLE, ERR_ARG = 1, 2, 4, 8, 16
 XXH64_NOALLOC_MAX_FILES = 1024  # GFS_XXH64_NOALLOC_MAX_FILES
 CFG_NO_FILE_MAP = 1  # GFS_CFG_NO_FILE_MAP
 CFG_RETAIN_CACHE = 2  # GFS_CFG_RETAIN_CACHE
+CFG_HOST_TABLE = 4  # GFS_CFG_HOST_TABLE
 
 
 class Config(ctypes.Structure):
@@ -160,11 +161,12 @@ class Session:
     """One file-system session on one GPU (initializer() .. delete GPUGlobals)."""
 
     def __init__(self, log_page=16, pool_bytes=2 << 30, max_files=1024, ring_slots=4096, host_workers=8,
-                 staging_depth=8, timeout_s=30.0, device=0, file_map=True, retain_cache=False):
+                 staging_depth=8, timeout_s=30.0, device=0, file_map=True, retain_cache=False, host_table=False):
         """retain_cache: keep the buffer cache in HBM when the session closes,
         for the next session of this process with the same log_page,
         pool_bytes, max_files and device (kept only if every file is closed
-        and every page clean); see retained_pages."""
+        and every page clean); see retained_pages.  host_table: build grep
+        dictionary tables on the host (the device build's fallback)."""
         L = lib()
         c = Config()
         L.gfs_default_config(ctypes.byref(c))
@@ -174,7 +176,8 @@ class Session:
         c.ring_slots = ring_slots
         c.host_workers = host_workers
         c.staging_depth = staging_depth
-        c.flags = (0 if file_map else CFG_NO_FILE_MAP) | (CFG_RETAIN_CACHE if retain_cache else 0)
+        c.flags = ((0 if file_map else CFG_NO_FILE_MAP) | (CFG_RETAIN_CACHE if retain_cache else 0) |
+                   (CFG_HOST_TABLE if host_table else 0))
         c.timeout_ns = int(timeout_s * 1e9)
         c.device = device
         h = ctypes.c_void_p()
@@ -333,7 +336,7 @@ class Grep:
     def _info(self):
         info = (ctypes.c_longlong * 10)()
         self.s.L.gfs_grep_info(self._h, info, 10)
-        (self.n_words, self.n_files, self.buckets, self.smem_table, self.smem_bytes, self.chunks, self.status,
+        (self.n_words, self.n_files, self.slots, self.smem_table, self.smem_bytes, self.chunks, self.status,
          self.status_site, self.build_us, self.open_us) = [int(v) for v in info]
 
     def run(self, n_ctas=0, direct=False):

@@ -32,6 +32,7 @@
  * for flagged files only, so counts equal the reference on any input.
  */
 #include <cuda_runtime.h>
+#include <cooperative_groups.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
@@ -78,11 +79,14 @@ struct GrepDev {
     const uint64_t* sizes;
     const uint64_t* chunk_prefix; /* n_files + 1, in GR_CH chunks */
     uint64_t total_chunks;
-    uint32_t nb;                  /* buckets */
-    const uint16_t* tags;         /* nb * 4 slot tags (grep_tag), 0 = empty */
-    const uint4* rec_lo;          /* nb * 4: bytes 0..15 of each slot's record */
-    const uint4* rec_hi;          /* nb * 4: bytes 16..31 (separate, so the short-word
-                                     probes touch half the bytes) */
+    uint32_t m;                   /* table slots */
+    uint32_t r;                   /* displacement buckets */
+    grep_hashk hk;                /* seeded key-mix multipliers */
+    const uint16_t* tags;         /* m slot tags (grep_tag), 0 = empty */
+    const uint16_t* disp;         /* r displacements */
+    const uint4* rec_lo;          /* m: bytes 0..15 of each slot's record */
+    const uint4* rec_hi;          /* m: bytes 16..31 (separate, so the short-word
+                                     checks touch half the bytes) */
     const uint32_t* slot_word;    /* first record of each slot, ~0 if empty */
     const int32_t* next_dup;      /* next record with the same word, -1 */
     uint32_t* counts;             /* n_words x n_files */
@@ -97,6 +101,14 @@ struct GrepDev {
      * the SMs, bypassing the buffer cache */
     const uint64_t* maps;         /* per file: device address of its host mapping, 0 if none */
 };
+
+/* Shared-memory bytes of the table's parts (each a multiple of 128); the
+ * plan's global tags and displacements are padded to the same sizes.  The
+ * counters have 32 spare entries past the m slots (one per lane; see
+ * CountSink::hit_if). */
+__host__ __device__ __forceinline__ uint32_t grep_tag_smem(uint32_t m) { return (2u * m + 127u) & ~127u; }
+__host__ __device__ __forceinline__ uint32_t grep_disp_smem(uint32_t r) { return (2u * r + 127u) & ~127u; }
+__host__ __device__ __forceinline__ uint32_t grep_cnt_smem(uint32_t m) { return (4u * (m + 32u) + 127u) & ~127u; }
 
 namespace {
 
@@ -199,13 +211,27 @@ __device__ __forceinline__ bool rec_equal(const GrepDev& P, uint32_t slot, bool 
     return eq;
 }
 
-/* The dictionary table a scan works with: slot tags, and (table in shared
- * memory) one 32-bit counter per slot for the current file.  Without shared
- * memory counts go straight to the global count matrix. */
+/* The dictionary table a scan works with: slot tags and displacements
+ * (shared memory, or the plan's global copy), and (table in shared memory)
+ * one 32-bit counter per slot for the current file.  Without shared memory
+ * counts go straight to the global count matrix. */
 struct Tbl {
     const uint16_t* tags;
+    const uint16_t* disp;
     uint32_t* cnt;
 };
+
+/* The slot a hash selects: its bucket's displacement, then the slot mix. */
+template <bool SMEM>
+__device__ __forceinline__ uint32_t tbl_slot(const GrepDev& P, const Tbl& t, uint32_t h) {
+    const uint32_t b = grep_bucket(h, P.r);
+    const uint32_t d = SMEM ? (uint32_t)t.disp[b] : (uint32_t)__ldg(t.disp + b);
+    return grep_slot(h, d, P.m);
+}
+template <bool SMEM>
+__device__ __forceinline__ uint32_t tbl_tag(const Tbl& t, uint32_t slot) {
+    return SMEM ? (uint32_t)t.tags[slot] : (uint32_t)__ldg(t.tags + slot);
+}
 
 /* A slot counter holds one CTA's count of one word in one file, which the
  * uint32 count matrix bounds anyway: a plain add, no overflow check. */
@@ -223,29 +249,30 @@ struct CountSink {
     bool smem;
     int f;
     __device__ __forceinline__ void hit(uint32_t slot) const { count_hit(P, t, smem, slot, f); }
+    /* counts slot if h; with the table in shared memory a miss adds to the
+     * lane's own spare counter past the table's m (never flushed), so the
+     * add needs no branch */
+    __device__ __forceinline__ void hit_if(bool h, uint32_t slot) const {
+        if (smem) atomicAdd(&t.cnt[h ? slot : P.m + (threadIdx.x & 31u)], 1u);
+        else if (h) flush_slot(P, slot, 1u, f);
+    }
     __device__ __forceinline__ void long_run() const { atomicOr(&P.long_flags[f], 1u); }
 };
 struct TotalSink {
     uint32_t n = 0;
     __device__ __forceinline__ void hit(uint32_t) { n++; }
+    __device__ __forceinline__ void hit_if(bool h, uint32_t) { n += h ? 1u : 0u; }
     __device__ __forceinline__ void long_run() {}
 };
 
-/* Slow, general lookup: every tag match in both buckets is verified. */
-template <class Sink>
+/* General lookup of a key of any length 1..32: the one slot its hash
+ * selects, its tag, then the record. */
+template <bool SMEM, class Sink>
 __device__ void lookup_hit(const GrepDev& P, const Tbl& t, const uint32_t k[8], uint32_t len, Sink& sink) {
-    const uint32_t h1 = grep_h1(grep_mix(k, (int)len));
-    const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h1, P.nb), tag = grep_tag(h1, (int)len);
-    const uint32_t bs[2] = {b1, b2};
-    for (int r = 0; r < (b2 == b1 ? 1 : 2); r++)
-        for (int i = 0; i < 4; i++) {
-            const uint32_t slot = 4u * bs[r] + (uint32_t)i;
-            const uint32_t tg = t.tags[slot];
-            if (tg != tag) continue;
-            if (!rec_equal(P, slot, (tg & GREP_TAG_LONG) != 0u, k, len)) continue;
-            sink.hit(slot);
-            return;
-        }
+    const uint32_t h = grep_h1(grep_mix(&P.hk, k, (int)len));
+    const uint32_t slot = tbl_slot<SMEM>(P, t, h);
+    const uint32_t tg = tbl_tag<SMEM>(t, slot);
+    if (tg == grep_tag(h, (int)len) && rec_equal(P, slot, (tg & GREP_TAG_LONG) != 0u, k, len)) sink.hit(slot);
 }
 
 struct StageDesc {
@@ -313,15 +340,6 @@ __device__ __forceinline__ int file_of(const GrepDev& P, uint64_t c) {
 #define GR_BM_WORDS 18
 #define GR_WSCR (GR_BM_WORDS * 4 + GR_SEG) /* bytes per warp: bitmap + 256 u16 starts */
 
-/* Bit 15 / bit 31 set where the low / high 16-bit tag of w equals the
- * token's (tt = tag in both halves).  Exact for the low half; the high half
- * can read as a match when the low half matches too, which the record check
- * and the exact candidate loop absorb. */
-__device__ __forceinline__ uint32_t z16(uint32_t w, uint32_t tt) {
-    const uint32_t x = w ^ tt;
-    return (x - 0x00010001u) & ~x & 0x80008000u;
-}
-
 /* letters from bit r of the bitmap on: 1..32, or 33 for a run of 33+ */
 __device__ __forceinline__ uint32_t run_len(const uint32_t* bm, uint32_t r) {
     const uint32_t w = r >> 5, b = r & 31u;
@@ -330,94 +348,66 @@ __device__ __forceinline__ uint32_t run_len(const uint32_t* bm, uint32_t r) {
     return 32u + (__funnelshift_r(bm[w + 1], bm[w + 2], b) & 1u);
 }
 
-/* Tag candidates of a token of at most 16 letters, key k[0..3] zero padded:
- * a mask with bits 31/15 (bucket b1 slots 1/0), 30/14 (b1 slots 3/2),
- * 29/13 (b2 slots 1/0) and 28/12 (b2 slots 3/2). */
-__device__ __forceinline__ uint32_t cands16(const GrepDev& P, const Tbl& t, const uint32_t k[4], uint32_t len,
-                                            uint32_t* b1o, uint32_t* b2o) {
-    const uint32_t a = len * 0x9E3779B1u + k[0] * 0x85EBCA77u + k[1] * 0xC2B2AE3Du + k[2] * 0x27D4EB2Fu +
-                       k[3] * 0x165667B1u; /* grep_mix for len <= 16 */
-    const uint32_t h1 = grep_h1(a);
-    const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h1, P.nb);
-    const uint32_t tt = grep_tag(h1, (int)len) * 0x00010001u;
-    const uint2 q1 = ((const uint2*)t.tags)[b1];
-    const uint2 q2 = ((const uint2*)t.tags)[b2];
-    *b1o = b1;
-    *b2o = b2;
-    /* when b2 == b1 the second half repeats the first: harmless */
-    uint32_t m = z16(q1.x, tt) | (z16(q1.y, tt) >> 1);
-    m |= (z16(q2.x, tt) >> 2) | (z16(q2.y, tt) >> 3);
-    return m;
-}
-/* slot of the candidate at the highest set bit of m */
-__device__ __forceinline__ uint32_t cand_slot(uint32_t m, uint32_t b1, uint32_t b2) {
-    const uint32_t p = 31u - (uint32_t)__clz(m);
-    const uint32_t w = (15u - (p & 15u)) & 3u;
-    return 4u * (w < 2u ? b1 : b2) + ((w & 1u) << 1) + (p >> 4);
-}
 __device__ __forceinline__ bool key_eq(const uint4 r, const uint32_t k[4]) {
     return r.x == k[0] && r.y == k[1] && r.z == k[2] && r.w == k[3];
 }
 
-/* a short token whose first candidate was not the word: check every slot
- * of both buckets exactly (a short token's candidates are short words, so
- * equal first 16 bytes mean equal words); returns the slot or ~0 */
-__device__ __forceinline__ uint32_t other_cands16(const GrepDev& P, const Tbl& t, const uint32_t* k, uint32_t len) {
-    const uint32_t kk[4] = {k[0], k[1], k[2], k[3]};
-    const uint32_t h1 = grep_h1(len * 0x9E3779B1u + kk[0] * 0x85EBCA77u + kk[1] * 0xC2B2AE3Du +
-                                kk[2] * 0x27D4EB2Fu + kk[3] * 0x165667B1u);
-    const uint32_t b1 = grep_bucket(h1, P.nb), b2 = grep_b2(h1, P.nb), tag = grep_tag(h1, (int)len);
-    for (uint32_t j = 0; j < 8u; j++) {
-        const uint32_t c = 4u * (j < 4u ? b1 : b2) + (j & 3u);
-        if (t.tags[c] == tag && key_eq(__ldg(P.rec_lo + c), kk)) return c;
-    }
-    return 0xFFFFFFFFu;
-}
-
 /* NTOK tokens per lane (list entries tb0 + lane + 32 i), straight-line so
- * their loads overlap */
-template <int NTOK, class Sink>
+ * their loads overlap, with no branch on the common path.  A token of at
+ * most 16 letters: key from five shared words, the short hash (key words
+ * 0..3), one displacement and one tag load, on a tag hit the record's
+ * first 16 bytes, and one counter add.  Tokens of 17+ letters (rare) take
+ * a warp-uniform slow path. */
+template <bool SMEM, int NTOK, class Sink>
 __device__ __forceinline__ void scan_tokens(const GrepDev& P, const Tbl& tbl, const uint8_t* base, const uint32_t* bm,
                                             const uint16_t* slist, uint32_t seg0, uint32_t tb0, uint32_t n_s,
                                             const uint4* km, Sink& sink) {
     const uint32_t lane = threadIdx.x & 31u;
-    uint32_t st[NTOK], len[NTOK], k[NTOK][4], b1[NTOK], b2[NTOK], m[NTOK], slot[NTOK];
-    bool v[NTOK], f[NTOK];
+    uint32_t st[NTOK], len[NTOK], k[NTOK][4], slot[NTOK];
+    bool v[NTOK], c[NTOK];
 #pragma unroll
     for (int i = 0; i < NTOK; i++) {
         const uint32_t ti = tb0 + lane + 32u * (uint32_t)i;
         v[i] = ti < n_s;
         st[i] = v[i] ? slist[ti] : seg0;
-        len[i] = v[i] ? run_len(bm, st[i] - seg0) : 0u;
-        f[i] = v[i] && len[i] <= 16u;
+        /* letters from st on, 1..32 (32 also for longer runs) */
+        const uint32_t r = st[i] - seg0, w = r >> 5, b = r & 31u;
+        const uint32_t x = __funnelshift_r(bm[w], bm[w + 1], b);
+        len[i] = (uint32_t)__popc(x & ~(x + 1u));
     }
 #pragma unroll
-    for (int i = 0; i < NTOK; i++) key16(base, st[i], f[i] ? len[i] : 0u, k[i], km);
+    for (int i = 0; i < NTOK; i++) key16(base, st[i], len[i] <= 16u ? len[i] : 0u, k[i], km);
 #pragma unroll
-    for (int i = 0; i < NTOK; i++) m[i] = f[i] ? cands16(P, tbl, k[i], len[i], &b1[i], &b2[i]) : 0u;
-#pragma unroll
-    for (int i = 0; i < NTOK; i++) slot[i] = m[i] ? cand_slot(m[i], b1[i], b2[i]) : 0xFFFFFFFFu;
+    for (int i = 0; i < NTOK; i++) {
+        const uint32_t a = len[i] * P.hk.c[0] + k[i][0] * P.hk.c[1] + k[i][1] * P.hk.c[2] + k[i][2] * P.hk.c[3] +
+                           k[i][3] * P.hk.c[4]; /* grep_mix for len <= 16 */
+        const uint32_t h = grep_h1(a);
+        slot[i] = tbl_slot<SMEM>(P, tbl, h);
+        c[i] = v[i] && len[i] <= 16u && tbl_tag<SMEM>(tbl, slot[i]) == ((h | 1u) & 0x7FFFu); /* grep_tag, len <= 16 */
+    }
     uint4 r[NTOK];
 #pragma unroll
-    for (int i = 0; i < NTOK; i++) r[i] = m[i] ? __ldg(P.rec_lo + slot[i]) : make_uint4(0, 0, 0, 0);
+    for (int i = 0; i < NTOK; i++) r[i] = c[i] ? __ldg(P.rec_lo + slot[i]) : make_uint4(0, 0, 0, 0);
 #pragma unroll
-    for (int i = 0; i < NTOK; i++)
-        if (m[i] && !key_eq(r[i], k[i])) slot[i] = other_cands16(P, tbl, k[i], len[i]);
-#pragma unroll
-    for (int i = 0; i < NTOK; i++)
-        if (slot[i] != 0xFFFFFFFFu) sink.hit(slot[i]);
+    for (int i = 0; i < NTOK; i++) sink.hit_if(c[i] && key_eq(r[i], k[i]), slot[i]);
     /* rare: tokens of 17..32 letters take the general lookup; a run of 33+
      * letters flags the file for the fix-up kernel */
+    bool lg = false;
 #pragma unroll
-    for (int i = 0; i < NTOK; i++)
-        if (v[i] && len[i] > 16u) {
-            if (len[i] > 32u) sink.long_run();
-            else {
-                uint32_t kk[8];
-                key32(base, st[i], len[i], kk);
-                lookup_hit(P, tbl, kk, len[i], sink);
+    for (int i = 0; i < NTOK; i++) lg |= v[i] && len[i] > 16u;
+    if (__any_sync(0xFFFFFFFFu, lg)) {
+#pragma unroll
+        for (int i = 0; i < NTOK; i++)
+            if (v[i] && len[i] > 16u) {
+                const uint32_t L = run_len(bm, st[i] - seg0);
+                if (L > 32u) sink.long_run();
+                else {
+                    uint32_t kk[8];
+                    key32(base, st[i], L, kk);
+                    lookup_hit<SMEM>(P, tbl, kk, L, sink);
+                }
             }
-        }
+    }
 }
 
 template <bool SMEM, class Sink>
@@ -464,20 +454,20 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, c
     /* rounds of two tokens per lane; a last round of at most 32 tokens takes
      * one per lane (warp-uniform choice) */
     for (uint32_t tb0 = 0; tb0 < n_s; tb0 += 64u) {
-        if (n_s - tb0 > 32u) scan_tokens<2>(P, tbl, base, bm, slist, seg0, tb0, n_s, km, sink);
-        else scan_tokens<1>(P, tbl, base, bm, slist, seg0, tb0, n_s, km, sink);
+        if (n_s - tb0 > 32u) scan_tokens<SMEM, 2>(P, tbl, base, bm, slist, seg0, tb0, n_s, km, sink);
+        else scan_tokens<SMEM, 1>(P, tbl, base, bm, slist, seg0, tb0, n_s, km, sink);
     }
 }
 
 template <bool SMEM, int NC>
 __device__ void flush_counts(const GrepDev& P, const Tbl& t, int f) {
-    if (!SMEM) return;
-    const uint32_t nslots = 4u * P.nb;
-    for (uint32_t i = threadIdx.x; i < nslots; i += NC * 32) {
-        const uint32_t n = t.cnt[i];
-        if (n) {
-            t.cnt[i] = 0u;
-            flush_slot(P, i, n, f);
+    if constexpr (SMEM) {
+        for (uint32_t i = threadIdx.x; i < P.m; i += NC * 32) {
+            const uint32_t n = t.cnt[i];
+            if (n) {
+                t.cnt[i] = 0u;
+                flush_slot(P, i, n, f);
+            }
         }
     }
 }
@@ -840,22 +830,29 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
     constexpr uint32_t CH = (uint32_t)NC * GR_SEG;
     extern __shared__ __align__(128) uint8_t dsm[];
     __shared__ Shared sh;
-    /* shared memory: slot tags (8 B per bucket), slot counters (16 B per
-     * bucket), the stage ring, per-warp scratch */
-    const uint32_t tag_bytes = SMEM ? (8u * P.nb + 127u) & ~127u : 0u;
-    const uint32_t tbl_bytes = SMEM ? tag_bytes + ((16u * P.nb + 127u) & ~127u) : 0u;
+    /* shared memory: slot tags, displacements, slot counters, the stage
+     * ring, per-warp scratch */
+    const uint32_t tag_bytes = SMEM ? grep_tag_smem(P.m) : 0u;
+    const uint32_t disp_bytes = SMEM ? grep_disp_smem(P.r) : 0u;
+    const uint32_t tbl_bytes = SMEM ? tag_bytes + disp_bytes + grep_cnt_smem(P.m) : 0u;
     Tbl tbl;
     tbl.tags = SMEM ? (const uint16_t*)dsm : P.tags;
-    tbl.cnt = SMEM ? (uint32_t*)(dsm + tag_bytes) : nullptr;
+    tbl.disp = SMEM ? (const uint16_t*)(dsm + tag_bytes) : P.disp;
+    tbl.cnt = SMEM ? (uint32_t*)(dsm + tag_bytes + disp_bytes) : nullptr;
     uint8_t* stages = dsm + tbl_bytes;
     uint8_t* wscr = stages + GR_STAGES * GR_STAGE + (size_t)(threadIdx.x >> 5) * GR_WSCR;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    if (SMEM)
-        for (uint32_t i = threadIdx.x; i < P.nb; i += blockDim.x) {
-            ((uint2*)dsm)[i] = __ldg((const uint2*)P.tags + i);
+    if constexpr (SMEM) {
+        /* the plan's global tags and displacements are zero padded to these
+         * sizes (multiples of 128 bytes) */
+        for (uint32_t i = threadIdx.x; i < tag_bytes / 16u; i += blockDim.x)
+            ((uint4*)dsm)[i] = __ldg((const uint4*)P.tags + i);
+        for (uint32_t i = threadIdx.x; i < disp_bytes / 16u; i += blockDim.x)
+            ((uint4*)(dsm + tag_bytes))[i] = __ldg((const uint4*)P.disp + i);
+        for (uint32_t i = threadIdx.x; i < grep_cnt_smem(P.m) / 16u; i += blockDim.x)
             ((uint4*)tbl.cnt)[i] = make_uint4(0u, 0u, 0u, 0u);
-        }
+    }
     if (threadIdx.x == 0) {
         for (int s = 0; s < GR_STAGES; s++) {
             mbar_init(&sh.full[s], 1u);
@@ -1025,9 +1022,10 @@ __device__ void count_piece(const GrepDev& P, PageCursor& pc, uint64_t a, uint64
                ((uint32_t)buf[4 * i + 3] << 24);
     Tbl t;
     t.tags = P.tags;
+    t.disp = P.disp;
     t.cnt = nullptr;
     CountSink sink{P, t, false, f};
-    lookup_hit(P, t, k, (uint32_t)len, sink);
+    lookup_hit<false>(P, t, k, (uint32_t)len, sink);
 }
 } // namespace
 
@@ -1233,6 +1231,7 @@ __device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, ui
     if (lane == 0) { pf = pin_file(S, fd); pp_init(pp); }
     Tbl t;
     t.tags = D.G.tags;
+    t.disp = D.G.disp;
     t.cnt = nullptr;
     TotalSink sink;
     int err = 0;
@@ -1411,28 +1410,35 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev 
 }
 
 /* ---------------- dictionary table built on the device ----------------
- * The same table as the host build (same hashes, tags, buckets, load), made
- * by five small kernels: keys, dedupe, duplicate chains, a parallel
- * bucketised cuckoo insertion, and the table image.  Where several valid
- * placements exist the device may pick another one than the host; the
- * counts a scan produces do not depend on it. */
+ * The same table as the host build (same hashes, tags, geometry), made by
+ * five kernels: keys, dedupe, duplicate chains, the seeded displacement
+ * search (one cooperative launch), and the table image.  Where several
+ * valid displacements exist the device may pick another one than the host;
+ * the counts a scan produces do not depend on it. */
 struct TbDev {
     const uint8_t* dict; /* n records of 32 bytes */
     int n;
     uint4* klo;          /* key bytes 0..15 / 16..31 per record */
     uint4* khi;
-    uint32_t* h1;
+    uint32_t* h1;        /* per record: hash under the current seed */
     int* len;
     int* set;            /* dedupe set: cap entries, -1 empty */
     uint32_t cap;
     int* rep;            /* per record: the record its word is counted under, -1 for empty */
     int* head;           /* per representative: its last duplicate, -1 */
     int* chain;          /* per duplicate: the next duplicate of its word, -1 */
-    int* slot_of;        /* nb * 4 slots: representative, -1 empty */
-    uint32_t nb;
-    uint32_t* fail;      /* set when an insertion ran out of kicks */
+    uint32_t m, r;       /* slots, displacement buckets */
+    int* owner;          /* m slots: representative, -1 empty */
+    uint32_t* bsize;     /* r: words per bucket */
+    int* bkeys;          /* r x GREP_MAX_BUCKET: each bucket's representatives */
+    uint16_t* dsp;       /* r displacements */
+    unsigned long long* hset; /* duplicate-hash check: cap entries, ~0 empty */
+    uint32_t* fail;      /* [0] set while the current seed fails; [1] the seed that succeeded */
+    uint32_t seed0, n_seeds; /* seeds tried: seed0 .. seed0 + n_seeds - 1 */
+    grep_hashk hk;       /* filled by the host from the seed that succeeded */
     /* the image */
     uint16_t* tags;
+    uint16_t* disp;
     uint4* rec_lo;
     uint4* rec_hi;
     uint32_t* slot_word;
@@ -1462,19 +1468,19 @@ static __global__ void k_tb_keys(TbDev T) {
     T.klo[w] = make_uint4(k[0], k[1], k[2], k[3]);
     T.khi[w] = make_uint4(k[4], k[5], k[6], k[7]);
     T.len[w] = len;
-    T.h1[w] = len ? grep_h1(grep_mix(k, len)) : 0u;
     T.head[w] = -1;
     T.chain[w] = -1;
 }
 
 __device__ __forceinline__ bool tb_same(const TbDev& T, int a, int b) {
-    if (T.h1[a] != T.h1[b] || T.len[a] != T.len[b]) return false;
+    if (T.len[a] != T.len[b]) return false;
     const uint4 x = T.klo[a], y = T.klo[b], u = T.khi[a], v = T.khi[b];
     return x.x == y.x && x.y == y.y && x.z == y.z && x.w == y.w && u.x == v.x && u.y == v.y && u.z == v.z && u.w == v.w;
 }
 
 /* the first record of each distinct word to claim its set entry becomes the
- * word's representative; the others are its duplicates */
+ * word's representative; the others are its duplicates.  The set is probed
+ * by a hash of the key alone (not the seeded one), so it runs once. */
 static __global__ void k_tb_dedupe(TbDev T) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= T.n) return;
@@ -1482,7 +1488,10 @@ static __global__ void k_tb_dedupe(TbDev T) {
         T.rep[w] = -1;
         return;
     }
-    uint32_t i = T.h1[w] & (T.cap - 1u);
+    const uint4 x = T.klo[w], y = T.khi[w];
+    const uint32_t hs = (x.x * 0x9E3779B1u) ^ (x.y * 0x85EBCA77u) ^ (x.z * 0xC2B2AE3Du) ^ (x.w * 0x27D4EB2Fu) ^
+                        (y.x * 0x165667B1u) ^ (y.y * 0xD3A2646Du) ^ (y.z * 0xFD7046C5u) ^ (y.w * 0xB55A4F09u);
+    uint32_t i = grep_h1(hs) & (T.cap - 1u);
     for (uint32_t probe = 0; probe < T.cap; probe++, i = (i + 1u) & (T.cap - 1u)) {
         int cur = T.set[i];
         if (cur < 0) {
@@ -1507,48 +1516,124 @@ static __global__ void k_tb_chains(TbDev T) {
     if (r >= 0 && r != w) T.chain[w] = atomicExch(&T.head[r], w);
 }
 
-/* one thread per representative; an evicted word is carried on by the
- * thread that evicted it; at most 4096 moves per thread */
-static __global__ void k_tb_insert(TbDev T) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= T.n || T.rep[w] != w) return;
-    int cur = w;
-    uint32_t rng = 0x9E3779B9u ^ (uint32_t)w * 0x85EBCA6Bu;
-    for (int kick = 0; kick < 4096; kick++) {
-        const uint32_t h = T.h1[cur];
-        const uint32_t b[2] = {grep_bucket(h, T.nb), grep_b2(h, T.nb)};
-        /* the emptier of the two buckets */
-        int best = -1, best_free = 0;
-        for (int q = 0; q < 2; q++) {
-            int nfree = 0, first = -1;
-            for (int i = 0; i < GREP_WAYS; i++) {
-                const int sl = (int)(b[q] * GREP_WAYS) + i;
-                if (((volatile int*)T.slot_of)[sl] < 0) {
-                    nfree++;
-                    if (first < 0) first = sl;
+/* The seeded part of the device build, in one cooperative launch (grid-wide
+ * syncs between the steps).  For each seed in turn, until one succeeds:
+ *   1. every distinct word's hash under the seed's multipliers;
+ *   2. a check that no two distinct words share a 32-bit hash (no
+ *      displacement could separate them), through a set keyed by the hash,
+ *      and the words grouped by bucket (fixed lists of GREP_MAX_BUCKET);
+ *   3. the displacement search: size classes from the largest bucket size
+ *      down to 1, so large buckets are placed while the table is emptiest
+ *      (as in the sequential build); inside a class every warp takes
+ *      buckets in turn.  A bucket's warp tests 32 displacements per round
+ *      (lane l tries base + l, loading the owners of all the bucket's
+ *      candidate slots at once); for the first displacement that fits,
+ *      lanes 0..z-1 claim the z slots by CAS together and undo their claims
+ *      if any lost a race to another bucket.
+ * On success fail[1] holds the seed, T.owner the slot of every word and
+ * T.dsp the displacements; fail[0] stays set if every seed failed. */
+static __global__ void __launch_bounds__(256) k_tb_search(TbDev T) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const uint32_t gw = tid >> 5, nw = nth >> 5;
+    for (uint32_t sd = T.seed0; sd < T.seed0 + T.n_seeds; sd++) {
+        grep_hashk hk;
+        grep_hash_seed(sd, &hk);
+        if (tid == 0) T.fail[0] = 0u;
+        for (uint32_t b = tid; b < T.r; b += nth) {
+            T.bsize[b] = 0u;
+            T.dsp[b] = 0;
+        }
+        for (uint32_t sl = tid; sl < T.m; sl += nth) T.owner[sl] = -1;
+        for (uint32_t i = tid; i < T.cap; i += nth) T.hset[i] = ~0ull;
+        for (int w = (int)tid; w < T.n; w += (int)nth)
+            if (T.rep[w] == w) {
+                const uint4 x = T.klo[w], y = T.khi[w];
+                const uint32_t k[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
+                T.h1[w] = grep_h1(grep_mix(&hk, k, T.len[w]));
+            }
+        grid.sync();
+        for (int w = (int)tid; w < T.n; w += (int)nth)
+            if (T.rep[w] == w) {
+                const uint32_t h = T.h1[w];
+                const unsigned long long e = ((unsigned long long)h << 32) | (uint32_t)w;
+                for (uint32_t i = h & (T.cap - 1u), probe = 0; probe < T.cap; probe++, i = (i + 1u) & (T.cap - 1u)) {
+                    const unsigned long long cur = atomicCAS(&T.hset[i], ~0ull, e);
+                    if (cur == ~0ull) break;
+                    if ((uint32_t)(cur >> 32) == h) {
+                        atomicOr(&T.fail[0], 1u);
+                        break;
+                    }
+                }
+                const uint32_t b = grep_bucket(h, T.r);
+                const uint32_t i = atomicAdd(&T.bsize[b], 1u);
+                if (i < GREP_MAX_BUCKET) T.bkeys[(size_t)b * GREP_MAX_BUCKET + i] = w;
+                else atomicOr(&T.fail[0], 1u);
+            }
+        grid.sync();
+        bool failed = *(volatile uint32_t*)&T.fail[0] != 0u;
+        for (int z = GREP_MAX_BUCKET; z >= 1 && !failed; z--) {
+            for (uint32_t b = gw; b < T.r; b += nw) {
+                if (T.bsize[b] != (uint32_t)z) continue;
+                const int* keys = T.bkeys + (size_t)b * GREP_MAX_BUCKET;
+                uint32_t hh[GREP_MAX_BUCKET];
+                for (int i = 0; i < z; i++) hh[i] = T.h1[keys[i]];
+                const int mykey = lane < (uint32_t)z ? keys[lane] : -1;
+                const uint32_t myh = lane < (uint32_t)z ? hh[lane] : 0u;
+                uint32_t found = 0xFFFFFFFFu;
+                for (uint32_t base = 0; base < 65536u && found == 0xFFFFFFFFu; base += 32u) {
+                    const uint32_t d = base + lane;
+                    uint32_t sl[GREP_MAX_BUCKET];
+                    bool ok = true;
+                    for (int i = 0; i < z; i++) {
+                        sl[i] = grep_slot(hh[i], d, T.m);
+                        for (int q = 0; q < i; q++) ok = ok && sl[q] != sl[i];
+                    }
+                    /* owners of all candidate slots: independent loads, 8 in flight */
+                    for (int i0 = 0; i0 < z; i0 += 8) {
+                        int o[8];
+#pragma unroll
+                        for (int j = 0; j < 8; j++) o[j] = i0 + j < z ? ((volatile int*)T.owner)[sl[i0 + j]] : -1;
+#pragma unroll
+                        for (int j = 0; j < 8; j++) ok = ok && o[j] < 0;
+                    }
+                    unsigned cand = __ballot_sync(0xFFFFFFFFu, ok);
+                    while (cand) {
+                        const int l = __ffs(cand) - 1;
+                        cand &= cand - 1u;
+                        const uint32_t dd = base + (uint32_t)l;
+                        bool mine = false;
+                        if (lane < (uint32_t)z) mine = atomicCAS(&T.owner[grep_slot(myh, dd, T.m)], -1, mykey) == -1;
+                        const unsigned lost = __ballot_sync(0xFFFFFFFFu, lane < (uint32_t)z && !mine);
+                        if (!lost) {
+                            found = dd;
+                            break;
+                        }
+                        if (mine) atomicExch(&T.owner[grep_slot(myh, dd, T.m)], -1);
+                    }
+                }
+                if (lane == 0) {
+                    if (found == 0xFFFFFFFFu) atomicOr(&T.fail[0], 1u);
+                    else T.dsp[b] = (uint16_t)found;
                 }
             }
-            if (nfree > best_free) {
-                best_free = nfree;
-                best = first;
-            }
+            grid.sync();
+            failed = *(volatile uint32_t*)&T.fail[0] != 0u;
         }
-        if (best >= 0 && atomicCAS(&T.slot_of[best], -1, cur) == -1) return;
-        if (best >= 0) continue; /* lost the slot to another thread: look again */
-        rng ^= rng << 13;
-        rng ^= rng >> 17;
-        rng ^= rng << 5;
-        const int victim = (int)(b[rng & 1u] * GREP_WAYS + ((rng >> 8) & 3u));
-        cur = atomicExch(&T.slot_of[victim], cur);
-        if (cur < 0) return; /* the slot had just been freed: placed */
+        if (!failed) {
+            if (tid == 0) T.fail[1] = sd;
+            return;
+        }
+        grid.sync(); /* every thread has read the flag before the next seed clears it */
     }
-    atomicOr(T.fail, 1u); /* the carried word is lost: the build is retried */
 }
 
 static __global__ void k_tb_image(TbDev T) {
     const uint32_t sl = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sl < T.nb * GREP_WAYS) {
-        const int w = T.slot_of[sl];
+    if (sl < T.m) {
+        const int w = T.owner[sl];
         if (w < 0) {
             T.tags[sl] = 0;
             T.rec_lo[sl] = make_uint4(0u, 0u, 0u, 0u);
@@ -1561,6 +1646,7 @@ static __global__ void k_tb_image(TbDev T) {
             T.slot_word[sl] = (uint32_t)w;
         }
     }
+    if (sl < T.r) T.disp[sl] = T.dsp[sl];
     /* duplicate chains: representative -> its duplicates -> -1 */
     if (sl < (uint32_t)T.n) T.next_dup[sl] = T.rep[sl] == (int)sl ? T.head[sl] : T.chain[sl];
 }
@@ -1607,18 +1693,20 @@ struct BuildWs {
     };
     std::mutex mu;
     std::vector<Key> key;
-    std::vector<int> uniq, last, seen, slot_of;
-    std::vector<uint32_t> ba, bb;
+    std::vector<int> uniq, last, seen, slot_of, bkeys;
+    std::vector<uint32_t> bstart, bfill, order;
+    std::vector<uint16_t> disp;
     std::vector<int32_t> next_dup;
-    uint32_t nb = 0;
+    uint32_t m = 0, r = 0;
+    grep_hashk hk{};
 };
 BuildWs g_ws;
 
-/* Load 0.92: the table lives in shared memory, and the less of the SM's
- * combined L1/shared storage it takes, the more L1 is left to cache the
- * records the scan verifies candidates against (measured: lower loads were
- * slower).  16-bit tags keep false candidates rare at this load.  Result in
- * W: nb, slot_of (slot -> first record of its word, -1 empty), next_dup. */
+/* Host build of the table (the fallback of the device build, and the build
+ * a session with GFS_CFG_HOST_TABLE asks for): the same geometry, hashes
+ * and displacement search as k_tb_search, one bucket at a time, largest
+ * first.  Result in W: m, r, hk, slot_of (slot -> first record of its word,
+ * -1 empty), disp, next_dup. */
 bool build_table(const uint8_t* dict, int n_words, BuildWs& W) {
     const size_t nw = n_words > 0 ? (size_t)n_words : 1u;
     auto& key = W.key;
@@ -1627,7 +1715,7 @@ bool build_table(const uint8_t* dict, int n_words, BuildWs& W) {
     W.uniq.reserve(nw);
     W.last.assign(nw, -1);
     W.next_dup.assign(nw, -1);
-    /* duplicates: open addressing on the word hash, exact key compare */
+    /* duplicates: open addressing on a hash of the key, exact key compare */
     size_t cap = 16;
     while (cap < 2 * nw) cap <<= 1;
     W.seen.assign(cap, -1);
@@ -1635,8 +1723,9 @@ bool build_table(const uint8_t* dict, int n_words, BuildWs& W) {
         BuildWs::Key& kw = key[(size_t)w];
         rec_key(dict + (size_t)w * 32, kw.k, &kw.len);
         if (kw.len == 0) continue;
-        kw.h1 = grep_h1(grep_mix(kw.k, kw.len));
-        for (size_t i = kw.h1 & (cap - 1);; i = (i + 1) & (cap - 1)) {
+        uint32_t hs = 0;
+        for (int i = 0; i < 8; i++) hs ^= kw.k[i] * (0x9E3779B1u + 0x3C6EF372u * (uint32_t)i);
+        for (size_t i = grep_h1(hs) & (cap - 1);; i = (i + 1) & (cap - 1)) {
             const int u = W.seen[i];
             if (u < 0) {
                 W.seen[i] = w;
@@ -1645,57 +1734,61 @@ bool build_table(const uint8_t* dict, int n_words, BuildWs& W) {
                 break;
             }
             const BuildWs::Key& ku = key[(size_t)u];
-            if (ku.h1 == kw.h1 && ku.len == kw.len && memcmp(ku.k, kw.k, sizeof kw.k) == 0) {
+            if (ku.len == kw.len && memcmp(ku.k, kw.k, sizeof kw.k) == 0) {
                 W.next_dup[(size_t)W.last[(size_t)u]] = w;
                 W.last[(size_t)u] = w;
                 break;
             }
         }
     }
-    /* bucketised cuckoo placement (2 choices x 4 slots), random-walk kicks */
-    W.ba.resize(nw);
-    W.bb.resize(nw);
-    uint32_t nb = (uint32_t)((double)W.uniq.size() / (GREP_WAYS * 0.92)) + 16u;
-    for (int attempt = 0; attempt < 20; attempt++, nb = nb + nb / 8u + 1u) {
-        for (int w : W.uniq) {
-            W.ba[(size_t)w] = grep_bucket(key[(size_t)w].h1, nb);
-            W.bb[(size_t)w] = grep_b2(key[(size_t)w].h1, nb);
-        }
-        auto& slot_of = W.slot_of;
-        slot_of.assign((size_t)nb * GREP_WAYS, -1);
-        uint64_t rng = 0x243F6A8885A308D3ULL ^ nb;
+    uint32_t m0, r;
+    grep_geometry((uint32_t)n_words, &m0, &r);
+    for (uint32_t seed = 0; seed < 16; seed++) {
+        const uint32_t m = m0 + m0 / 16u * (seed / 8u);
+        grep_hash_seed(seed, &W.hk);
+        for (int w : W.uniq) key[(size_t)w].h1 = grep_h1(grep_mix(&W.hk, key[(size_t)w].k, key[(size_t)w].len));
+        /* words grouped by bucket */
+        W.bstart.assign((size_t)r + 1, 0u);
+        for (int w : W.uniq) W.bstart[grep_bucket(key[(size_t)w].h1, r) + 1]++;
+        for (uint32_t b = 0; b < r; b++) W.bstart[b + 1] += W.bstart[b];
+        W.bfill.assign(W.bstart.begin(), W.bstart.end() - 1);
+        W.bkeys.resize(W.uniq.size() + 1);
+        for (int w : W.uniq) W.bkeys[W.bfill[grep_bucket(key[(size_t)w].h1, r)]++] = w;
+        /* buckets by decreasing size */
+        W.order.resize(r);
+        for (uint32_t b = 0; b < r; b++) W.order[b] = b;
+        std::stable_sort(W.order.begin(), W.order.end(), [&](uint32_t x, uint32_t y) {
+            return W.bstart[x + 1] - W.bstart[x] > W.bstart[y + 1] - W.bstart[y];
+        });
+        W.slot_of.assign(m, -1);
+        W.disp.assign(r, 0);
         bool ok = true;
-        for (int w : W.uniq) {
-            int cur = w;
-            int kicks = 0;
-            for (;;) {
-                const uint32_t b[2] = {W.ba[(size_t)cur], W.bb[(size_t)cur]};
-                /* the emptier of the two buckets (fewer kicks near full load) */
-                int placed = -1, best_free = 0;
-                for (int r = 0; r < 2; r++) {
-                    int nfree = 0, first = -1;
-                    for (int i = 0; i < GREP_WAYS; i++)
-                        if (slot_of[b[r] * GREP_WAYS + (uint32_t)i] < 0) {
-                            nfree++;
-                            if (first < 0) first = (int)(b[r] * GREP_WAYS + (uint32_t)i);
-                        }
-                    if (nfree > best_free) { best_free = nfree; placed = first; }
+        for (uint32_t b : W.order) {
+            const uint32_t z = W.bstart[b + 1] - W.bstart[b];
+            if (z == 0) break;
+            if (z > GREP_MAX_BUCKET) { ok = false; break; }
+            const int* ks = W.bkeys.data() + W.bstart[b];
+            uint32_t sl[GREP_MAX_BUCKET];
+            for (uint32_t i = 0; i < z && ok; i++)
+                for (uint32_t q = 0; q < i; q++)
+                    if (key[(size_t)ks[q]].h1 == key[(size_t)ks[i]].h1) ok = false;
+            uint32_t d = 0;
+            for (; ok && d < 65536u; d++) {
+                bool fit = true;
+                for (uint32_t i = 0; i < z && fit; i++) {
+                    sl[i] = grep_slot(key[(size_t)ks[i]].h1, d, m);
+                    fit = W.slot_of[sl[i]] < 0;
+                    for (uint32_t q = 0; q < i && fit; q++) fit = sl[q] != sl[i];
                 }
-                if (placed >= 0) {
-                    slot_of[(size_t)placed] = cur;
-                    break;
-                }
-                if (++kicks > 2000) { ok = false; break; }
-                rng ^= rng << 13; rng ^= rng >> 7; rng ^= rng << 17;
-                const uint32_t victim = b[rng & 1u] * GREP_WAYS + (uint32_t)((rng >> 8) & 3u);
-                const int ev = slot_of[victim];
-                slot_of[victim] = cur;
-                cur = ev;
+                if (fit) break;
             }
-            if (!ok) break;
+            if (!ok || d >= 65536u) { ok = false; break; }
+            for (uint32_t i = 0; i < z; i++) W.slot_of[sl[i]] = ks[i];
+            W.disp[b] = (uint16_t)d;
         }
         if (!ok) continue;
-        W.nb = nb;
+        W.m = m;
+        W.r = r;
         return true;
     }
     return false;
@@ -1706,7 +1799,7 @@ bool build_table(const uint8_t* dict, int n_words, BuildWs& W) {
 struct gfs_grep {
     gfs_ctx* ctx = nullptr;
     int n_files = 0, n_words = 0;
-    uint32_t nb = 0; /* table buckets */
+    uint32_t m = 0, r = 0; /* table slots, displacement buckets */
     GrepDev dev{};
     void* dmem = nullptr; /* one allocation for everything */
     std::vector<uint64_t> sizes;
@@ -1737,17 +1830,19 @@ static uint64_t host_us() {
 }
 
 /* Device layout of a plan: the table image and the file names first, then
- * what the device fills or the host adds later. */
+ * what the device fills or the host adds later.  Tags and displacements are
+ * zero padded to their shared-memory sizes (the scan copies them whole). */
 struct PlanLayout {
-    size_t o_tbl, o_recs, o_sw, o_nd, o_names, o_cnt, o_fds, o_sz, o_pf, o_fl, o_st, o_fo, o_fn, o_xxh, o_maps, total;
+    size_t o_tbl, o_disp, o_recs, o_sw, o_nd, o_names, o_cnt, o_fds, o_sz, o_pf, o_fl, o_st, o_fo, o_fn, o_xxh,
+        o_maps, total;
 };
-static PlanLayout plan_layout(uint32_t nb, int n_words, int n_files) {
+static PlanLayout plan_layout(uint32_t m, uint32_t r, int n_words, int n_files) {
     PlanLayout L;
-    const size_t ns = (size_t)nb * 4;
     L.o_tbl = 0;
-    L.o_recs = align_up(L.o_tbl + (size_t)nb * 8, 256);
-    L.o_sw = align_up(L.o_recs + ns * 32, 256);
-    L.o_nd = align_up(L.o_sw + ns * 4, 256);
+    L.o_disp = align_up(L.o_tbl + grep_tag_smem(m), 256);
+    L.o_recs = align_up(L.o_disp + grep_disp_smem(r), 256);
+    L.o_sw = align_up(L.o_recs + (size_t)m * 32, 256);
+    L.o_nd = align_up(L.o_sw + (size_t)m * 4, 256);
     L.o_names = align_up(L.o_nd + (size_t)n_words * 4 + 4, 256);
     L.o_cnt = align_up(L.o_names + (size_t)n_files * GFS_NAME_MAX, 256);
     L.o_fds = align_up(L.o_cnt + (size_t)n_words * n_files * 4 + 4, 256);
@@ -1764,62 +1859,86 @@ static PlanLayout plan_layout(uint32_t nb, int n_words, int n_files) {
 }
 
 /* Device build of the dictionary table (the dictionary's n_words records
- * are in pinned host memory at hdict; flag is 4 spare pinned bytes).  On
- * success returns the bucket count and leaves the build state in *T and
- * its memory in *tmp; the caller runs k_tb_image into the plan memory and
- * frees *tmp.  0: every insertion attempt failed (*tmp freed). */
-static uint32_t device_table(gfs_ctx* ctx, cudaStream_t s, const uint8_t* hdict, uint32_t* flag, int n_words,
-                             TbDev* T, void** tmp) {
+ * are in pinned host memory at hdict; flag is 8 spare pinned bytes).  On
+ * success returns true and leaves the build state (geometry, seed) in *T
+ * and its memory in *tmp; the caller runs k_tb_image into the plan memory
+ * and frees *tmp.  false: every seed failed, or the device could not run
+ * the cooperative search (*tmp freed); the caller builds on the host. */
+static bool device_table(gfs_ctx* ctx, cudaStream_t s, const uint8_t* hdict, uint32_t* flag, int n_words,
+                         TbDev* T, void** tmp) {
     const size_t n = (size_t)(n_words > 0 ? n_words : 1);
     uint32_t cap = 16;
     while (cap < 2 * n) cap <<= 1;
-    uint32_t nb = (uint32_t)((double)n_words / (GREP_WAYS * 0.92)) + 16u;
-    uint32_t nb_max = nb;
-    for (int a = 0; a < 4; a++) nb_max = nb_max + nb_max / 8u + 1u;
+    uint32_t m0, r;
+    grep_geometry((uint32_t)n_words, &m0, &r);
+    const uint32_t m_max = m0 + m0 / 16u * 2u;
     const size_t o_dict = 0, o_klo = align_up(n * 32, 256), o_khi = align_up(o_klo + n * 16, 256),
                  o_h1 = align_up(o_khi + n * 16, 256), o_len = align_up(o_h1 + n * 4, 256),
                  o_rep = align_up(o_len + n * 4, 256), o_head = align_up(o_rep + n * 4, 256),
                  o_nd = align_up(o_head + n * 4, 256), o_set = align_up(o_nd + n * 4, 256),
-                 o_slots = align_up(o_set + (size_t)cap * 4, 256), o_fail = align_up(o_slots + (size_t)nb_max * 16, 256),
-                 total = o_fail + 256;
-    uint8_t* m = (uint8_t*)gfs__dev_alloc(ctx, total, s);
-    *tmp = m;
-    if (!m) return 0;
+                 o_hs = align_up(o_set + (size_t)cap * 4, 256), o_own = align_up(o_hs + (size_t)cap * 8, 256),
+                 o_bsz = align_up(o_own + (size_t)m_max * 4, 256), o_bk = align_up(o_bsz + (size_t)r * 4, 256),
+                 o_dsp = align_up(o_bk + (size_t)r * GREP_MAX_BUCKET * 4, 256),
+                 o_fail = align_up(o_dsp + (size_t)r * 2, 256), total = o_fail + 256;
+    uint8_t* mem = (uint8_t*)gfs__dev_alloc(ctx, total, s);
+    *tmp = mem;
+    if (!mem) return false;
     TbDev& D = *T;
-    D.dict = m + o_dict;
+    D.dict = mem + o_dict;
     D.n = n_words;
-    D.klo = (uint4*)(m + o_klo);
-    D.khi = (uint4*)(m + o_khi);
-    D.h1 = (uint32_t*)(m + o_h1);
-    D.len = (int*)(m + o_len);
-    D.rep = (int*)(m + o_rep);
-    D.head = (int*)(m + o_head);
-    D.set = (int*)(m + o_set);
+    D.klo = (uint4*)(mem + o_klo);
+    D.khi = (uint4*)(mem + o_khi);
+    D.h1 = (uint32_t*)(mem + o_h1);
+    D.len = (int*)(mem + o_len);
+    D.rep = (int*)(mem + o_rep);
+    D.head = (int*)(mem + o_head);
+    D.set = (int*)(mem + o_set);
     D.cap = cap;
-    D.slot_of = (int*)(m + o_slots);
-    D.fail = (uint32_t*)(m + o_fail);
-    D.chain = (int*)(m + o_nd);
+    D.chain = (int*)(mem + o_nd);
+    D.hset = (unsigned long long*)(mem + o_hs);
+    D.owner = (int*)(mem + o_own);
+    D.bsize = (uint32_t*)(mem + o_bsz);
+    D.bkeys = (int*)(mem + o_bk);
+    D.dsp = (uint16_t*)(mem + o_dsp);
+    D.fail = (uint32_t*)(mem + o_fail);
+    D.r = r;
     const int nt = 256, gw = (n_words + nt - 1) / nt;
+    /* the cooperative search: at most four 256-thread blocks per SM, as many
+     * as fit at once */
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tb_search, nt, 0);
+    const int blocks = sms * (per_sm < 4 ? per_sm : 4);
+    cudaMemsetAsync(D.fail, 0, 8, s);
     if (n_words > 0) {
-        cudaMemcpyAsync(m + o_dict, hdict, (size_t)n_words * 32, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(mem + o_dict, hdict, (size_t)n_words * 32, cudaMemcpyHostToDevice, s);
         cudaMemsetAsync(D.set, 0xFF, (size_t)cap * 4, s);
         k_tb_keys<<<gw, nt, 0, s>>>(D);
         k_tb_dedupe<<<gw, nt, 0, s>>>(D);
         k_tb_chains<<<gw, nt, 0, s>>>(D);
     }
-    for (int a = 0; a < 5; a++, nb = nb + nb / 8u + 1u) {
-        D.nb = nb;
-        cudaMemsetAsync(D.slot_of, 0xFF, (size_t)nb * 16, s);
-        cudaMemsetAsync(D.fail, 0, 4, s);
-        if (n_words > 0) k_tb_insert<<<gw, nt, 0, s>>>(D);
-        cudaMemcpyAsync(flag, D.fail, 4, cudaMemcpyDeviceToHost, s);
+    /* 8 seeds at the base size, then 4 at each of two larger tables */
+    const uint32_t plan[3][2] = {{0u, 8u}, {8u, 4u}, {12u, 4u}};
+    for (int a = 0; a < 3 && blocks > 0; a++) {
+        D.m = m0 + m0 / 16u * (uint32_t)a;
+        D.seed0 = plan[a][0];
+        D.n_seeds = plan[a][1];
+        void* args[] = {&D};
+        if (cudaLaunchCooperativeKernel((const void*)k_tb_search, dim3((unsigned)blocks), dim3(nt), args, 0, s) !=
+            cudaSuccess)
+            break;
+        cudaMemcpyAsync(flag, D.fail, 8, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) break;
-        if (*flag == 0u) return nb;
+        if (flag[0] == 0u) {
+            grep_hash_seed(flag[1], &D.hk);
+            return true;
+        }
     }
     cudaGetLastError();
-    gfs__dev_free(ctx, m, s);
+    gfs__dev_free(ctx, mem, s);
     *tmp = nullptr;
-    return 0;
+    return false;
 }
 
 extern "C" {
@@ -1875,20 +1994,30 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     const uint64_t t_build = host_us();
     TbDev T{};
     void* tmp = nullptr;
-    uint32_t nb = device_table(ctx, s, hb, (uint32_t*)(hb + align_up(dict_bytes, 256)), n_words, &T, &tmp);
+    const bool on_dev = !(gfs__config_flags(ctx) & GFS_CFG_HOST_TABLE) &&
+                        device_table(ctx, s, hb, (uint32_t*)(hb + align_up(dict_bytes, 256)), n_words, &T, &tmp);
     std::unique_lock<std::mutex> lk(g_ws.mu, std::defer_lock);
-    if (!nb) {
-        /* the device insertion gave up: build on the host */
+    uint32_t m, r;
+    grep_hashk hk;
+    if (on_dev) {
+        m = T.m;
+        r = T.r;
+        hk = T.hk;
+    } else {
+        /* the device search gave up (or the session asked for it): build
+         * on the host */
         lk.lock();
         if (!build_table(hb, n_words, g_ws)) { delete g; return -GFS_ENOMEM; }
-        nb = g_ws.nb;
+        m = g_ws.m;
+        r = g_ws.r;
+        hk = g_ws.hk;
     }
-    g->nb = nb;
-    const size_t ns = (size_t)nb * 4; /* slots */
-    const PlanLayout L = plan_layout(nb, n_words, n_files);
-    const size_t o_tbl = L.o_tbl, o_recs = L.o_recs, o_sw = L.o_sw, o_nd = L.o_nd, o_names = L.o_names,
-                 o_cnt = L.o_cnt, o_fds = L.o_fds, o_sz = L.o_sz, o_pf = L.o_pf, o_fl = L.o_fl, o_st = L.o_st,
-                 o_fo = L.o_fo, o_fn = L.o_fn, o_xxh = L.o_xxh, o_maps = L.o_maps, total = L.total;
+    g->m = m;
+    g->r = r;
+    const PlanLayout L = plan_layout(m, r, n_words, n_files);
+    const size_t o_tbl = L.o_tbl, o_disp = L.o_disp, o_recs = L.o_recs, o_sw = L.o_sw, o_nd = L.o_nd,
+                 o_names = L.o_names, o_cnt = L.o_cnt, o_fds = L.o_fds, o_sz = L.o_sz, o_pf = L.o_pf, o_fl = L.o_fl,
+                 o_st = L.o_st, o_fo = L.o_fo, o_fn = L.o_fn, o_xxh = L.o_xxh, o_maps = L.o_maps, total = L.total;
     g->dmem = gfs__dev_alloc(ctx, total, s);
     if (!g->dmem || !(hb = (uint8_t*)gfs__host_bounce(ctx, tmp ? names_bytes : o_cnt))) {
         gfs__dev_free(ctx, tmp, s);
@@ -1899,29 +2028,32 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     uint8_t* b = (uint8_t*)g->dmem;
     cudaMemsetAsync(b + o_cnt, 0, total - o_cnt, s);
     if (tmp) {
-        /* the device-built image, then the names */
+        /* the device-built image (tags and displacements zero padded), then
+         * the names */
+        cudaMemsetAsync(b, 0, o_recs, s);
         T.tags = (uint16_t*)(b + o_tbl);
+        T.disp = (uint16_t*)(b + o_disp);
         T.rec_lo = (uint4*)(b + o_recs);
-        T.rec_hi = T.rec_lo + ns;
+        T.rec_hi = T.rec_lo + m;
         T.slot_word = (uint32_t*)(b + o_sw);
         T.next_dup = (int32_t*)(b + o_nd);
-        const uint32_t items = (uint32_t)(ns > (size_t)n_words ? ns : (size_t)n_words);
+        const uint32_t items = m > (uint32_t)n_words ? m : (uint32_t)n_words;
         k_tb_image<<<(items + 255) / 256, 256, 0, s>>>(T);
         gfs__dev_free(ctx, tmp, s);
         memset(hb, 0, names_bytes);
         for (int i = 0; i < n_files; i++) memcpy(hb + (size_t)i * GFS_NAME_MAX, paths[i], strlen(paths[i]));
         cudaMemcpyAsync(b + o_names, hb, names_bytes, cudaMemcpyHostToDevice, s);
     } else {
-        /* the host-built image: slot tags, record bytes 0..15 of every
-         * slot, then bytes 16..31, first record of each slot, duplicate
-         * chains; names */
+        /* the host-built image: slot tags, displacements, record bytes
+         * 0..15 of every slot, then bytes 16..31, first record of each
+         * slot, duplicate chains; names */
         BuildWs& W = g_ws;
         memset(hb, 0, o_cnt);
         uint16_t* tags = (uint16_t*)(hb + o_tbl);
         uint32_t* lo = (uint32_t*)(hb + o_recs);
-        uint32_t* hi = lo + ns * 4;
+        uint32_t* hi = lo + (size_t)m * 4;
         uint32_t* sw = (uint32_t*)(hb + o_sw);
-        for (size_t sl = 0; sl < ns; sl++) {
+        for (size_t sl = 0; sl < m; sl++) {
             const int w = W.slot_of[sl];
             if (w < 0) {
                 sw[sl] = 0xFFFFFFFFu;
@@ -1933,6 +2065,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
             memcpy(hi + sl * 4, kw.k + 4, 16);
             sw[sl] = (uint32_t)w;
         }
+        memcpy(hb + o_disp, W.disp.data(), (size_t)r * 2);
         if (n_words) memcpy(hb + o_nd, W.next_dup.data(), (size_t)n_words * 4);
         for (int i = 0; i < n_files; i++) memcpy(hb + o_names + (size_t)i * GFS_NAME_MAX, paths[i], strlen(paths[i]));
         cudaMemcpyAsync(b, hb, o_cnt, cudaMemcpyHostToDevice, s);
@@ -1945,10 +2078,13 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     d.fds = (const int*)(b + o_fds);
     d.sizes = (const uint64_t*)(b + o_sz);
     d.chunk_prefix = (const uint64_t*)(b + o_pf);
-    d.nb = nb;
+    d.m = m;
+    d.r = r;
+    d.hk = hk;
     d.tags = (const uint16_t*)(b + o_tbl);
+    d.disp = (const uint16_t*)(b + o_disp);
     d.rec_lo = (const uint4*)(b + o_recs);
-    d.rec_hi = d.rec_lo + (size_t)nb * 4;
+    d.rec_hi = d.rec_lo + m;
     d.slot_word = (const uint32_t*)(b + o_sw);
     d.next_dup = (const int32_t*)(b + o_nd);
     d.counts = (uint32_t*)(b + o_cnt);
@@ -1999,7 +2135,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     }
     /* shared memory: table (if it fits) + stages + token lists + scratch */
     g->sms = sms;
-    size_t with_tbl = align_up((size_t)nb * 8, 128) + align_up((size_t)nb * 16, 128) + fixed;
+    size_t with_tbl = (size_t)grep_tag_smem(m) + grep_disp_smem(r) + grep_cnt_smem(m) + fixed;
     g->smem = with_tbl <= (size_t)maxsm;
     g->smem_bytes = g->smem ? with_tbl : fixed;
     cudaFuncSetAttribute(k_grep_scan<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
@@ -2210,7 +2346,7 @@ int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts) {
 }
 
 int gfs_grep_info(gfs_grep* g, long long* out, int n) {
-    long long v[10] = {g->n_words, g->n_files, (long long)g->nb, g->smem ? 1 : 0, (long long)g->smem_bytes,
+    long long v[10] = {g->n_words, g->n_files, (long long)g->m, g->smem ? 1 : 0, (long long)g->smem_bytes,
                        (long long)g->dev.total_chunks, (long long)g->last_status[0], (long long)g->last_status[1],
                        g->build_us, g->open_us};
     int k = n < 10 ? n : 10;

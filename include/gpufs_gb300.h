@@ -52,6 +52,10 @@ typedef struct gfs_config {
  * session compares the host's ctime and size with those its cached pages
  * belong to and drops the pages if they differ. */
 #define GFS_CFG_RETAIN_CACHE 2u
+/* gfs_config.flags: build grep dictionary tables on the host instead of on
+ * the device (the device build falls back to the host build by itself when
+ * every seed fails; this flag takes that path directly) */
+#define GFS_CFG_HOST_TABLE 4u
 
 #define GFS_NSTATS 21
 /* gfs_get_stats order: device hits(page accesses), misses, evictions,

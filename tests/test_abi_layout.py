@@ -42,7 +42,7 @@ int main(void) {
     OFF(gfs_file, size); OFF(gfs_file, ctime_ns); OFF(gfs_file, map_dev);
     OFF(gfs_open_reply, size); OFF(gfs_open_reply, ctime_ns); OFF(gfs_open_reply, map_dev);
     OFF(gfs_req, offset); OFF(gfs_req, length); OFF(gfs_req, dev_addr); OFF(gfs_req, done_addr);
-    P("GFS_CFG_NO_FILE_MAP", GFS_CFG_NO_FILE_MAP); P("GFS_CFG_RETAIN_CACHE", GFS_CFG_RETAIN_CACHE);
+    P("GFS_CFG_NO_FILE_MAP", GFS_CFG_NO_FILE_MAP); P("GFS_CFG_RETAIN_CACHE", GFS_CFG_RETAIN_CACHE); P("GFS_CFG_HOST_TABLE", GFS_CFG_HOST_TABLE);
     P("GFS_NSTATS", GFS_NSTATS);
     P("GFS_XXH64_NOALLOC_MAX_FILES", GFS_XXH64_NOALLOC_MAX_FILES);
     P("GFS_SV_READ", GFS_SV_READ); P("GFS_SV_GREP", GFS_SV_GREP); P("GFS_SV_WRITE", GFS_SV_WRITE);
@@ -86,6 +86,7 @@ def test_serve_records_match(c_layout, dtype, cname):
 def test_constants_match(c_layout):
     assert g.CFG_NO_FILE_MAP == c_layout["GFS_CFG_NO_FILE_MAP"]
     assert g.CFG_RETAIN_CACHE == c_layout["GFS_CFG_RETAIN_CACHE"]
+    assert g.CFG_HOST_TABLE == c_layout["GFS_CFG_HOST_TABLE"]
     assert len(g.STAT_NAMES) == c_layout["GFS_NSTATS"]
     assert g.XXH64_NOALLOC_MAX_FILES == c_layout["GFS_XXH64_NOALLOC_MAX_FILES"]
     assert (g.SV_READ, g.SV_GREP, g.SV_WRITE) == (c_layout["GFS_SV_READ"], c_layout["GFS_SV_GREP"],

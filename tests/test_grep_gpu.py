@@ -260,7 +260,8 @@ def test_batched_counts_and_xxh64(built, shm_dir, n_ctas, pool_mb):
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def test_reference_fixture_inputs(built):
+@pytest.mark.parametrize("host_table", [False, True])
+def test_reference_fixture_inputs(built, host_table):
     """The reference's own grep inputs (the first 4000 records of
     samples/grep_text/input/dict.gpu over samples/grep_text/input/pg100.txt.small,
     copied into tests/golden by make_golden.py): the cold, resident and
@@ -272,7 +273,7 @@ def test_reference_fixture_inputs(built):
     with open(os.path.join(GOLDEN, "reference_fixture_counts.json")) as f:
         want = json.load(f)
     for lp in (12, 16):
-        with g.Session(log_page=lp, pool_bytes=64 << 20, timeout_s=20) as s:
+        with g.Session(log_page=lp, pool_bytes=64 << 20, timeout_s=20, host_table=host_table) as s:
             with g.Grep(s, dpath, [tpath]) as gr:
                 for direct in (False, False, True):
                     gr.run(0, direct=direct)
@@ -280,3 +281,39 @@ def test_reference_fixture_inputs(built):
                     assert int(got.sum()) == want["total"]
                     assert oracle.xxh64(got.astype("<u4").tobytes()) == int(want["xxh64"], 16)
             assert s.last_error() == 0
+
+
+def test_host_built_table(built, shm_dir):
+    """The host build of the dictionary table (the device build's fallback,
+    forced here) gives the same counts as the oracle, for short and long
+    words, duplicates and an empty record."""
+    paths, dpath = datagen.grep_corpus(shm_dir, n_files=3, total_bytes=3 * (1 << 20) + 5, n_vocab=6000,
+                                       n_dict=3000, seed=51)
+    recs = open(dpath, "rb").read()
+    extra = [b"x" * 17, b"y" * 24, b"z" * 32, recs[:32].rstrip(b"\0"), b""]
+    recs += b"".join(w + b"\0" * (32 - len(w)) for w in extra)
+    d2 = os.path.join(shm_dir, "hdict.gpu")
+    _write(d2, recs)
+    with open(paths[0], "ab") as f:
+        f.write(b" " + b"x" * 17 + b" " + b"y" * 24 + b"\n" + b"z" * 32 + b" " + b"y" * 25 + b" ")
+    with g.Session(log_page=16, pool_bytes=128 << 20, timeout_s=20, host_table=True) as s:
+        _check(s, d2, paths)
+        _check(s, d2, paths, direct=True)
+        assert s.last_error() == 0
+
+
+def test_table_seeds_and_sizes(built, shm_dir):
+    """Dictionaries of 1, 2, 33 and 5000 words: the device-built table gives
+    the oracle's counts."""
+    voc = datagen.vocab(8000, seed=61)
+    paths = [os.path.join(shm_dir, "s%d.txt" % i) for i in range(2)]
+    datagen.zipf_files(paths, [400000, 123457], voc, s=1.1, seed=62)
+    texts = [open(p, "rb").read() for p in paths]
+    with g.Session(log_page=16, pool_bytes=64 << 20, timeout_s=20) as s:
+        for nd in (1, 2, 33, 5000):
+            dpath = os.path.join(shm_dir, "sd%d.gpu" % nd)
+            datagen.dictionary(dpath, voc, nd, seed=63 + nd)
+            want = oracle.grep_counts(open(dpath, "rb").read(), texts, mode="fast")
+            got = g.grep_text(s, dpath, paths)
+            assert np.array_equal(got, want), nd
+        assert s.last_error() == 0
