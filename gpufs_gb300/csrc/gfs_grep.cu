@@ -69,6 +69,7 @@
 #define GR_STAGE (GR_LB + GR_CH + GR_LA + 32)
 #define GR_STAGES 3
 #define GR_WIN 32                     /* pages per window, incl. look-behind/ahead */
+#define GR_PF 6                       /* chunks prefetched into L2 ahead of their copy */
 
 extern __device__ gfs_state* g_gfs;
 
@@ -140,6 +141,11 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                  ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
+/* bring bytes into L2 ahead of their copy to shared memory (16-byte aligned
+ * address, size a multiple of 16) */
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 template <int NC>
@@ -160,8 +166,9 @@ __device__ __forceinline__ uint32_t nib4(uint32_t a) { return (a * 0x00204081u) 
 __device__ __forceinline__ uint32_t alpha16(uint4 v) {
     return nib4(alpha4(v.x)) | (nib4(alpha4(v.y)) << 4) | (nib4(alpha4(v.z)) << 8) | (nib4(alpha4(v.w)) << 12);
 }
+/* [A-Za-z_]: bit 5 folds upper case onto lower case */
 __device__ __forceinline__ uint32_t is_alpha(uint32_t c) {
-    return ((c - 65u < 26u) || (c - 97u < 26u) || c == 95u) ? 1u : 0u;
+    return (uint32_t)((c | 32u) - 97u < 26u) | (uint32_t)(c == 95u);
 }
 
 /* key of a token of len <= 16 at byte st of a 4-byte aligned smem buffer
@@ -422,17 +429,24 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, c
     const uint32_t off = seg0 + 16u * (uint32_t)lane;
     const uint4 v = *(const uint4*)(base + off);
     /* letters among the staged bytes of this file (< avail); token starts
-     * only among the chunk's own bytes (< clen) */
-    uint32_t ax = alpha16(v);
-    ax &= off >= avail ? 0u : (avail - off >= 16u ? 0xFFFFu : ((1u << (avail - off)) - 1u));
-    const uint32_t a = ax & (off >= clen ? 0u : (clen - off >= 16u ? 0xFFFFu : ((1u << (clen - off)) - 1u)));
+     * only among the chunk's own bytes (< clen).  Every segment but a file's
+     * last has its bytes and the 32 after it staged (and then lies inside
+     * the chunk): no masks (a warp-uniform test). */
+    uint32_t ax = alpha16(v), a = ax;
+    const uint32_t q = seg0 + GR_SEG + (uint32_t)lane;
+    uint32_t cont;
+    if (__all_sync(0xFFFFFFFFu, seg0 + GR_SEG + 32u <= avail)) {
+        cont = __ballot_sync(0xFFFFFFFFu, is_alpha(base[q]));
+    } else {
+        ax &= off >= avail ? 0u : (avail - off >= 16u ? 0xFFFFu : ((1u << (avail - off)) - 1u));
+        a = ax & (off >= clen ? 0u : (clen - off >= 16u ? 0xFFFFu : ((1u << (clen - off)) - 1u)));
+        cont = __ballot_sync(0xFFFFFFFFu, q < avail && is_alpha(base[q]));
+    }
     /* byte before the segment (the look-behind when seg0 == 0; nothing before
      * the file's first byte) and the 32 bytes after it, one per lane */
     const uint32_t before = (seg0 == 0u && d.pos == 0u) ? 0u : is_alpha(base[(int)seg0 - 1]);
     uint32_t pb = __shfl_up_sync(0xFFFFFFFFu, ax >> 15, 1);
     if (lane == 0) pb = before;
-    const uint32_t q = seg0 + GR_SEG + (uint32_t)lane;
-    const uint32_t cont = __ballot_sync(0xFFFFFFFFu, q < avail && is_alpha(base[q]));
     ((uint16_t*)bm)[lane] = (uint16_t)ax;
     if (lane == 0) {
         bm[16] = cont;
@@ -448,8 +462,18 @@ __device__ __forceinline__ void scan_segment(const GrepDev& P, const Tbl& tbl, c
         if (lane >= dd) incl += t;
     }
     const uint32_t n_s = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    uint32_t js = incl - cnt;
-    for (uint32_t m = starts; m; m &= m - 1u) slist[js++] = (uint16_t)(off + (uint32_t)(__ffs(m) - 1));
+    /* a lane's starts into the list: four unrolled predicated steps (16
+     * bytes of text rarely hold more tokens), then a warp-uniform loop */
+    const uint32_t js = incl - cnt;
+    uint32_t mm = starts;
+#pragma unroll
+    for (uint32_t qq = 0; qq < 4u; qq++) {
+        const uint32_t pos = off + (uint32_t)(__ffs(mm) - 1);
+        if (mm) slist[js + qq] = (uint16_t)pos;
+        mm &= mm - 1u;
+    }
+    if (__any_sync(0xFFFFFFFFu, mm != 0u))
+        for (uint32_t qq = 4u; mm; qq++, mm &= mm - 1u) slist[js + qq] = (uint16_t)(off + (uint32_t)(__ffs(mm) - 1));
     __syncwarp();
     /* rounds of two tokens per lane; a last round of at most 32 tokens takes
      * one per lane (warp-uniform choice) */
@@ -607,6 +631,23 @@ __device__ bool stream_file(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t*
                         bulk_g2s(dst + (GR_LB - lbb) + done, src, piece, &sh.full[s]);
                         done += piece;
                     }
+                    /* the chunk GR_PF ahead (inside this window) into L2, so
+                     * its copy finds it there: the stage ring alone holds
+                     * few bytes in flight against HBM latency */
+                    if (kk + GR_PF < kw) {
+                        const uint64_t pa = (kk + GR_PF) * CH;
+                        uint64_t pe = pa + CH < fsize ? pa + CH : fsize;
+                        pe = (pe + 15u) & ~15ull;
+                        for (uint64_t q = pa; q < pe;) {
+                            const uint32_t pg = (uint32_t)(q >> lp);
+                            const uint32_t inpg = (uint32_t)(q & pmask);
+                            uint32_t piece = page - inpg;
+                            if (piece > pe - q) piece = (uint32_t)(pe - q);
+                            if (pg - lb < n)
+                                bulk_prefetch_l2(S->pool + ((size_t)sh.frames[buf][pg - lb] << lp) + inpg, piece);
+                            q += piece;
+                        }
+                    }
                 }
             }
             __syncwarp();
@@ -643,7 +684,7 @@ __device__ void emit_marker(const GrepDev& P, Shared& sh, int f, uint32_t fseq, 
 
 /* Producer of the plain scan: the CTA's static run of chunks [c0, c1) of
  * the concatenated corpus. */
-__device__ void producer(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* stages, uint64_t c0, uint64_t c1) {
+__device__ __noinline__ void producer(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* stages, uint64_t c0, uint64_t c1) {
     const int lane = threadIdx.x & 31;
     Window prev = {0, 0, 1, 0, false};
     uint32_t g = 0;
@@ -672,7 +713,7 @@ __device__ void producer(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* st
  * first), each numbered in sequence for the consumers' per-file flushes;
  * an empty file is one empty stage (the hasher still finishes its XXH64);
  * the end is an f = -1 stage numbered one past the last file. */
-__device__ void producer_batch(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* stages) {
+__device__ __noinline__ void producer_batch(gfs_state* S, const GrepDev& P, Shared& sh, uint8_t* stages) {
     const int lane = threadIdx.x & 31;
     Window prev = {0, 0, 1, 0, false};
     uint32_t g = 0, fseq = 0;
@@ -714,7 +755,7 @@ __device__ __forceinline__ bool cbar_wait(Shared& sh, const GrepDev& P, uint32_t
  * chunks in order (chunks are whole 32-byte stripes except a file's last),
  * lanes 0..3 carrying the four accumulators; it releases every stage it has
  * read like a consumer. */
-__device__ void hasher(const GrepDev& P, Shared& sh, uint8_t* stages) {
+__device__ __noinline__ void hasher(const GrepDev& P, Shared& sh, uint8_t* stages) {
     const int lane = threadIdx.x & 31;
     uint64_t v = gfsx::acc_init(lane & 3);
     for (uint32_t g = 0;; g++) {
@@ -1433,7 +1474,8 @@ struct TbDev {
     int* bkeys;          /* r x GREP_MAX_BUCKET: each bucket's representatives */
     uint16_t* dsp;       /* r displacements */
     unsigned long long* hset; /* duplicate-hash check: cap entries, ~0 empty */
-    uint32_t* fail;      /* [0] set while the current seed fails; [1] the seed that succeeded */
+    uint32_t* fail;      /* [0] set while the current seed fails; [1] the seed that succeeded;
+                            [2] the current seed's largest bucket */
     uint32_t seed0, n_seeds; /* seeds tried: seed0 .. seed0 + n_seeds - 1 */
     grep_hashk hk;       /* filled by the host from the seed that succeeded */
     /* the image */
@@ -1541,7 +1583,10 @@ static __global__ void __launch_bounds__(256) k_tb_search(TbDev T) {
     for (uint32_t sd = T.seed0; sd < T.seed0 + T.n_seeds; sd++) {
         grep_hashk hk;
         grep_hash_seed(sd, &hk);
-        if (tid == 0) T.fail[0] = 0u;
+        if (tid == 0) {
+            T.fail[0] = 0u;
+            T.fail[2] = 0u;
+        }
         for (uint32_t b = tid; b < T.r; b += nth) {
             T.bsize[b] = 0u;
             T.dsp[b] = 0;
@@ -1571,10 +1616,12 @@ static __global__ void __launch_bounds__(256) k_tb_search(TbDev T) {
                 const uint32_t i = atomicAdd(&T.bsize[b], 1u);
                 if (i < GREP_MAX_BUCKET) T.bkeys[(size_t)b * GREP_MAX_BUCKET + i] = w;
                 else atomicOr(&T.fail[0], 1u);
+                atomicMax(&T.fail[2], i + 1u); /* the largest bucket */
             }
         grid.sync();
         bool failed = *(volatile uint32_t*)&T.fail[0] != 0u;
-        for (int z = GREP_MAX_BUCKET; z >= 1 && !failed; z--) {
+        const int zmax = (int)min(*(volatile uint32_t*)&T.fail[2], (uint32_t)GREP_MAX_BUCKET);
+        for (int z = zmax; z >= 1 && !failed; z--) {
             for (uint32_t b = gw; b < T.r; b += nw) {
                 if (T.bsize[b] != (uint32_t)z) continue;
                 const int* keys = T.bkeys + (size_t)b * GREP_MAX_BUCKET;
