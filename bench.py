@@ -604,7 +604,7 @@ def run_workload(args, rank, ws, local, td, data_dir):
         mbytes = rows * cols * 4
         sess = g.Session(log_page=21, pool_bytes=mbytes + (512 << 20), max_files=64, host_workers=workers,
                          staging_depth=4, timeout_s=120, device=local)
-        nblocks, nthreads = 152, 1024  # one wave: every block holds the files open for the whole launch
+        nblocks, nthreads = 152, 512  # one wave: every block holds the files open for the whole launch
         clk.start()
         for _ in range(warm):
             sess.bigmatrix(vp, mp, op, nblocks, nthreads)

@@ -1,0 +1,344 @@
+/*
+ * bigmatrix_mmap over the GPU file system (samples/bigmatrix_mmap/bigmatrix_mmap.cu:66-168):
+ * y = A x with A (rows x cols FP32, row-major) and x read through gmmap, y
+ * written through gmmap of a write-once file.
+ *
+ * Each block owns a contiguous run of rows and keeps one matrix page mapped
+ * at a time (the reference's get_row, :45-60, remaps only when the cursor
+ * leaves the page); eight whole rows of a page are one pass in which every
+ * thread keeps sixteen 16-byte loads in flight; rows are reduced in a fixed
+ * order (warp shuffles, then one warp over the partials), so results are
+ * deterministic -- the reference adds the per-thread partials with a
+ * shared-memory float atomicAdd (:35), whose order varies run to run.
+ *
+ * This translation unit is compiled without the 64-register cap of the
+ * device-API units: the kernel is bounded at 512 threads a block, which
+ * leaves each thread the registers of its sixteen loads.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+#include <sys/stat.h>
+
+#include "fs_calls.cu.h"
+#include "gfs_device.cuh"
+#include "gfs_block.cuh"
+#include "gfs_runtime.h"
+
+extern __device__ gfs_state* g_gfs;
+
+/* gfs_calls.cu: a read-only file's bytes in its registered host mapping */
+__device__ const void* gfs_direct_addr(int fd, unsigned long long off, unsigned long long size);
+/* gfs_apps.cu */
+long long gfs__sum_results(long long* d, int n, cudaStream_t s);
+
+namespace {
+
+__device__ unsigned int g_init_lock; /* INIT_LOCK of the reference sample */
+
+/* block-wide sum of one float per thread, fixed order */
+__device__ float block_sum(float v, float* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    float r = 0.f;
+    if (warp == 0) {
+        r = lane < nw ? red[lane] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xFFFFFFFFu, r, o);
+    }
+    __syncthreads();
+    return r; /* valid in warp 0 */
+}
+
+/* partial dot of n floats (a, b 16-byte aligned when n4 path) */
+__device__ float dot_part(const float* a, const float* b, uint32_t n) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    const uint32_t n4 = ((((uintptr_t)a | (uintptr_t)b) & 15u) == 0u) ? n / 4u : 0u;
+    const float4* a4 = (const float4*)a;
+    const float4* b4 = (const float4*)b;
+    const uint32_t bd = blockDim.x;
+    uint32_t i = threadIdx.x;
+    /* two independent 16-byte row loads in flight per thread */
+    for (; i + bd < n4; i += 2u * bd) {
+        const float4 p0 = __ldcg(a4 + i), p1 = __ldcg(a4 + i + bd);
+        const float4 q0 = __ldg(b4 + i), q1 = __ldg(b4 + i + bd);
+        s0 = fmaf(p0.x, q0.x, s0); s1 = fmaf(p0.y, q0.y, s1); s2 = fmaf(p0.z, q0.z, s2); s3 = fmaf(p0.w, q0.w, s3);
+        s0 = fmaf(p1.x, q1.x, s0); s1 = fmaf(p1.y, q1.y, s1); s2 = fmaf(p1.z, q1.z, s2); s3 = fmaf(p1.w, q1.w, s3);
+    }
+    for (; i < n4; i += bd) {
+        const float4 p = __ldcg(a4 + i), q = __ldg(b4 + i);
+        s0 = fmaf(p.x, q.x, s0);
+        s1 = fmaf(p.y, q.y, s1);
+        s2 = fmaf(p.z, q.z, s2);
+        s3 = fmaf(p.w, q.w, s3);
+    }
+    for (uint32_t i = 4u * n4 + threadIdx.x; i < n; i += blockDim.x) s0 = fmaf(a[i], b[i], s0);
+    return (s0 + s1) + (s2 + s3);
+}
+
+/* Eight rows at once: a (16-byte aligned) holds rows of stride4 float4s,
+ * b the vector.  Each thread takes two column steps per iteration: two
+ * float4s of b and the eight rows' float4s beside each (sixteen 16-byte
+ * loads in flight, about 90 registers, which the 512-thread launch bound
+ * leaves room for); the eight sums are reduced together in a fixed order.
+ * y[0..7] (shared) are valid after return. */
+__device__ __noinline__ void dot_rows8(const float* a, size_t stride4, const float* b, uint32_t n4, float* red, float* y) {
+    float s[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) s[k] = 0.f;
+    const float4* a4 = (const float4*)a;
+    const float4* b4 = (const float4*)b;
+    const uint32_t bd = blockDim.x;
+    uint32_t i = threadIdx.x;
+    for (; i + bd < n4; i += 2u * bd) {
+        const float4 q0 = __ldg(b4 + i), q1 = __ldg(b4 + i + bd);
+        float4 p0[8], p1[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            p0[k] = __ldcs(a4 + (size_t)k * stride4 + i);
+            p1[k] = __ldcs(a4 + (size_t)k * stride4 + i + bd);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            s[k] = fmaf(p0[k].w, q0.w, fmaf(p0[k].z, q0.z, fmaf(p0[k].y, q0.y, fmaf(p0[k].x, q0.x, s[k]))));
+            s[k] = fmaf(p1[k].w, q1.w, fmaf(p1[k].z, q1.z, fmaf(p1[k].y, q1.y, fmaf(p1[k].x, q1.x, s[k]))));
+        }
+    }
+    for (; i < n4; i += bd) {
+        const float4 q = __ldg(b4 + i);
+        float4 p[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) p[k] = __ldcs(a4 + (size_t)k * stride4 + i);
+#pragma unroll
+        for (int k = 0; k < 8; k++) s[k] = fmaf(p[k].w, q.w, fmaf(p[k].z, q.z, fmaf(p[k].y, q.y, fmaf(p[k].x, q.x, s[k]))));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xFFFFFFFFu, s[k], o);
+    }
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 8; k++) red[k * 32 + warp] = s[k];
+    __syncthreads();
+    if (warp == 0)
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            float r = lane < nw ? red[k * 32 + lane] : 0.f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xFFFFFFFFu, r, o);
+            if (lane == 0) y[k] = r;
+        }
+    __syncthreads();
+}
+
+/* y = A x.  vec/mat/out: device file names; x_buf: cols floats of scratch
+ * per block when x does not fit in one page. */
+/* direct: read the matrix straight from its registered host mapping when it
+ * has one (one pass over a cold matrix: no cache pages, SM loads over the
+ * host link) */
+__global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
+    k_bigmatrix(const char* f_v, const char* f_m, const char* f_o, float* x_scratch, long long* res, int direct) {
+    __shared__ float red[8 * 32];
+    __shared__ float ys[8];
+    __shared__ int s_fail;
+    const uint32_t page = g_gfs->page_size;
+    int zfd_m = gopen(f_m, O_GRDONLY);
+    int zfd_o = gopen(f_o, O_GWRONCE);
+    int zfd_v = gopen(f_v, O_GRDONLY);
+    if (zfd_m < 0 || zfd_o < 0 || zfd_v < 0) {
+        if (threadIdx.x == 0) res[blockIdx.x] = zfd_m < 0 ? zfd_m : (zfd_o < 0 ? zfd_o : zfd_v);
+        if (zfd_m >= 0) gclose(zfd_m);
+        if (zfd_o >= 0) gclose(zfd_o);
+        if (zfd_v >= 0) gclose(zfd_v);
+        return;
+    }
+    /* the first block truncates the output, the others wait for it
+     * (bigmatrix_mmap.cu:88-97, INIT_LOCK) */
+    if (threadIdx.x == 0) {
+        s_fail = 0;
+        unsigned int prev = atomicCAS(&g_init_lock, 0u, 1u);
+        if (prev == 0u) {
+            single_thread_ftruncate(zfd_o, 0);
+            __threadfence();
+            atomicExch(&g_init_lock, 2u);
+        } else {
+            unsigned long long deadline = gfs_globaltimer() + 30000000000ULL;
+            while (atomicAdd(&g_init_lock, 0u) != 2u) {
+                if (gfs_globaltimer() > deadline) { s_fail = -GFS_ETIMEDOUT; break; }
+                __nanosleep(1000);
+            }
+        }
+    }
+    __syncthreads();
+    const uint64_t size_v = fstat(zfd_v) / 4, size_m = fstat(zfd_m) / 4;
+    const uint64_t cols = size_v, rows = cols ? size_m / cols : 0;
+    long long result = s_fail;
+    const float* x = nullptr;
+    volatile void* xmap = (volatile void*)-1;
+    if (!result && cols) {
+        if (cols * 4 <= page) {
+            xmap = gmmap(NULL, cols * 4, 0, O_GRDONLY, zfd_v, 0);
+            if (xmap == (volatile void*)-1) result = -GFS_EIO;
+            x = (const float*)xmap;
+        } else {
+            float* xs = x_scratch + (size_t)blockIdx.x * cols;
+            long long got = (long long)gread(zfd_v, 0, cols * 4, (uchar*)xs);
+            if (got != (long long)(cols * 4)) result = got < 0 ? got : -GFS_EIO;
+            x = xs;
+        }
+    }
+    const uint64_t per = rows ? (rows + gridDim.x - 1) / gridDim.x : 0;
+    const uint64_t r0 = (uint64_t)blockIdx.x * per, r1 = r0 + per < rows ? r0 + per : rows;
+    volatile uint8_t* mpage = (volatile uint8_t*)-1;
+    uint64_t mbase = ~0ull;
+    volatile uint8_t* opage = (volatile uint8_t*)-1;
+    uint64_t obase = ~0ull;
+    /* map the output page holding y[r] (block-collective) and store y there
+     * (thread 0; gmunmap of that page later is block-collective, so the
+     * store is ordered before it without a barrier of its own) */
+    auto put_y = [&](uint64_t r, float y) {
+        const uint64_t oo = r * 4, ob = oo / page * page;
+        if (ob != obase) {
+            if (opage != (volatile uint8_t*)-1) gmunmap(opage, 0);
+            uint64_t olen = rows * 4 - ob < page ? rows * 4 - ob : page;
+            opage = (volatile uint8_t*)gmmap(NULL, olen, 0, O_GWRONCE, zfd_o, (off_t)ob);
+            if (opage == (volatile uint8_t*)-1) { result = -GFS_EIO; obase = ~0ull; return; }
+            obase = ob;
+        }
+        if (threadIdx.x == 0) *(volatile float*)(opage + (oo - ob)) = y;
+    };
+    /* the matrix page holding byte pb, mapped (block-collective) */
+    auto map_m = [&](uint64_t pb) {
+        if (pb == mbase) return;
+        if (mpage != (volatile uint8_t*)-1) gmunmap(mpage, 0);
+        uint64_t mlen = size_m * 4 - pb < page ? size_m * 4 - pb : page;
+        mpage = (volatile uint8_t*)gmmap(NULL, mlen, 0, O_GRDONLY, zfd_m, (off_t)pb);
+        if (mpage == (volatile uint8_t*)-1) { result = -GFS_EIO; mbase = ~0ull; return; }
+        mbase = pb;
+    };
+    const bool vec4 = (cols & 3u) == 0u && (((uintptr_t)x) & 15u) == 0u;
+    const uint8_t* dm = (direct && !result) ? (const uint8_t*)gfs_direct_addr(zfd_m, 0, size_m * 4) : nullptr;
+    if (dm) {
+        /* the whole matrix in one mapping: eight-row passes anywhere */
+        for (uint64_t r = r0; r < r1 && !result;) {
+            if (vec4 && r + 8 <= r1) {
+                dot_rows8((const float*)(dm + r * cols * 4), cols / 4, x, (uint32_t)(cols / 4), red, ys);
+                for (int k = 0; k < 8 && !result; k++) put_y(r + (uint64_t)k, ys[k]);
+                r += 8;
+            } else {
+                float y = block_sum(dot_part((const float*)(dm + r * cols * 4), x, (uint32_t)cols), red);
+                put_y(r, y);
+                r++;
+            }
+        }
+    }
+    for (uint64_t r = dm ? r1 : r0; r < r1 && !result;) {
+        const uint64_t rbeg = r * cols * 4, rend = rbeg + cols * 4;
+        const uint64_t pb0 = rbeg / page * page;
+        if (vec4 && r + 8 <= r1 && rbeg + 8 * cols * 4 <= pb0 + page) {
+            /* eight whole rows inside one page */
+            map_m(pb0);
+            if (result) break;
+            dot_rows8((const float*)(mpage + (rbeg - pb0)), cols / 4, x, (uint32_t)(cols / 4), red, ys);
+            for (int k = 0; k < 8 && !result; k++) put_y(r + (uint64_t)k, ys[k]);
+            r += 8;
+            continue;
+        }
+        /* one row; it may span pages: walk its segments */
+        float acc = 0.f;
+        for (uint64_t pos = rbeg; pos < rend && !result;) {
+            const uint64_t pb = pos / page * page;
+            map_m(pb);
+            if (result) break;
+            const uint64_t seg_end = pb + page < rend ? pb + page : rend;
+            acc += dot_part((const float*)(mpage + (pos - pb)), x + (pos - rbeg) / 4, (uint32_t)((seg_end - pos) / 4));
+            pos = seg_end;
+        }
+        if (result) break;
+        float y = block_sum(acc, red);
+        put_y(r, y);
+        r++;
+    }
+    if (mpage != (volatile uint8_t*)-1) gmunmap(mpage, 0);
+    if (opage != (volatile uint8_t*)-1) gmunmap(opage, 0);
+    if (xmap != (volatile void*)-1) gmunmap(xmap, 0);
+    int c0 = gclose(zfd_m), c1 = gclose(zfd_v), c2 = gclose(zfd_o);
+    if (threadIdx.x == 0)
+        res[blockIdx.x] = result ? result : (c0 < 0 ? c0 : (c1 < 0 ? c1 : (c2 < 0 ? c2 : (long long)(r1 > r0 ? r1 - r0 : 0))));
+}
+
+} // namespace
+
+extern "C" {
+
+void gfs__preload_bigmatrix() {
+    cudaFuncAttributes a;
+    cudaFuncGetAttributes(&a, k_bigmatrix);
+}
+
+static int bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
+                     int nthreads, float* kernel_ms, int direct) {
+    if (!vec_path || !mat_path || !out_path || nblocks < 1 || nthreads < 32 || nthreads > GFS_BIGMATRIX_THREADS)
+        return -GFS_EINVAL;
+    if (strlen(vec_path) >= GFS_NAME_MAX || strlen(mat_path) >= GFS_NAME_MAX || strlen(out_path) >= GFS_NAME_MAX)
+        return -GFS_EINVAL;
+    if (gfs__activate(ctx)) return -GFS_EIO;
+    cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
+    char names[3 * GFS_NAME_MAX];
+    memset(names, 0, sizeof names);
+    memcpy(names, vec_path, strlen(vec_path));
+    memcpy(names + GFS_NAME_MAX, mat_path, strlen(mat_path));
+    memcpy(names + 2 * GFS_NAME_MAX, out_path, strlen(out_path));
+    char* d = (char*)gfs__scratch(ctx, 256 + sizeof(long long) * (size_t)nblocks);
+    if (!d) return -GFS_ENOMEM;
+    long long* res = (long long*)(d + 256);
+    cudaMemcpyAsync(d, names, sizeof names, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(res, 0, sizeof(long long) * (size_t)nblocks, s);
+    unsigned int zero = 0;
+    cudaMemcpyToSymbolAsync(g_init_lock, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, s);
+    /* x scratch only when x does not fit a page */
+    float* xs = nullptr;
+    long long vbytes = 0;
+    {
+        struct stat st;
+        if (stat(vec_path, &st) == 0) vbytes = (long long)st.st_size;
+    }
+    if ((uint64_t)vbytes > gfs_page_size(ctx) && cudaMalloc(&xs, (size_t)vbytes * (size_t)nblocks) != cudaSuccess)
+        return -GFS_ENOMEM;
+    cudaEvent_t a, b;
+    if (kernel_ms) {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, s);
+    }
+    k_bigmatrix<<<nblocks, nthreads, 0, s>>>(d, d + GFS_NAME_MAX, d + 2 * GFS_NAME_MAX, xs, res, direct);
+    cudaError_t le = cudaGetLastError();
+    if (kernel_ms) {
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(kernel_ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+    long long r = le == cudaSuccess ? gfs__sum_results(res, nblocks, s) : -GFS_EINVAL;
+    if (xs) cudaFree(xs);
+    return r < 0 ? (int)r : 0;
+}
+
+int gfs_bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
+                  int nthreads, float* kernel_ms) {
+    return bigmatrix(ctx, vec_path, mat_path, out_path, nblocks, nthreads, kernel_ms, 0);
+}
+
+int gfs_bigmatrix_direct(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
+                         int nthreads, float* kernel_ms) {
+    return bigmatrix(ctx, vec_path, mat_path, out_path, nblocks, nthreads, kernel_ms, 1);
+}
+
+} /* extern "C" */

@@ -1238,6 +1238,7 @@ void gfs__preload_kernels() {
     gfs__preload_workloads();
     gfs__preload_grep();
     gfs__preload_apps();
+    gfs__preload_bigmatrix();
 }
 
 long long gfs_retained_pages(gfs_ctx* c) { return c ? (long long)c->retained_pages : -GFS_EINVAL; }

@@ -34,6 +34,7 @@ void gfs__preload_runtime(void);
 void gfs__preload_workloads(void);
 void gfs__preload_grep(void);
 void gfs__preload_apps(void);
+void gfs__preload_bigmatrix(void);
 const gfs_state* gfs__host_state(gfs_ctx* c);
 double _timestamp(void);
 #ifdef __cplusplus

@@ -161,7 +161,9 @@ int gfs_memcopy(gfs_ctx* ctx, const char* src, const char* dst, int nblocks, int
  * y = A x, A read through gmmap page windows (rows x cols FP32 row-major,
  * cols = size(vec)/4), x mapped once (read with gread when larger than a
  * page), y written through gmmap of out_path (write-once, truncated first).
- * FP32 accumulation, deterministic reduction order. */
+ * FP32 accumulation, deterministic reduction order.  nthreads: 32 ..
+ * GFS_BIGMATRIX_THREADS per block (-GFS_EINVAL beyond). */
+#define GFS_BIGMATRIX_THREADS 512
 int gfs_bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, const char* out_path, int nblocks,
                   int nthreads, float* kernel_ms);
 /* The same GEMV read once: when the matrix file has a registered host
