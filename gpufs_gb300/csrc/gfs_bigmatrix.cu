@@ -289,6 +289,8 @@ static int bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, c
     if (strlen(vec_path) >= GFS_NAME_MAX || strlen(mat_path) >= GFS_NAME_MAX || strlen(out_path) >= GFS_NAME_MAX)
         return -GFS_EINVAL;
     if (gfs__activate(ctx)) return -GFS_EIO;
+    gfs__premap(ctx, vec_path);
+    gfs__premap(ctx, mat_path);
     cudaStream_t s = (cudaStream_t)gfs_kernel_stream(ctx);
     char names[3 * GFS_NAME_MAX];
     memset(names, 0, sizeof names);

@@ -139,11 +139,50 @@ __device__ __forceinline__ void blk_copy_round(gfs_state* S, const int* frames, 
 /* ------------------------------------------------------------------ */
 /* read                                                                */
 /* ------------------------------------------------------------------ */
+/* Fill the fresh frames of a round (bit j of `fresh`: frames[j] holds page
+ * first + j, still LOADING) from the file's registered host mapping: the
+ * whole block sweeps each page in turn, consecutive threads on consecutive
+ * 16-byte units (the mapping is page aligned), four loads in flight per
+ * thread, so a block keeps its threads x 64 bytes in flight over the host
+ * link. */
+__device__ __forceinline__ void blk_fill_round(gfs_state* S, const int* frames, unsigned fresh, uint32_t first,
+                                               uint64_t map_dev, uint64_t fsize) {
+    const uint64_t tid = (uint64_t)blk_tid(), nthr = (uint64_t)blk_nthr();
+    const uint32_t lp = S->log_page;
+    for (unsigned m = fresh; m; m &= m - 1u) {
+        const int j = __ffs(m) - 1;
+        const uint64_t pst = ((uint64_t)(first + (uint32_t)j)) << lp;
+        uint8_t* dst = frame_data(S, (uint32_t)frames[j]);
+        if (!map_dev || pst >= fsize) {
+            /* no bytes behind the page (a fresh page without a mapping, or
+             * past the end of the file): hand out zeros */
+            for (uint64_t i = tid; i < ((1ull << lp) >> 4); i += nthr) ((uint4*)dst)[i] = make_uint4(0, 0, 0, 0);
+            continue;
+        }
+        const uint64_t len = fsize - pst < (1ull << lp) ? fsize - pst : (1ull << lp);
+        const uint4* src = (const uint4*)(uintptr_t)(map_dev + pst);
+        uint4* d4 = (uint4*)dst;
+        const uint64_t n16 = len >> 4;
+        uint64_t i = tid;
+        for (; i + 3u * nthr < n16; i += 4u * nthr) {
+            const uint4 a = src[i], b = src[i + nthr], c = src[i + 2u * nthr], d = src[i + 3u * nthr];
+            d4[i] = a;
+            d4[i + nthr] = b;
+            d4[i + 2u * nthr] = c;
+            d4[i + 3u * nthr] = d;
+        }
+        for (; i < n16; i += nthr) d4[i] = src[i];
+        const uint8_t* s1 = (const uint8_t*)src;
+        for (uint64_t q = (n16 << 4) + tid; q < len; q += nthr) dst[q] = s1[q];
+    }
+}
+
 __device__ __noinline__ long long blk_read(gfs_state* S, int fd, uint64_t off, uint64_t size, uint8_t* buf) {
     __shared__ PinFile s_pf;
     __shared__ uint64_t s_off, s_size;
     __shared__ uint8_t* s_buf;
     __shared__ int s_frames[32];
+    __shared__ unsigned s_fresh, s_later;
     __shared__ int s_err, s_round, s_retry;
     const int tid = blk_tid(), nthr = blk_nthr();
     const unsigned m0 = nthr >= 32 ? 0xFFFFFFFFu : ((1u << nthr) - 1u); /* lanes of warp 0 */
@@ -174,22 +213,29 @@ __device__ __noinline__ long long blk_read(gfs_state* S, int fd, uint64_t off, u
         if (npages > s_round) npages = s_round;
         if (tid < 32) {
             int r = 0;
+            bool fresh = false;
             if (tid < npages) {
-                bool fresh;
-                r = pin_page(S, s_pf, first + (uint32_t)tid, GFS_PIN_READ | (npages > 1 ? GFS_PIN_NOALLOC : 0), &fresh);
-                if (r >= 0 && fresh) {
-                    /* no host bytes behind this page (cannot happen below the
-                     * clamped size of an open file): hand out zeros */
-                    uint32_t* d = (uint32_t*)frame_data(S, (uint32_t)r);
-                    for (uint32_t k = 0; k < (S->page_size >> 2); k++) d[k] = 0u;
-                    publish_valid(S, (uint32_t)r);
-                }
+                /* a miss of a file with a registered mapping is filled by
+                 * this block (SM loads over the host link); others by the
+                 * host */
+                r = pin_page(S, s_pf, first + (uint32_t)tid,
+                             GFS_PIN_READ | GFS_PIN_SMFILL | (npages > 1 ? GFS_PIN_NOALLOC : 0), &fresh);
                 s_frames[tid] = r;
             }
+            const unsigned fr_mask = __ballot_sync(m0, tid < npages && r >= 0 && fresh);
             unsigned nomem = __ballot_sync(m0, tid < npages && r == -GFS_ENOMEM);
-            unsigned bad = __ballot_sync(m0, tid < npages && r < 0 && r != -GFS_ENOMEM);
+            unsigned bad = __ballot_sync(m0, tid < npages && r < 0 && r != -GFS_ENOMEM && r != -GFS_EAGAIN);
+            const unsigned later = __ballot_sync(m0, tid < npages && r == -GFS_EAGAIN);
             if (bad || nomem) {
-                if (tid < npages && r >= 0) unpin(S, (uint32_t)r);
+                if (tid < npages && r >= 0) {
+                    if (fresh) { /* give back a page never filled */
+                        gfs_frame* F = &S->frames[r];
+                        index_remove(S, ld_rlx64(&F->key), (uint32_t)r);
+                        release_owned(S, (uint32_t)r, GFS_FS_LOADING, 1u);
+                    } else {
+                        unpin(S, (uint32_t)r);
+                    }
+                }
                 int e = bad ? __shfl_sync(m0, r, __ffs(bad) - 1) : 0;
                 if (tid == 0) {
                     s_retry = 1;
@@ -199,11 +245,48 @@ __device__ __noinline__ long long blk_read(gfs_state* S, int fd, uint64_t off, u
                 }
             } else if (tid == 0) {
                 s_retry = 0;
+                s_fresh = fr_mask;
+                s_later = later;
             }
         }
         __syncthreads();
         if (s_err) return s_err;
         if (s_retry) continue;
+        if (s_fresh) {
+            blk_fill_round(S, s_frames, s_fresh, first, s_pf.map_dev, s_pf.size);
+            __syncthreads();
+            if (tid < npages && ((s_fresh >> tid) & 1u)) {
+                const uint64_t pst = ((uint64_t)(first + (uint32_t)tid)) << lp;
+                const uint64_t len = !s_pf.map_dev || pst >= s_pf.size ? 0u
+                                     : (s_pf.size - pst < (1ull << lp) ? s_pf.size - pst : (1ull << lp));
+                st_rlx(&S->frames[s_frames[tid]].content, (uint32_t)len);
+                publish_valid(S, (uint32_t)s_frames[tid]);
+            }
+        }
+        if (s_later) {
+            /* pages another block was loading: now that every page this
+             * block filled is published, wait for them (a miss by then is
+             * filled by the host inside pin_page) */
+            __syncthreads();
+            if (tid < npages && ((s_later >> tid) & 1u)) {
+                bool fresh = false;
+                int r = pin_page(S, s_pf, first + (uint32_t)tid, GFS_PIN_READ, &fresh);
+                if (r >= 0 && fresh) { /* no bytes behind it: zeros */
+                    uint32_t* d = (uint32_t*)frame_data(S, (uint32_t)r);
+                    for (uint32_t k = 0; k < (S->page_size >> 2); k++) d[k] = 0u;
+                    publish_valid(S, (uint32_t)r);
+                }
+                s_frames[tid] = r;
+                if (r < 0) atomicCAS(&s_err, 0, r);
+            }
+            __syncthreads();
+            if (s_err) {
+                /* give back the pages held */
+                if (tid < npages && s_frames[tid] >= 0) unpin(S, (uint32_t)s_frames[tid]);
+                __syncthreads();
+                return s_err;
+            }
+        }
         uint64_t pend = ((uint64_t)(first + (uint32_t)npages)) << lp;
         uint64_t end = base + total < pend ? base + total : pend;
         blk_copy_round(S, s_frames, first, npages, pos, end, s_buf, base, false);
@@ -418,25 +501,74 @@ __device__ __noinline__ int blk_munmap(gfs_state* S, const volatile void* addr) 
 /* Write back every dirty frame of slot fd, spread over the block's threads
  * (each thread one frame at a time, so the block keeps many write-backs in
  * flight).  Returns 0 or the first error. */
+/* Write back every dirty frame of slot fd.  Each warp works in rounds: every
+ * lane takes its next dirty frame of the file (lanes own interleaved words
+ * of the dirty bitmap) and a write-stage slot; the warp copies the lanes'
+ * frames into their slots one after another with coalesced 16-byte stores
+ * (host memory over the link), then every lane sends its request, so a
+ * block keeps its threads' write-backs in flight and the host only merges
+ * and writes.  A frame without a slot is copied by the host.  Returns 0 or
+ * the first error. */
 __device__ __noinline__ int blk_flush(gfs_state* S, int fd) {
     __shared__ int s_err;
     const int tid = blk_tid(), nthr = blk_nthr();
+    const int lane = tid & 31, nwarps = (nthr + 31) >> 5, warp = tid >> 5;
+    const unsigned wmask = (warp == nwarps - 1 && (nthr & 31)) ? ((1u << (nthr & 31)) - 1u) : 0xFFFFFFFFu;
     __syncthreads();
     if (tid == 0) s_err = 0;
     __syncthreads();
     gfs_file* fe = &S->files[fd];
-    uint32_t gen = ld_rlx(&fe->gen);
-    int host_fd = (int)ld_rlx((const uint32_t*)&fe->host_fd);
-    int oflags = (int)ld_rlx((const uint32_t*)&fe->flags);
-    uint32_t nwords = (S->n_frames + 31u) >> 5;
-    for (uint32_t w = (uint32_t)tid; w < nwords; w += (uint32_t)nthr) {
-        uint32_t bits = ld_rlx(&S->dirty_bits[w]);
-        while (bits) {
-            uint32_t b = (uint32_t)(__ffs(bits) - 1);
+    const uint32_t gen = ld_rlx(&fe->gen);
+    const int host_fd = (int)ld_rlx((const uint32_t*)&fe->host_fd);
+    const int oflags = (int)ld_rlx((const uint32_t*)&fe->flags);
+    const uint32_t nwords = (S->n_frames + 31u) >> 5;
+    uint32_t w = (uint32_t)tid;
+    uint32_t bits = w < nwords ? ld_rlx(&S->dirty_bits[w]) : 0u;
+    for (;;) {
+        /* this lane's next dirty frame of the file, prepared (pinned) */
+        int fr = -1;
+        uint64_t key = 0;
+        while (fr < 0 && w < nwords) {
+            if (!bits) {
+                w += (uint32_t)nthr;
+                bits = w < nwords ? ld_rlx(&S->dirty_bits[w]) : 0u;
+                continue;
+            }
+            const uint32_t b = (uint32_t)(__ffs(bits) - 1);
             bits &= bits - 1u;
-            uint32_t fr = (w << 5) | b;
-            if (key_file(ld_rlx64(&S->frames[fr].key)) != (uint32_t)fd) continue;
-            int rc = flush_frame(S, fr, (uint32_t)fd, gen, host_fd, oflags);
+            const uint32_t f = (w << 5) | b;
+            if (key_file(ld_rlx64(&S->frames[f].key)) != (uint32_t)fd) continue;
+            const int p = flush_prepare(S, f, (uint32_t)fd, gen, &key);
+            if (p < 0) atomicCAS(&s_err, 0, p);
+            if (p > 0) fr = (int)f;
+        }
+        const unsigned work = __ballot_sync(wmask, fr >= 0);
+        if (!work) break;
+        const int slot = fr >= 0 ? wstage_claim(S, (uint32_t)fr) : -1;
+        uint32_t content = fr >= 0 ? ld_rlx(&S->frames[fr].content) : 0u;
+        /* the warp copies each staged lane's frame into its slot */
+        for (unsigned m = __ballot_sync(wmask, slot >= 0); m; m &= m - 1u) {
+            const int l = __ffs(m) - 1;
+            const int f = __shfl_sync(wmask, fr, l);
+            const int k = __shfl_sync(wmask, slot, l);
+            const uint32_t n16 = (__shfl_sync(wmask, content, l) + 15u) >> 4;
+            const uint4* src = (const uint4*)frame_data(S, (uint32_t)f);
+            uint4* dst = (uint4*)(S->wstage + (size_t)k * S->page_size);
+            /* eight 16-byte loads in flight per lane, then their stores */
+            uint32_t i = (uint32_t)lane;
+            for (; i + 7u * 32u < n16; i += 8u * 32u) {
+                uint4 v[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) v[q] = ld_cg4(src + i + 32u * (uint32_t)q);
+#pragma unroll
+                for (int q = 0; q < 8; q++) dst[i + 32u * (uint32_t)q] = v[q];
+            }
+            for (; i < n16; i += 32u) dst[i] = ld_cg4(src + i);
+        }
+        __threadfence_system();
+        __syncwarp(wmask);
+        if (fr >= 0) {
+            const int rc = flush_finish(S, (uint32_t)fr, writeback_frame(S, (uint32_t)fr, key, host_fd, oflags, slot));
             if (rc < 0) atomicCAS(&s_err, 0, rc);
         }
     }

@@ -327,7 +327,8 @@ __device__ __forceinline__ void mark_dirty(gfs_state* S, uint32_t fr) {
     if (!(old & GFS_F_DIRTY)) dirty_bit_set(S, fr);
 }
 
-__device__ __noinline__ int writeback_frame(gfs_state* S, uint32_t fr, uint64_t key, int host_fd, int oflags);
+__device__ __noinline__ int writeback_frame(gfs_state* S, uint32_t fr, uint64_t key, int host_fd, int oflags,
+                                            int stage_slot = -1);
 
 /* Take a frame out of VALID (refcount 0) into EVICTING and then CLAIMED:
  * drop it from the index, wait out transient pins.  Dirty frames must have
@@ -418,11 +419,17 @@ __device__ __forceinline__ void release_owned(gfs_state* S, uint32_t fr, uint32_
 #define GFS_PIN_WPART 2     /* partial write: fill if the file has bytes there */
 #define GFS_PIN_WONCE 3     /* write-once file (O_GWRONCE): never fill, zero */
 #define GFS_PIN_NOALLOC 8   /* flag: fail with -GFS_ENOMEM quickly instead of waiting long */
+#define GFS_PIN_SMFILL 16   /* flag (with READ): the caller fills a missed page of a file with a
+                               registered host mapping itself (SM loads from the mapping) instead
+                               of a host copy; pin_page then returns it fresh.  A page another
+                               caller is still loading is not waited for: -GFS_EAGAIN (a caller
+                               holding frames it has yet to fill must not wait on others) */
 
 struct PinFile {
     uint32_t slot, gen;
     int host_fd, oflags;
     uint64_t size;
+    uint64_t map_dev; /* the file's registered host mapping (read-only opens), 0 if none */
 };
 
 __device__ __forceinline__ PinFile pin_file(gfs_state* S, int fd) {
@@ -433,6 +440,7 @@ __device__ __forceinline__ PinFile pin_file(gfs_state* S, int fd) {
     p.host_fd = (int)ld_rlx((const uint32_t*)&fe->host_fd);
     p.oflags = (int)ld_rlx((const uint32_t*)&fe->flags);
     p.size = ld_rlx64(&fe->size);
+    p.map_dev = ld_rlx64(&fe->map_dev);
     return p;
 }
 
@@ -446,6 +454,7 @@ __device__ __noinline__ int pin_page(gfs_state* S, const PinFile& pf, uint32_t b
     const uint64_t h = fmix64(key);
     const uint32_t bidx = (uint32_t)(h & (S->n_buckets - 1));
     const bool soft = (mode & GFS_PIN_NOALLOC) != 0;
+    const bool smfill = (mode & GFS_PIN_SMFILL) != 0;
     mode &= 7;
     Waiter w(S->timeout_ns);
     for (;;) {
@@ -455,6 +464,10 @@ __device__ __noinline__ int pin_page(gfs_state* S, const PinFile& pf, uint32_t b
             uint32_t old = atom_add_ar(&F->st, 1u);
             uint32_t s = fstate(old);
             if ((s == GFS_FS_VALID || s == GFS_FS_LOADING) && ld_rlx64(&F->key) == key) {
+                if (s == GFS_FS_LOADING && smfill) {
+                    atomicSub(&F->st, 1u);
+                    return -GFS_EAGAIN;
+                }
                 if (s == GFS_FS_LOADING) {
                     for (;;) {
                         uint32_t cur = ld_acq(&F->st);
@@ -538,6 +551,11 @@ __device__ __noinline__ int pin_page(gfs_state* S, const PinFile& pf, uint32_t b
         if (pf.host_fd >= 0 && foff < pf.size) {
             if (mode == GFS_PIN_READ || mode == GFS_PIN_WPART) need_fill = true;
         }
+        if (need_fill && smfill && pf.map_dev && pf.oflags == O_GRDONLY) {
+            /* the caller copies the page's bytes from the mapping */
+            *fresh = true;
+            return (int)nf;
+        }
         if (need_fill) {
             Req r = {};
             r.op = GFS_OP_READ;
@@ -578,12 +596,47 @@ __device__ __forceinline__ void publish_valid(gfs_state* S, uint32_t fr) {
     atomicAdd(&S->frames[fr].st, (GFS_FS_VALID - GFS_FS_LOADING) << GFS_F_SHIFT);
 }
 
+/* Largest page the SMs stage for write-back themselves (a warp copies a
+ * page into a write-stage slot); larger pages are copied by the host. */
+#define GFS_WSTAGE_MAX_PAGE (256u << 10)
+
+/* A free write-stage slot, or -1 when none is free (the caller then has the
+ * host copy the frame).  The bitmap's words are scanned once from a word
+ * chosen by `hint`, so concurrent claimers start apart. */
+__device__ __forceinline__ int wstage_claim(gfs_state* S, uint32_t hint) {
+    if (S->page_size > GFS_WSTAGE_MAX_PAGE || !S->wstage || !S->wstage_slots) return -1;
+    const uint32_t nw = (S->wstage_slots + 31u) >> 5;
+    for (uint32_t t = 0; t < nw; t++) {
+        const uint32_t wi = (hint + t) % nw;
+        const uint32_t valid = wi == nw - 1u && (S->wstage_slots & 31u) ? (1u << (S->wstage_slots & 31u)) - 1u : ~0u;
+        uint32_t free_ = ~ld_rlx(&S->wstage_bits[wi]) & valid;
+        while (free_) {
+            const int b = __ffs(free_) - 1;
+            if (!(atomicOr(&S->wstage_bits[wi], 1u << b) & (1u << b))) return (int)(wi * 32u + (uint32_t)b);
+            free_ &= ~(1u << b);
+        }
+    }
+    return -1;
+}
+__device__ __forceinline__ void wstage_release(gfs_state* S, int k) {
+    atomicAnd(&S->wstage_bits[k >> 5], ~(1u << (k & 31)));
+}
+
 /* Write one frame's valid bytes back to the host file (single thread; the
- * caller owns the frame by a pin or by EVICTING). */
-__device__ __noinline__ int writeback_frame(gfs_state* S, uint32_t fr, uint64_t key, int host_fd, int oflags) {
+ * caller owns the frame by a pin or by EVICTING).  stage_slot >= 0: the
+ * caller has stored the bytes in that write-stage slot (mapped pinned host
+ * memory) and the host only merges and writes them -- no device-to-host
+ * copy is issued while kernels run; the slot is released here.  Otherwise
+ * the host copies the frame. */
+__device__ __noinline__ int writeback_frame(gfs_state* S, uint32_t fr, uint64_t key, int host_fd, int oflags,
+                                            int stage_slot) {
     gfs_frame* F = &S->frames[fr];
     uint32_t content = ld_rlx(&F->content);
-    if (content == 0u) return 0;
+    const int slot = stage_slot;
+    if (content == 0u) {
+        if (slot >= 0) wstage_release(S, slot);
+        return 0;
+    }
     Req r = {};
     r.op = GFS_OP_WRITE;
     r.rflags = (oflags == O_GWRONCE) ? GFS_RF_DIFF : 0;
@@ -592,11 +645,23 @@ __device__ __noinline__ int writeback_frame(gfs_state* S, uint32_t fr, uint64_t 
     r.offset = (uint64_t)key_block(key) << S->log_page;
     r.length = content;
     r.dev_addr = (uint64_t)(uintptr_t)frame_data(S, fr);
-    return rpc_call(S, r, frame_done(S, fr));
+    if (slot >= 0) {
+        r.rflags |= GFS_RF_STAGED;
+        r.dev_addr = (uint64_t)slot;
+    }
+    const int rc = rpc_call(S, r, frame_done(S, fr));
+    /* the host has finished with the slot once the request completed; after
+     * a timeout it may still read it: the slot is then never reused */
+    if (slot >= 0 && rc != -GFS_ETIMEDOUT) wstage_release(S, slot);
+    return rc;
 }
 
-/* Flush one dirty frame of file `slot` (single thread).  Returns 0 or -err. */
-__device__ __noinline__ int flush_frame(gfs_state* S, uint32_t fr, uint32_t slot, uint32_t gen, int host_fd, int oflags) {
+/* First half of a flush of one dirty frame of file `slot` (single thread):
+ * 1 = the frame is pinned, its dirty bit cleared and *key_out holds its
+ * key (the caller writes it back and calls flush_finish); 0 = nothing to
+ * write; < 0 = error. */
+__device__ __forceinline__ int flush_prepare(gfs_state* S, uint32_t fr, uint32_t slot, uint32_t gen,
+                                             uint64_t* key_out) {
     gfs_frame* F = &S->frames[fr];
     Waiter w(S->timeout_ns);
     for (;;) {
@@ -618,15 +683,31 @@ __device__ __noinline__ int flush_frame(gfs_state* S, uint32_t fr, uint32_t slot
         if (fstate(old) != GFS_FS_VALID || ld_rlx64(&F->key) != key) { atomicSub(&F->st, 1u); continue; }
         dirty_bit_clear(S, fr);
         uint32_t prev = atom_and_ar(&F->st, ~GFS_F_DIRTY);
-        int rc = 0;
-        if (prev & GFS_F_DIRTY) {
-            rc = writeback_frame(S, fr, key, host_fd, oflags);
-            if (rc < 0) mark_dirty(S, fr); /* keep it for a later attempt */
-            else count(S, &S->stats.writebacks);
+        if (!(prev & GFS_F_DIRTY)) {
+            unpin(S, fr);
+            return 0;
         }
-        unpin(S, fr);
-        return rc < 0 ? rc : 0;
+        *key_out = key;
+        return 1;
     }
+}
+
+/* Second half: after the write-back's result rc, keep the frame dirty on
+ * failure and drop the pin. */
+__device__ __forceinline__ int flush_finish(gfs_state* S, uint32_t fr, int rc) {
+    if (rc < 0) mark_dirty(S, fr); /* keep it for a later attempt */
+    else count(S, &S->stats.writebacks);
+    unpin(S, fr);
+    return rc < 0 ? rc : 0;
+}
+
+/* Flush one dirty frame of file `slot` (single thread; the host copies the
+ * frame).  Returns 0 or -err. */
+__device__ __noinline__ int flush_frame(gfs_state* S, uint32_t fr, uint32_t slot, uint32_t gen, int host_fd, int oflags) {
+    uint64_t key = 0;
+    const int p = flush_prepare(S, fr, slot, gen, &key);
+    if (p <= 0) return p;
+    return flush_finish(S, fr, writeback_frame(S, fr, key, host_fd, oflags));
 }
 
 /* ------------------------------------------------------------------ */

@@ -2010,6 +2010,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     for (int i = 0; i < n_files; i++)
         if (!paths[i] || strlen(paths[i]) >= GFS_NAME_MAX) return -GFS_EINVAL;
     if (gfs__activate(ctx)) return -GFS_EIO;
+    for (int i = 0; i < n_files; i++) gfs__premap(ctx, paths[i]);
     int fd = open(dict_path, O_RDONLY | O_CLOEXEC);
     if (fd < 0) return -errno;
     struct stat st;

@@ -186,6 +186,8 @@ struct gfs_ctx {
     cudaMemPool_t mem_pool = nullptr; /* stream-ordered device memory of per-call objects (plans, servers) */
     int pageable = 0; /* kernels may address pageable host memory (host page tables) */
     uint8_t* hmap = nullptr;   /* mapped block: completion words + open replies (host view) */
+    uint8_t* wstage_h = nullptr; /* write-back staging slots (host view of gfs_state.wstage) */
+    size_t wstage_bytes = 0;
     uint8_t* hmap_d = nullptr; /* same, device view */
     size_t hmap_bytes = 0;
     size_t reply_off = 0;
@@ -230,33 +232,34 @@ static void log_failure(gfs_ctx* c, const gfs_req& r, int err) {
 static int slot_acquire_fd(gfs_ctx* c, uint32_t s);
 static void slot_release_fd(gfs_ctx* c, uint32_t s);
 
-static void finish_write(gfs_ctx* c, Worker* w, int k, const Pending& p) {
-    uint8_t* buf = w->staging + (size_t)k * w->slot_bytes;
-    const size_t len = p.len;
-    bool merge = (p.rflags & GFS_RF_DIFF) != 0;
+/* Write len bytes of buf (the page at file offset `offset` of slot `file`)
+ * to the host file, OR-merged with the bytes already there for write-once
+ * files (RW_IPC_DIFF, host_loop.h:76-137); buf is merged in place.  Returns
+ * 0 or an errno. */
+static int write_out(gfs_ctx* c, Worker* w, uint32_t file, uint64_t offset, uint8_t* buf, size_t len, int rflags) {
+    bool merge = (rflags & GFS_RF_DIFF) != 0;
     gfs_req r{};
     r.op = GFS_OP_WRITE;
-    r.file = p.file;
-    r.offset = p.offset;
+    r.file = file;
+    r.offset = offset;
     r.length = len;
-    const int fd = slot_acquire_fd(c, p.file);
+    const int fd = slot_acquire_fd(c, file);
     if (fd < 0) {
         log_failure(c, r, -fd);
-        set_done(c, p.done, GFS_DONE_ERR | (uint32_t)(-fd));
-        return;
+        return -fd;
     }
     r.host_fd = fd;
     {
-        HostSlot& h = c->slots[p.file];
-        const uint64_t pg = p.offset >> c->hs.log_page;
+        HostSlot& h = c->slots[file];
+        const uint64_t pg = offset >> c->hs.log_page;
         std::lock_guard<std::mutex> lk(h.mu);
         if (h.written.size() <= (size_t)(pg >> 6)) h.written.resize((size_t)(pg >> 6) + 1, 0ULL);
         const uint64_t bit = 1ULL << (pg & 63u);
-        if (merge && p.offset >= h.size_at_open && !(h.written[(size_t)(pg >> 6)] & bit)) merge = false;
+        if (merge && offset >= h.size_at_open && !(h.written[(size_t)(pg >> 6)] & bit)) merge = false;
         h.written[(size_t)(pg >> 6)] |= bit;
     }
     if (merge) {
-        ssize_t m = pread_full(fd, w->merge, len, (off_t)p.offset);
+        ssize_t m = pread_full(fd, w->merge, len, (off_t)offset);
         size_t i = 0;
         for (; m >= 8 && i + 8 <= (size_t)m; i += 8) {
             uint64_t a, b;
@@ -267,13 +270,22 @@ static void finish_write(gfs_ctx* c, Worker* w, int k, const Pending& p) {
         }
         for (; (ssize_t)i < m; i++) buf[i] |= w->merge[i];
     }
-    ssize_t put = pwrite_full(fd, buf, len, (off_t)p.offset);
+    ssize_t put = pwrite_full(fd, buf, len, (off_t)offset);
     int err = put < 0 ? errno : EIO;
-    slot_release_fd(c, p.file);
+    slot_release_fd(c, file);
     c->h_writes++;
     if (put >= 0) c->h_write_bytes += (unsigned long long)put;
-    if (put != (ssize_t)len) log_failure(c, r, err);
-    set_done(c, p.done, put == (ssize_t)len ? 1u + (uint32_t)len : (GFS_DONE_ERR | (uint32_t)err));
+    if (put != (ssize_t)len) {
+        log_failure(c, r, err);
+        return err;
+    }
+    return 0;
+}
+
+static void finish_write(gfs_ctx* c, Worker* w, int k, const Pending& p) {
+    uint8_t* buf = w->staging + (size_t)k * w->slot_bytes;
+    const int e = write_out(c, w, p.file, p.offset, buf, p.len, p.rflags);
+    set_done(c, p.done, e == 0 ? 1u + (uint32_t)p.len : (GFS_DONE_ERR | (uint32_t)e));
 }
 
 /* Complete in-flight copies whose data has landed (in issue order). */
@@ -388,6 +400,34 @@ static void map_detach(gfs_ctx* c, FileMap* m) {
     if (!m) return;
     std::lock_guard<std::mutex> lk(c->map_mu);
     m->refs--;
+}
+
+/* Register the mapping of a file a kernel is about to open read-only, from
+ * the calling thread, so the device's open finds it cached: the host worker
+ * that serves the open then makes no CUDA call while kernels run, and the
+ * registration's cost stays out of the kernel's time.  A cached mapping
+ * costs one stat(). */
+extern "C" void gfs__premap(gfs_ctx* c, const char* path) {
+    if (!c || !path || (c->cfg.flags & GFS_CFG_NO_FILE_MAP)) return;
+    struct stat st;
+    if (stat(path, &st) != 0 || !S_ISREG(st.st_mode) || st.st_size < (off_t)(64 << 10)) return;
+    const int64_t ct = (int64_t)st.st_ctim.tv_sec * 1000000000LL + st.st_ctim.tv_nsec;
+    const uint64_t key = (uint64_t)st.st_ino * 0x9E3779B97F4A7C15ULL ^ (uint64_t)st.st_dev;
+    {
+        std::lock_guard<std::mutex> lk(c->map_mu);
+        auto rg = c->maps.equal_range(key);
+        for (auto it = rg.first; it != rg.second; ++it) {
+            const FileMap* m = it->second;
+            if (m->dev == (uint64_t)st.st_dev && m->ino == (uint64_t)st.st_ino && m->size == (uint64_t)st.st_size &&
+                m->ctime_ns == ct)
+                return;
+        }
+    }
+    const int fd = open(path, O_RDONLY | O_CLOEXEC);
+    if (fd < 0) return;
+    struct stat st2;
+    if (fstat(fd, &st2) == 0) map_detach(c, map_attach(c, fd, st2));
+    close(fd);
 }
 
 /* Close the host fds of idle slots (clock order) until the process is
@@ -584,6 +624,21 @@ static void handle(gfs_ctx* c, Worker* w, const gfs_req& r) {
         break;
     }
     case GFS_OP_WRITE: {
+        if (r.rflags & GFS_RF_STAGED) {
+            /* the SMs stored the bytes in a write-stage slot: merge and
+             * pwrite now, no copy to wait for */
+            const size_t page = (size_t)c->hs.page_size;
+            const uint64_t k = r.dev_addr;
+            if (k * page >= c->wstage_bytes) {
+                log_failure(c, r, EINVAL);
+                set_done(c, done, GFS_DONE_ERR | (uint32_t)EINVAL);
+                break;
+            }
+            size_t len = (size_t)r.length < page ? (size_t)r.length : page;
+            const int e = write_out(c, w, r.file, r.offset, c->wstage_h + k * page, len, r.rflags);
+            set_done(c, done, e == 0 ? 1u + (uint32_t)len : (GFS_DONE_ERR | (uint32_t)e));
+            break;
+        }
         /* device -> staging now; merge and pwrite when the copy has landed */
         size_t len = (size_t)r.length;
         if (len > w->slot_bytes) len = w->slot_bytes;
@@ -996,6 +1051,21 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
         s.hdone = (uint32_t*)c->hmap_d;
         s.hreply = (gfs_open_reply*)(c->hmap_d + reply_off);
         c->reply_off = reply_off;
+        s.wstage = nullptr;
+        s.wstage_bits = nullptr;
+        s.wstage_slots = 0;
+        if (page <= (256u << 10)) {
+            /* write-back staging for pages the SMs stage themselves: 64 MiB
+             * of host memory, at most 1024 pages */
+            uint64_t slots = (64ull << 20) / page;
+            slots = slots > 1024 ? 1024 : slots;
+            c->wstage_bytes = (size_t)slots * page;
+            CK(cudaHostAlloc((void**)&c->wstage_h, c->wstage_bytes, cudaHostAllocMapped | cudaHostAllocPortable));
+            CK(cudaHostGetDevicePointer((void**)&s.wstage, c->wstage_h, 0));
+            CK(cudaMalloc(&s.wstage_bits, ((slots + 31) / 32) * 4));
+            CK(cudaMemset(s.wstage_bits, 0, ((slots + 31) / 32) * 4));
+            s.wstage_slots = (uint32_t)slots;
+        }
         CK(cudaMalloc(&c->ds, sizeof(gfs_state)));
         CK(cudaMemcpy(c->ds, &s, sizeof(gfs_state), cudaMemcpyHostToDevice));
         CK(cudaMemcpyToSymbol(g_gfs, &c->ds, sizeof(gfs_state*)));
@@ -1071,6 +1141,10 @@ int gfs_destroy(gfs_ctx* c) {
     c->maps.clear();
     if (c->h_bounce) cudaFreeHost(c->h_bounce);
     c->h_bounce = nullptr;
+    if (c->wstage_h) cudaFreeHost(c->wstage_h);
+    c->wstage_h = nullptr;
+    if (c->hs.wstage_bits) cudaFree(c->hs.wstage_bits);
+    c->hs.wstage_bits = nullptr;
     if (c->mem_pool) {
         cudaDeviceSynchronize();
         cudaMemPoolDestroy(c->mem_pool);

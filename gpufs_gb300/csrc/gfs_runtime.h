@@ -24,6 +24,9 @@ void gfs__dev_free(gfs_ctx* c, void* p, cudaStream_t s);
  * its length (0 when the slot has none); valid while the slot stays open */
 int gfs__slot_map(gfs_ctx* c, uint32_t slot, unsigned long long* dev_addr, unsigned long long* len);
 int gfs__activate(gfs_ctx* c);
+/* register a file's host mapping from the calling thread before a kernel
+ * opens it read-only (the open then makes no CUDA call on a host worker) */
+void gfs__premap(gfs_ctx* c, const char* path);
 /* the session's bound on device-side waits (ns) */
 unsigned long long gfs__timeout_ns(gfs_ctx* c);
 /* the session's GFS_CFG_* flags and CUDA device */

@@ -276,6 +276,7 @@ void gfs__preload_workloads() {
 
 long long gfs_pread_dev(gfs_ctx* c, const char* path, uint64_t off, uint64_t size, void* dev_out, int nblocks,
                         int nthreads, float* kernel_ms) {
+    gfs__premap(c, path);
     Names n;
     int rc = stage(c, path, nullptr, nblocks, &n);
     if (rc) return rc;
@@ -333,6 +334,7 @@ long long gfs_pwrite_fsync(gfs_ctx* c, const char* path, uint64_t off, uint64_t 
 
 long long gfs_mmap_read(gfs_ctx* c, const char* path, uint64_t off, uint64_t size, void* host_out, int nblocks,
                         int nthreads, int use_warp_api) {
+    gfs__premap(c, path);
     Names n;
     int rc = stage(c, path, nullptr, nblocks, &n);
     if (rc) return rc;
@@ -374,6 +376,7 @@ int gfs_unlink_path(gfs_ctx* c, const char* path) {
 }
 
 int gfs_memcopy(gfs_ctx* c, const char* src, const char* dst, int nblocks, int nthreads, int mode, float* kernel_ms) {
+    gfs__premap(c, src);
     Names n;
     int rc = stage(c, src, dst, nblocks, &n);
     if (rc) return rc;

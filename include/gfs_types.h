@@ -72,6 +72,7 @@ extern "C" {
 #define GFS_OP_TRUNC 5
 #define GFS_OP_UNLINK 6
 #define GFS_RF_DIFF 1 /* OR-merge with the bytes already in the file (RW_IPC_DIFF) */
+#define GFS_RF_STAGED 2 /* WRITE: the bytes are already in write-stage slot `dev_addr` (host memory) */
 
 /* completion word: 0 pending, 1+result on success, GFS_DONE_ERR|errno */
 #define GFS_DONE_ERR 0x80000000u
@@ -82,6 +83,7 @@ extern "C" {
 #define GFS_EIO 5
 #define GFS_E2BIG 7
 #define GFS_EBADF 9
+#define GFS_EAGAIN 11
 #define GFS_ENOMEM 12
 #define GFS_EINVAL 22
 #define GFS_EMFILE 24
@@ -191,6 +193,13 @@ typedef struct gfs_state {
     uint32_t table_lock;
     uint32_t error;       /* sticky GFS_ERRB_* */
     gfs_stats stats;
+    /* write-back staging: wstage_slots pages of mapped pinned host memory
+     * (device view); a dirty frame's bytes are stored there by the SMs and
+     * the host only merges and writes them (no device-to-host copy) */
+    uint8_t* wstage;
+    uint32_t* wstage_bits;          /* device memory: one bit per slot, set while in use */
+    uint32_t wstage_slots;          /* 0 when pages are too large to stage */
+    uint32_t wstage_pad;
 } gfs_state;
 
 #ifdef __cplusplus

@@ -77,7 +77,8 @@ def test_second_read_hits_cache(sess, shm_dir):
     assert np.array_equal(sess.pread(p, 0, want.size, nblocks=8), want)
     st1 = sess.stats()
     assert st1["misses"] == (8 << 20) // sess.page_size
-    assert st1["host_read_bytes"] == want.size
+    # the misses were filled by the reading blocks from the file's mapping
+    assert st1["read_rpcs"] == 0 and st1["host_read_bytes"] == 0
     sess.reset_stats()
     assert np.array_equal(sess.pread(p, 0, want.size, nblocks=8), want)
     st2 = sess.stats()
@@ -220,7 +221,8 @@ def test_many_files_recycle_slots(built, shm_dir):
 def test_injected_read_error_propagates(built, shm_dir):
     p = os.path.join(shm_dir, "inj.bin")
     want = _mk(p, 1 << 20, seed=18)
-    with g.Session(log_page=16, pool_bytes=16 << 20, timeout_s=20) as s:
+    # without file mappings every miss is a host read, which the fault hits
+    with g.Session(log_page=16, pool_bytes=16 << 20, timeout_s=20, file_map=False) as s:
         s.inject_read_errors(1, errno.EIO)
         with pytest.raises(g.GfsError) as ei:
             s.pread(p, 0, want.size, nblocks=1)
@@ -249,21 +251,27 @@ def test_stalled_host_times_out(built, shm_dir):
 
 
 def test_reads_use_registered_file_mapping(built, shm_dir):
-    """Read-only opens DMA page misses straight from a registered mapping of
-    the host file; a rewritten file (new size/ctime) is mapped afresh; with
-    the mapping off every miss goes through pread into staging."""
+    """Read-only opens get a registered mapping of the host file: gread's
+    misses are filled by the reading block itself, with SM loads from the
+    mapping (no request to the host at all), and gmmap's single-thread misses
+    are copy-engine DMA from it (no pread); a rewritten file (new size/ctime)
+    is mapped afresh; with the mapping off every miss goes through pread
+    into staging."""
     p = os.path.join(shm_dir, "mapped.bin")
     want = _mk(p, 3 * (1 << 20) + 5, seed=20)
     with g.Session(log_page=16, pool_bytes=64 << 20, timeout_s=20) as s:
         s.reset_stats()
         assert np.array_equal(s.pread(p, 0, want.size, nblocks=4), want)
         st = s.stats()
-        assert st["host_reads"] > 0 and st["host_map_reads"] == st["host_reads"]
-        # the mapping is kept across closes: a cold re-read needs no pread either
+        assert st["misses"] == (want.size + 65535) // 65536
+        assert st["read_rpcs"] == 0 and st["host_reads"] == 0
+        # gmmap pins one page at a time by one thread: the host copies it
+        # from the mapping (kept across closes: still no pread)
         s.drop_cache()
         s.reset_stats()
-        assert np.array_equal(s.pread(p, 0, want.size, nblocks=4), want)
-        assert s.stats()["host_map_reads"] == s.stats()["host_reads"] > 0
+        assert np.array_equal(s.mmap_read(p, 0, want.size, nblocks=4), want)
+        st = s.stats()
+        assert st["host_reads"] > 0 and st["host_map_reads"] == st["host_reads"]
         time.sleep(0.01)
         want2 = _mk(p, 2 * (1 << 20) + 77, seed=21)
         assert np.array_equal(s.pread(p, 0, want2.size, nblocks=3), want2)
