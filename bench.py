@@ -873,7 +873,7 @@ def _served_data(d, target_bytes, max_files):
 
 def _served_trace(sizes, n_req, n_out, rng):
     """Requests: file popularity Zipf(0.9) over a seeded permutation, lengths
-    log-uniform 4 KiB .. 16 MiB, offsets 4 KiB-aligned within the file, op mix
+    log-uniform 4 KiB .. 16 MiB, offsets uniform over the file's bytes, op mix
     80 % read+XXH64 / 15 % grep / 5 % write (writes to disjoint 16 MiB regions
     of the output files)."""
     import numpy as np
@@ -896,8 +896,7 @@ def _served_trace(sizes, n_req, n_out, rng):
             wcount += 1
         else:
             f = int(files[k])
-            pages = int(sz[f]) // 4096
-            off = int(rng.integers(0, pages + 1)) * 4096 if pages else 0
+            off = int(rng.integers(0, int(sz[f]) + 1))
             reqs[k] = (ops[k], f, off, lengths[k], 0)
     return reqs
 

@@ -1203,56 +1203,60 @@ __device__ int pp_cover(gfs_state* S, const PinFile& pf, PagePair& p, uint32_t a
     return 0;
 }
 
-/* read + XXH64 of [off, end) of a served file, by one warp.  Pages are
- * pinned up to 8 at a time, one lane each, so the misses of a large request
- * are in flight together; a pool short of frames falls back to one page at
- * a time (multi-page pins do not wait for frames). */
+/* read + XXH64 of [off, end) of a served file, by one warp, at any offset.
+ * The range is hashed in logical 512-byte chunks from `off` (so every full
+ * chunk is 16 whole stripes): a chunk's bytes are loaded as the 16-byte
+ * aligned units of the file that cover it (each inside one page; lane 0
+ * keeps the chunk's one or two pages pinned) into `raw`, then shifted into
+ * `st` by the chunk's offset within its first unit (funnel shifts of 32-bit
+ * words), where lanes 0..3 run the four accumulator lanes over them. */
 __device__ int sv_read_xxh(gfs_state* S, const ServeDev& D, int fd, uint64_t off, uint64_t end, uint8_t* st,
-                           unsigned long long* result) {
+                           uint8_t* raw, unsigned long long* result) {
     const int lane = threadIdx.x & 31;
     const uint32_t lp = S->log_page, pmask = S->page_size - 1u;
-    const PinFile pf = pin_file(S, fd);
+    PinFile pf;
+    PagePair pp;
+    if (lane == 0) { pf = pin_file(S, fd); pp_init(pp); }
     uint64_t v = gfsx::acc_init(lane & 3);
     int err = 0;
-    uint32_t batch = 8;
     const uint8_t* tail = st;
-    for (uint64_t pos = off; pos < end && !err;) {
-        const uint32_t first = (uint32_t)(pos >> lp), last = (uint32_t)((end - 1) >> lp);
-        const uint32_t nb = last - first + 1u < batch ? last - first + 1u : batch;
-        int fr = -1;
-        if ((uint32_t)lane < nb) {
-            bool fresh;
-            fr = pin_page(S, pf, first + (uint32_t)lane, GFS_PIN_READ | (nb > 1 ? GFS_PIN_NOALLOC : 0), &fresh);
-            if (fr >= 0 && fresh) publish_valid(S, (uint32_t)fr);
+    for (uint64_t pos = off; pos < end;) {
+        const uint32_t clen = end - pos < 512u ? (uint32_t)(end - pos) : 512u;
+        const uint64_t a0 = pos & ~15ull, cend = pos + clen;
+        int r = 0;
+        if (lane == 0) r = pp_cover(S, pf, pp, (uint32_t)(a0 >> lp), (uint32_t)((cend - 1) >> lp));
+        r = __shfl_sync(0xFFFFFFFFu, r, 0);
+        if (r < 0) { err = r; break; }
+        uint32_t pg0 = 0;
+        int f0 = 0, f1 = 0;
+        if (lane == 0) { pg0 = pp.pg[0]; f0 = pp.fr[0]; f1 = pp.fr[1]; }
+        pg0 = __shfl_sync(0xFFFFFFFFu, pg0, 0);
+        f0 = __shfl_sync(0xFFFFFFFFu, f0, 0);
+        f1 = __shfl_sync(0xFFFFFFFFu, f1, 0);
+        /* the aligned units covering [pos, cend): at most 33 */
+        for (uint32_t u = (uint32_t)lane; a0 + 16ull * u < cend; u += 32u) {
+            const uint64_t q = a0 + 16ull * u;
+            const int fr = (uint32_t)(q >> lp) == pg0 ? f0 : f1;
+            *(uint4*)(raw + 16u * u) = ld_cg4(S->pool + ((size_t)fr << lp) + (q & pmask));
         }
-        const unsigned nomem = __ballot_sync(0xFFFFFFFFu, (uint32_t)lane < nb && fr == -GFS_ENOMEM);
-        const unsigned bad = __ballot_sync(0xFFFFFFFFu, (uint32_t)lane < nb && fr < 0 && fr != -GFS_ENOMEM);
-        if (bad || nomem) {
-            if ((uint32_t)lane < nb && fr >= 0) unpin(S, (uint32_t)fr);
-            if (bad) err = __shfl_sync(0xFFFFFFFFu, fr, __ffs(bad) - 1);
-            else batch = 1; /* take the pages one at a time, waiting for frames */
-            continue;
+        __syncwarp();
+        /* shift by pos & 15 into st (16 bytes a lane, 512 at most) */
+        const uint32_t sh = (uint32_t)(pos & 15u);
+        if (16u * (uint32_t)lane < clen) {
+            const uint32_t* w = (const uint32_t*)(raw + (sh & ~3u) + 16u * (uint32_t)lane);
+            const uint32_t b = 8u * (sh & 3u);
+            const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], x3 = w[3], x4 = w[4];
+            *(uint4*)(st + 16u * (uint32_t)lane) = make_uint4(__funnelshift_r(x0, x1, b), __funnelshift_r(x1, x2, b),
+                                                              __funnelshift_r(x2, x3, b), __funnelshift_r(x3, x4, b));
         }
-        for (uint32_t j = 0; j < nb; j++) {
-            const int f = __shfl_sync(0xFFFFFFFFu, fr, (int)j);
-            const uint64_t pend = (((uint64_t)(first + j) + 1u) << lp) < end ? (((uint64_t)(first + j) + 1u) << lp) : end;
-            while (pos < pend) {
-                const uint32_t piece = pend - pos < 512 ? (uint32_t)(pend - pos) : 512u;
-                const uint8_t* src = S->pool + ((size_t)f << lp) + (pos & pmask); /* 16-byte aligned */
-                const uint32_t o = (uint32_t)lane * 16u;
-                if (o + 16u <= piece) *(uint4*)(st + o) = ld_cg4(src + o);
-                else if (o < piece)
-                    for (uint32_t b = o; b < piece; b++) st[b] = src[b];
-                __syncwarp();
-                const uint32_t stripes = piece / 32u;
-                if (lane < 4) v = gfsx::acc_stripes(v, st, stripes, lane);
-                tail = st + stripes * 32u;
-                pos += piece;
-                if (pos < end) __syncwarp();
-            }
-        }
-        if ((uint32_t)lane < nb) unpin(S, (uint32_t)fr);
+        __syncwarp();
+        const uint32_t stripes = clen / 32u;
+        if (lane < 4) v = gfsx::acc_stripes(v, st, stripes, lane);
+        tail = st + stripes * 32u;
+        pos = cend;
+        if (pos < end) __syncwarp();
     }
+    if (lane == 0) pp_release(S, pp);
     if (err) return err;
     const uint64_t v1 = __shfl_sync(0xFFFFFFFFu, v, 0), v2 = __shfl_sync(0xFFFFFFFFu, v, 1),
                    v3 = __shfl_sync(0xFFFFFFFFu, v, 2), v4 = __shfl_sync(0xFFFFFFFFu, v, 3);
@@ -1276,7 +1280,10 @@ __device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, ui
     t.cnt = nullptr;
     TotalSink sink;
     int err = 0;
-    for (uint64_t seg = off; seg < end; seg += GR_SEG) {
+    /* segments start 16-byte aligned in the file (the staged units are then
+     * aligned); bytes before off or from end on are staged as zeros, which
+     * are not letters, so the range reads as a text of its own */
+    for (uint64_t seg = off & ~15ull; seg < end; seg += GR_SEG) {
         /* stage [seg - 16, seg + 512 + 64) with bytes outside [off, end) zero */
         const uint64_t lo = seg >= off + GR_LB ? seg - GR_LB : off;
         const uint64_t hi = seg + GR_SEG + GR_LA < end ? seg + GR_SEG + GR_LA : end;
@@ -1294,16 +1301,20 @@ __device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, ui
         for (uint32_t u = (uint32_t)lane; u < (GR_LB + GR_SEG + GR_LA) / 16u; u += 32u) {
             const int64_t a = (int64_t)seg - GR_LB + 16 * (int64_t)u; /* file offset of this 16-byte unit */
             uint4 w = make_uint4(0, 0, 0, 0);
-            if (a >= (int64_t)off && (uint64_t)a < end) {
+            if (a + 16 > (int64_t)off && (uint64_t)a < end) {
                 const uint32_t pg = (uint32_t)((uint64_t)a >> lp);
                 const int fr = pg == pg0 ? f0 : f1;
                 w = ld_cg4(S->pool + ((size_t)fr << lp) + ((uint64_t)a & pmask));
                 const uint64_t rem = end - (uint64_t)a;
-                if (rem < 16) { /* zero the bytes past the end */
+                const int64_t skip = (int64_t)off - a; /* bytes before off in this unit */
+                if (rem < 16 || skip > 0) { /* zero the bytes outside [off, end) */
                     uint32_t* ww = (uint32_t*)&w;
                     for (int q = 0; q < 4; q++) {
-                        const int keep = (int)rem - 4 * q;
-                        ww[q] &= keep >= 4 ? 0xFFFFFFFFu : (keep <= 0 ? 0u : (1u << (8 * keep)) - 1u);
+                        const int keep = (int)(rem < 16 ? rem : 16) - 4 * q;
+                        uint32_t m = keep >= 4 ? 0xFFFFFFFFu : (keep <= 0 ? 0u : (1u << (8 * keep)) - 1u);
+                        const int drop = (int)skip - 4 * q;
+                        m &= drop >= 4 ? 0u : (drop <= 0 ? 0xFFFFFFFFu : ~((1u << (8 * drop)) - 1u));
+                        ww[q] &= m;
                     }
                 }
             }
@@ -1383,6 +1394,7 @@ __device__ int sv_write(gfs_state* S, int fd, uint64_t off, uint64_t len, uint32
  * its ring slot, serves it and publishes the completion. */
 __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev D) {
     __shared__ __align__(16) uint8_t stage[SV_WARPS][SV_STAGE];
+    __shared__ __align__(16) uint8_t rawb[SV_WARPS][33 * 16 + 16]; /* read requests' aligned units */
     __shared__ __align__(16) uint8_t wscr[SV_WARPS][GR_WSCR];
     __shared__ uint4 kmask[17];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1428,14 +1440,14 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev 
         const uint64_t len = ((uint64_t)__shfl_sync(0xFFFFFFFFu, b.w, 0) << 32) | __shfl_sync(0xFFFFFFFFu, b.z, 0);
         unsigned long long res = 0;
         int status = 0;
-        if (off & 15u) {
-            status = -GFS_EINVAL; /* offsets are 16-byte aligned (vector loads and stores) */
+        if (op == GFS_SV_WRITE && (off & 15u)) {
+            status = -GFS_EINVAL; /* written ranges start 16-byte aligned (vector stores) */
         } else if (op == GFS_SV_WRITE) {
             status = (int)file < D.n_out ? sv_write(S, D.out_fds[file], off, len, id, &res) : -GFS_EINVAL;
         } else if ((int)file < D.n_files && (op == GFS_SV_READ || op == GFS_SV_GREP)) {
             const uint64_t size = D.sizes[file];
             const uint64_t o = off < size ? off : size, e = len < size - o ? o + len : size;
-            if (op == GFS_SV_READ) status = sv_read_xxh(S, D, D.fds[file], o, e, stage[warp], &res);
+            if (op == GFS_SV_READ) status = sv_read_xxh(S, D, D.fds[file], o, e, stage[warp], rawb[warp], &res);
             else status = sv_grep(S, D, D.fds[file], o, e, stage[warp], wscr[warp], kmask, &res);
         } else {
             status = -GFS_EINVAL;

@@ -103,14 +103,23 @@ def test_served_requests_match_oracle(built, shm_dir, spread_ms, pool_mb):
         assert np.array_equal(got, want), k
 
 
-def test_served_unaligned_offset_is_einval(built, shm_dir):
+def test_served_any_offset(built, shm_dir):
+    """Read and grep requests start at any byte (as gread does); pieces cross
+    page boundaries at every alignment; writes must start 16-byte aligned."""
     paths, dpath, outs, rng = _setup(shm_dir, seed=50)
-    reqs = np.zeros(2, dtype=g.SERVE_REQ)
-    reqs[0] = (g.SV_READ, 5, 7, 100, 0)
-    reqs[1] = (g.SV_READ, 5, 4096, 100, 0)
+    raw_dict, first_idx = _dict_words(dpath)
+    sizes = [os.path.getsize(p) for p in paths]
+    reqs = np.zeros(64, dtype=g.SERVE_REQ)
+    for k in range(63):
+        f = 5 + k % 3
+        op = g.SV_READ if k % 2 == 0 else g.SV_GREP
+        off = int(rng.integers(0, sizes[f]))
+        if k < 16:  # just before a 64 KiB page boundary, every alignment
+            off = 65536 * (1 + k % 4) - 1 - k
+        reqs[k] = (op, f, off, int(rng.integers(1, 300000)), 0)
+    reqs[63] = (g.SV_WRITE, 0, 7, 100, 0)
     with g.Session(log_page=16, pool_bytes=32 << 20, max_files=64, timeout_s=30) as s:
         with g.Server(s, dpath, paths, outs) as sv:
             res = sv.run(reqs)
-    assert res[0]["status"] == -errno.EINVAL
-    assert res[1]["status"] == 0
-    assert res[1]["result"] == oracle.xxh64(np.fromfile(paths[5], dtype=np.uint8)[4096:4196])
+    assert res[63]["status"] == -errno.EINVAL
+    _check(res[:63], reqs[:63], paths, raw_dict, first_idx)
