@@ -727,7 +727,7 @@ def _run_batched(args, rank, ws, local, td, d, nt, workers, hbm, how, link, extr
     # staging pages): every candidate measured once on this GPU ...
     keys = ("log_page", "workers", "ring", "staging")
     cands = [{"log_page": lp, "workers": w, "ring": r, "staging": sd}
-             for lp in (16, 18, 20, 21) for w in (16, 24) for r in (4096, 16384) for sd in (4, 16)]
+             for lp in (20, 21) for w in (16, 24) for r in (8192, 16384) for sd in (8, 16)]
     best, tried = autotune.tune(cands, trial)
     extra["autotune"] = [{"cfg": c, "ms": (t * 1e3 if t is not None else None)} for c, t in tried]
     # ... then the random and the model-guided search replayed on those
@@ -739,7 +739,7 @@ def _run_batched(args, rank, ws, local, td, d, nt, workers, hbm, how, link, extr
     replay = lambda cfg: measured.get(json.dumps(cfg, sort_keys=True))  # noqa: E731
     wf = costmodel.workload_features(sizes, (0.0, 1.0, 0.0))
     feat = lambda cfg: np.concatenate([wf, costmodel.param_features(cfg, keys)])  # noqa: E731
-    budget, seeds = 8, 8
+    budget, seeds = 6, 8
     reg = {"random": [], "guided": []}
     for sd in range(seeds):
         rb, _ = autotune.tune_random(cands, replay, budget, seed=sd)
