@@ -253,7 +253,15 @@ __device__ __noinline__ int rpc_call(gfs_state* S, const Req& r, uint32_t* done)
     st_rlx_sys(done, 0u);
     __threadfence_system();
     Waiter w(S->timeout_ns);
-    uint32_t t = atomicAdd(&S->ring_tail, 1u);
+    /* the lanes of a warp that call together (a lane-per-page miss burst)
+     * take consecutive ring tickets with one atomic by their leader */
+    const unsigned act = __activemask();
+    uint32_t lane_id;
+    asm("mov.u32 %0, %%laneid;" : "=r"(lane_id));
+    const int lane = (int)lane_id, leader = __ffs(act) - 1;
+    uint32_t t = 0;
+    if (lane == leader) t = atomicAdd(&S->ring_tail, (uint32_t)__popc(act));
+    t = __shfl_sync(act, t, leader) + (uint32_t)__popc(act & ((1u << lane) - 1u));
     gfs_req* slot = S->ring + (t & (S->ring_slots - 1));
     while (ld_acq_sys(&slot->seq) != t) {
         if (!w.tick(2048)) {

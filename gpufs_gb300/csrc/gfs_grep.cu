@@ -1163,86 +1163,91 @@ __device__ __forceinline__ uint32_t sv_pattern(uint64_t x, uint32_t id) {
     return (uint32_t)(((uint32_t)x * 0x9E3779B1u + id * 0x85EBCA77u) >> 24);
 }
 
-/* lane 0 keeps up to two pinned pages of one file (pg0 < pg1) */
-struct PagePair {
-    uint32_t pg[2];
-    int fr[2];
-};
-__device__ __forceinline__ void pp_init(PagePair& p) { p.pg[0] = p.pg[1] = 0xFFFFFFFFu; p.fr[0] = p.fr[1] = -1; }
-__device__ __forceinline__ void pp_release(gfs_state* S, PagePair& p) {
-    for (int i = 0; i < 2; i++)
-        if (p.fr[i] >= 0) unpin(S, (uint32_t)p.fr[i]);
-    pp_init(p);
-}
-/* make pages [a, b] (b <= a + 1) the pinned pair; returns 0 or -error */
-__device__ int pp_cover(gfs_state* S, const PinFile& pf, PagePair& p, uint32_t a, uint32_t b) {
-    PagePair q;
-    pp_init(q);
-    for (int i = 0; i < 2; i++) {
-        if (p.fr[i] < 0) continue;
-        if (p.pg[i] == a) { q.pg[0] = a; q.fr[0] = p.fr[i]; }
-        else if (p.pg[i] == b && b != a) { q.pg[1] = b; q.fr[1] = p.fr[i]; }
-        else unpin(S, (uint32_t)p.fr[i]);
-    }
-    const uint32_t want[2] = {a, b};
-    for (int i = 0; i < (b == a ? 1 : 2); i++) {
-        if (q.fr[i] >= 0) continue;
-        bool fresh;
-        const int r = pin_page(S, pf, want[i], GFS_PIN_READ, &fresh);
-        if (r < 0) {
-            for (int j = 0; j < 2; j++)
-                if (q.fr[j] >= 0) unpin(S, (uint32_t)q.fr[j]);
-            pp_init(p);
-            return r;
+/* A warp's window of up to `batch` pinned pages of one file, lane j holding
+ * page lo + j, so the misses of a large request are in flight together; a
+ * pool short of frames makes it fall back to windows of at most two pages
+ * whose pins wait for frames.  cover() slides it to start at page pa so
+ * that it holds pages pa..pb (pb <= pa + 1, the pages of one piece). */
+struct PageWindow {
+    PinFile pf;
+    uint32_t lo = 0, nw = 0, batch = 8, last = 0;
+    int fr = -1;
+    __device__ int cover(gfs_state* S, uint32_t pa, uint32_t pb) {
+        if (nw != 0 && pa >= lo && pb < lo + nw) return 0;
+        const uint32_t lane = threadIdx.x & 31u;
+        for (;;) {
+            if (lane < nw) unpin(S, (uint32_t)fr);
+            nw = last - pa + 1u < batch ? last - pa + 1u : batch;
+            if (nw < pb - pa + 1u) nw = pb - pa + 1u;
+            lo = pa;
+            fr = -1;
+            if (lane < nw) {
+                bool fresh;
+                fr = pin_page(S, pf, lo + lane, GFS_PIN_READ | (nw > 2 ? GFS_PIN_NOALLOC : 0), &fresh);
+                if (fr >= 0 && fresh) publish_valid(S, (uint32_t)fr);
+            }
+            const unsigned nomem = __ballot_sync(0xFFFFFFFFu, lane < nw && fr == -GFS_ENOMEM);
+            const unsigned bad = __ballot_sync(0xFFFFFFFFu, lane < nw && fr < 0 && fr != -GFS_ENOMEM);
+            if (!bad && !nomem) return 0;
+            if (lane < nw && fr >= 0) unpin(S, (uint32_t)fr);
+            nw = 0;
+            if (bad) return __shfl_sync(0xFFFFFFFFu, fr, __ffs(bad) - 1);
+            if (batch <= 2) return -GFS_ENOMEM;
+            batch = 2;
         }
-        if (fresh) publish_valid(S, (uint32_t)r);
-        q.pg[i] = want[i];
-        q.fr[i] = r;
     }
-    p = q;
-    return 0;
-}
+    /* the frame of a page inside the window (every lane calls) */
+    __device__ int frame(uint32_t pg) const { return __shfl_sync(0xFFFFFFFFu, fr, (int)(pg - lo)); }
+    __device__ void release(gfs_state* S) {
+        if ((threadIdx.x & 31u) < nw) unpin(S, (uint32_t)fr);
+        nw = 0;
+    }
+};
 
 /* read + XXH64 of [off, end) of a served file, by one warp, at any offset.
- * The range is hashed in logical 512-byte chunks from `off` (so every full
- * chunk is 16 whole stripes): a chunk's bytes are loaded as the 16-byte
- * aligned units of the file that cover it (each inside one page; lane 0
- * keeps the chunk's one or two pages pinned) into `raw`, then shifted into
- * `st` by the chunk's offset within its first unit (funnel shifts of 32-bit
- * words), where lanes 0..3 run the four accumulator lanes over them. */
+ * Pages are pinned in windows of up to 8 (lane j holds page lo + j), so the
+ * misses of a large request are in flight together; a pool short of frames
+ * falls back to windows of one page (multi-page pins do not wait for
+ * frames).  The range is hashed in logical 512-byte chunks from `off` (so
+ * every full chunk is 16 whole stripes): a chunk's bytes are loaded as the
+ * 16-byte aligned units of the file that cover it (each inside one page)
+ * into `raw`, then shifted into `st` by the chunk's offset within its first
+ * unit (funnel shifts of 32-bit words), where lanes 0..3 run the four
+ * accumulator lanes over them. */
 __device__ int sv_read_xxh(gfs_state* S, const ServeDev& D, int fd, uint64_t off, uint64_t end, uint8_t* st,
                            uint8_t* raw, unsigned long long* result) {
     const int lane = threadIdx.x & 31;
     const uint32_t lp = S->log_page, pmask = S->page_size - 1u;
-    PinFile pf;
-    PagePair pp;
-    if (lane == 0) { pf = pin_file(S, fd); pp_init(pp); }
+    PageWindow win;
+    win.pf = pin_file(S, fd);
+    win.last = end > off ? (uint32_t)((end - 1) >> lp) : 0u;
     uint64_t v = gfsx::acc_init(lane & 3);
     int err = 0;
     const uint8_t* tail = st;
     for (uint64_t pos = off; pos < end;) {
         const uint32_t clen = end - pos < 512u ? (uint32_t)(end - pos) : 512u;
         const uint64_t a0 = pos & ~15ull, cend = pos + clen;
-        int r = 0;
-        if (lane == 0) r = pp_cover(S, pf, pp, (uint32_t)(a0 >> lp), (uint32_t)((cend - 1) >> lp));
-        r = __shfl_sync(0xFFFFFFFFu, r, 0);
-        if (r < 0) { err = r; break; }
-        uint32_t pg0 = 0;
-        int f0 = 0, f1 = 0;
-        if (lane == 0) { pg0 = pp.pg[0]; f0 = pp.fr[0]; f1 = pp.fr[1]; }
-        pg0 = __shfl_sync(0xFFFFFFFFu, pg0, 0);
-        f0 = __shfl_sync(0xFFFFFFFFu, f0, 0);
-        f1 = __shfl_sync(0xFFFFFFFFu, f1, 0);
-        /* the aligned units covering [pos, cend): at most 33 */
-        for (uint32_t u = (uint32_t)lane; a0 + 16ull * u < cend; u += 32u) {
-            const uint64_t q = a0 + 16ull * u;
-            const int fr = (uint32_t)(q >> lp) == pg0 ? f0 : f1;
-            *(uint4*)(raw + 16u * u) = ld_cg4(S->pool + ((size_t)fr << lp) + (q & pmask));
-        }
-        __syncwarp();
-        /* shift by pos & 15 into st (16 bytes a lane, 512 at most) */
+        err = win.cover(S, (uint32_t)(a0 >> lp), (uint32_t)((cend - 1) >> lp));
+        if (err) break;
         const uint32_t sh = (uint32_t)(pos & 15u);
-        if (16u * (uint32_t)lane < clen) {
+        if (sh == 0u) {
+            /* an aligned range (every chunk of it is): units straight into st */
+            const uint64_t q = a0 + 16ull * (uint32_t)lane;
+            const int f = win.frame(q < cend ? (uint32_t)(q >> lp) : win.lo);
+            if (q < cend) *(uint4*)(st + 16u * (uint32_t)lane) = ld_cg4(S->pool + ((size_t)f << lp) + (q & pmask));
+            __syncwarp();
+        } else {
+            /* the aligned units covering [pos, cend): at most 33 */
+            for (uint32_t u0 = 0; a0 + 16ull * u0 < cend; u0 += 32u) {
+                const uint64_t q = a0 + 16ull * (u0 + (uint32_t)lane);
+                const int f = win.frame(q < cend ? (uint32_t)(q >> lp) : win.lo);
+                if (q < cend)
+                    *(uint4*)(raw + 16u * (u0 + (uint32_t)lane)) = ld_cg4(S->pool + ((size_t)f << lp) + (q & pmask));
+            }
+            __syncwarp();
+        }
+        /* shift by pos & 15 into st (16 bytes a lane, 512 at most) */
+        if (sh != 0u && 16u * (uint32_t)lane < clen) {
             const uint32_t* w = (const uint32_t*)(raw + (sh & ~3u) + 16u * (uint32_t)lane);
             const uint32_t b = 8u * (sh & 3u);
             const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], x3 = w[3], x4 = w[4];
@@ -1256,7 +1261,7 @@ __device__ int sv_read_xxh(gfs_state* S, const ServeDev& D, int fd, uint64_t off
         pos = cend;
         if (pos < end) __syncwarp();
     }
-    if (lane == 0) pp_release(S, pp);
+    win.release(S);
     if (err) return err;
     const uint64_t v1 = __shfl_sync(0xFFFFFFFFu, v, 0), v2 = __shfl_sync(0xFFFFFFFFu, v, 1),
                    v3 = __shfl_sync(0xFFFFFFFFu, v, 2), v4 = __shfl_sync(0xFFFFFFFFu, v, 3);
@@ -1271,9 +1276,9 @@ __device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, ui
                        uint8_t* wscr, const uint4* km, unsigned long long* result) {
     const int lane = threadIdx.x & 31;
     const uint32_t lp = S->log_page, pmask = S->page_size - 1u;
-    PinFile pf;
-    PagePair pp;
-    if (lane == 0) { pf = pin_file(S, fd); pp_init(pp); }
+    PageWindow win;
+    win.pf = pin_file(S, fd);
+    win.last = end > off ? (uint32_t)((end - 1) >> lp) : 0u;
     Tbl t;
     t.tags = D.G.tags;
     t.disp = D.G.disp;
@@ -1287,23 +1292,16 @@ __device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, ui
         /* stage [seg - 16, seg + 512 + 64) with bytes outside [off, end) zero */
         const uint64_t lo = seg >= off + GR_LB ? seg - GR_LB : off;
         const uint64_t hi = seg + GR_SEG + GR_LA < end ? seg + GR_SEG + GR_LA : end;
-        int r = 0;
-        if (lane == 0) r = pp_cover(S, pf, pp, (uint32_t)(lo >> lp), (uint32_t)((hi - 1) >> lp));
-        r = __shfl_sync(0xFFFFFFFFu, r, 0);
+        const int r = win.cover(S, (uint32_t)(lo >> lp), (uint32_t)((hi - 1) >> lp));
         if (r < 0) { err = r; break; }
-        uint32_t pg0 = 0, pg1 = 0;
-        int f0 = 0, f1 = 0;
-        if (lane == 0) { pg0 = pp.pg[0]; pg1 = pp.pg[1]; f0 = pp.fr[0]; f1 = pp.fr[1]; }
-        pg0 = __shfl_sync(0xFFFFFFFFu, pg0, 0);
-        pg1 = __shfl_sync(0xFFFFFFFFu, pg1, 0);
-        f0 = __shfl_sync(0xFFFFFFFFu, f0, 0);
-        f1 = __shfl_sync(0xFFFFFFFFu, f1, 0);
-        for (uint32_t u = (uint32_t)lane; u < (GR_LB + GR_SEG + GR_LA) / 16u; u += 32u) {
+        for (uint32_t u0 = 0; u0 < (GR_LB + GR_SEG + GR_LA) / 16u; u0 += 32u) {
+            const uint32_t u = u0 + (uint32_t)lane;
             const int64_t a = (int64_t)seg - GR_LB + 16 * (int64_t)u; /* file offset of this 16-byte unit */
+            const bool in = u < (GR_LB + GR_SEG + GR_LA) / 16u && a + 16 > (int64_t)off && (uint64_t)a < end;
+            const int fr = win.frame(in ? (uint32_t)((uint64_t)a >> lp) : win.lo);
+            if (u >= (GR_LB + GR_SEG + GR_LA) / 16u) continue;
             uint4 w = make_uint4(0, 0, 0, 0);
-            if (a + 16 > (int64_t)off && (uint64_t)a < end) {
-                const uint32_t pg = (uint32_t)((uint64_t)a >> lp);
-                const int fr = pg == pg0 ? f0 : f1;
+            if (in) {
                 w = ld_cg4(S->pool + ((size_t)fr << lp) + ((uint64_t)a & pmask));
                 const uint64_t rem = end - (uint64_t)a;
                 const int64_t skip = (int64_t)off - a; /* bytes before off in this unit */
@@ -1330,7 +1328,7 @@ __device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, ui
         scan_segment<false>(D.G, t, st + GR_LB, d, 0u, wscr, km, sink);
         __syncwarp();
     }
-    if (lane == 0) pp_release(S, pp);
+    win.release(S);
     if (err) return err;
     uint32_t n = sink.n;
 #pragma unroll

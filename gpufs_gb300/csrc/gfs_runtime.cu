@@ -1285,8 +1285,12 @@ void* gfs__host_bounce(gfs_ctx* c, size_t bytes) {
         if (c->h_bounce) cudaFreeHost(c->h_bounce);
         c->h_bounce = nullptr;
         c->h_bounce_cap = 0;
+        /* powers of two up to 64 MiB (small requests grow rarely); above,
+         * the request rounded up to 2 MiB, so a large count matrix pins
+         * about its own size and no more */
         size_t cap = (size_t)1 << 20;
-        while (cap < bytes) cap <<= 1;
+        while (cap < bytes && cap < ((size_t)64 << 20)) cap <<= 1;
+        if (cap < bytes) cap = (bytes + ((size_t)2 << 20) - 1) & ~(((size_t)2 << 20) - 1);
         if (cudaHostAlloc(&c->h_bounce, cap, cudaHostAllocDefault) != cudaSuccess) {
             cudaGetLastError();
             c->h_bounce = nullptr;
