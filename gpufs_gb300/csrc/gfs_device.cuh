@@ -246,10 +246,18 @@ struct Req {
 __device__ __forceinline__ uint32_t* frame_done(gfs_state* S, uint32_t fr) { return S->hdone + fr; }
 __device__ __forceinline__ uint32_t* file_done(gfs_state* S, uint32_t slot) { return S->hdone + S->n_frames + slot; }
 
+/* A wait on the host already ran out in this session: later waits on it
+ * give up at once (one stalled host frees the GPU within about one
+ * timeout, not one timeout per request); gfs_last_error(ctx, 1) clears it */
+__device__ __forceinline__ bool host_stalled(gfs_state* S) {
+    return (ld_rlx(&S->error) & GFS_ERRB_TIMEOUT) != 0u;
+}
+
 /* Publish one request and wait for its completion word (in mapped host
  * memory; the host CPU writes it once the data has landed).  Returns the
  * non-negative result (bytes moved, or 0) or -errno / -GFS_ETIMEDOUT. */
 __device__ __noinline__ int rpc_call(gfs_state* S, const Req& r, uint32_t* done) {
+    if (host_stalled(S)) return -GFS_ETIMEDOUT;
     st_rlx_sys(done, 0u);
     __threadfence_system();
     Waiter w(S->timeout_ns);
@@ -292,7 +300,7 @@ __device__ __noinline__ int rpc_call(gfs_state* S, const Req& r, uint32_t* done)
     count(S, &S->stats.rpc_submitted);
     uint32_t c;
     while ((c = ld_acq_sys(done)) == 0u) {
-        if (!w.tick(1024)) {
+        if (!w.tick(1024) || host_stalled(S)) {
             count(S, &S->stats.timeouts);
             fail_at(S, GFS_ERRB_TIMEOUT, 2 + 16 * (uint32_t)r.op, GFS_ETIMEDOUT); /* no completion */
             return -GFS_ETIMEDOUT;
@@ -485,7 +493,7 @@ __device__ __noinline__ int pin_page(gfs_state* S, const PinFile& pf, uint32_t b
                             atomicSub(&F->st, 1u);
                             return -GFS_EIO; /* the loader failed */
                         }
-                        if (!w.tick(1024)) {
+                        if (!w.tick(1024) || host_stalled(S)) {
                             atomicSub(&F->st, 1u);
                             count(S, &S->stats.timeouts);
                             fail_at(S, GFS_ERRB_TIMEOUT, 4, GFS_ETIMEDOUT); /* LOADING never ended */
