@@ -791,6 +791,41 @@ __device__ __noinline__ void hasher(const GrepDev& P, Shared& sh, uint8_t* stage
  * file read as zero.  false: failed (the CTA is aborting). */
 #define GR_DWIN (GR_LB + GR_SEG + GR_LA + 32) /* bytes per warp window (39 x 16) */
 static_assert(GR_DWIN % 16 == 0 && GR_CONS * GR_DWIN <= GR_STAGES * GR_STAGE, "direct windows live in the stage ring");
+/* The 16-byte unit at file offset off (a multiple of 16) of a file of fsize
+ * bytes, read from q (where that offset's bytes live); zero outside the
+ * file. */
+__device__ __forceinline__ uint4 window_unit(const uint8_t* q, int64_t off, uint64_t fsize) {
+    if (off < 0 || off >= (int64_t)fsize) return make_uint4(0u, 0u, 0u, 0u);
+    if (off + 16 <= (int64_t)fsize) return *(const uint4*)q;
+    /* the file's last partial unit, byte by byte */
+    uint64_t lo = 0, hi = 0;
+    const int n = (int)((int64_t)fsize - off);
+    for (int i = 0; i < n; i++) {
+        const uint64_t b = q[i];
+        if (i < 8) lo |= b << (8 * i);
+        else hi |= b << (8 * (i - 8));
+    }
+    return make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+}
+
+/* The window at file position p of a file with a registered host mapping:
+ * both of a lane's units are loaded before either is stored (a store to the
+ * window could otherwise hold the second load behind the first one's round
+ * trip over the host link). */
+static_assert(GR_DWIN / 16 <= 64, "two 16-byte units per lane");
+__device__ __forceinline__ void load_mapped_window(const GrepDev& P, int f, uint64_t p, uint8_t* buf) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t fsize = P.sizes[f];
+    const int64_t first = (int64_t)p - GR_LB;
+    const uint8_t* src = (const uint8_t*)P.maps[f];
+    const int64_t o0 = first + 16 * (int64_t)lane, o1 = o0 + 16 * 32;
+    const uint4 v0 = window_unit(src + o0, o0, fsize);
+    const uint4 v1 = lane + 32u < GR_DWIN / 16u ? window_unit(src + o1, o1, fsize) : make_uint4(0u, 0u, 0u, 0u);
+    *(uint4*)(buf + 16u * lane) = v0;
+    if (lane + 32u < GR_DWIN / 16u) *(uint4*)(buf + 16u * (lane + 32u)) = v1;
+}
+
+/* The window of a file without a mapping, from its buffer-cache pages. */
 __device__ __noinline__ bool load_window(gfs_state* S, const GrepDev& P, Shared& sh, int f, uint64_t p, uint8_t* buf) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t fsize = P.sizes[f];
@@ -827,27 +862,11 @@ __device__ __noinline__ bool load_window(gfs_state* S, const GrepDev& P, Shared&
     }
     for (uint32_t u = lane; u < GR_DWIN / 16u; u += 32u) {
         const int64_t off = first + 16 * (int64_t)u;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (off >= 0 && off < (int64_t)fsize) {
-            /* 16-byte units never straddle a page (pages are >= 4 KiB) */
-            const uint8_t* q = src ? src + off
-                                   : S->pool + ((size_t)((uint32_t)(off >> lp) == pg0 ? fr0 : fr1) << lp) +
-                                         ((uint64_t)off & ((1ull << lp) - 1u));
-            if (off + 16 <= (int64_t)fsize) {
-                v = *(const uint4*)q;
-            } else {
-                /* the file's last partial unit, byte by byte */
-                uint64_t lo = 0, hi = 0;
-                const int n = (int)((int64_t)fsize - off);
-                for (int i = 0; i < n; i++) {
-                    const uint64_t b = q[i];
-                    if (i < 8) lo |= b << (8 * i);
-                    else hi |= b << (8 * (i - 8));
-                }
-                v = make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
-            }
-        }
-        *(uint4*)(buf + 16u * u) = v;
+        /* 16-byte units never straddle a page (pages are >= 4 KiB) */
+        const uint8_t* q = src ? src + off
+                               : S->pool + ((size_t)((uint32_t)(off >> lp) == pg0 ? fr0 : fr1) << lp) +
+                                     ((uint64_t)off & ((1ull << lp) - 1u));
+        *(uint4*)(buf + 16u * u) = window_unit(q, off, fsize);
     }
     __syncwarp();
     if (!src && lane == 0 && fsize > 0) {
@@ -859,6 +878,31 @@ __device__ __noinline__ bool load_window(gfs_state* S, const GrepDev& P, Shared&
         }
     }
     return true;
+}
+
+/* Direct scan, warp 31 (no producer there): walks the CTA's chunks up to
+ * GR_DPF chunks ahead of the consumers' item counter and asks L2 to fetch
+ * each chunk's bytes from the file's host mapping, so the consumers' window
+ * loads meet lines already on their way.  Purely a hint: it reads nothing
+ * into registers, and gives up quietly on abort or when the consumers stop
+ * moving for the session timeout. */
+#define GR_DPF 4
+__device__ __noinline__ void direct_prefetch(const GrepDev& P, Shared& sh, uint64_t c0, uint64_t c1) {
+    const uint32_t lane = threadIdx.x & 31u;
+    int f = file_of(P, c0);
+    for (uint64_t k = c0; k < c1; k++) {
+        Waiter w(sh.wait_ns);
+        while (c0 + *(volatile uint32_t*)&sh.next_item / GR_CONS + GR_DPF <= k) {
+            if (sh.abort || !w.tick(256)) return;
+        }
+        while (k >= P.chunk_prefix[f + 1]) f++;
+        const uint8_t* src = (const uint8_t*)P.maps[f];
+        if (!src) continue;
+        const uint64_t pos = (k - P.chunk_prefix[f]) * GR_CH, size = P.sizes[f];
+        const uint64_t end = pos + GR_CH + GR_LA < size ? pos + GR_CH + GR_LA : size;
+        for (uint64_t o = pos + 128u * lane; o < end; o += 32u * 128u)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(src + o));
+    }
 }
 
 /* One persistent 1024-thread CTA per SM: warp 31 pins pages and streams
@@ -960,6 +1004,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
     const uint64_t c0 = total * blockIdx.x / gridDim.x, c1 = total * (blockIdx.x + 1) / gridDim.x;
     if (warp == GR_CONS) {
         if (!DIRECT) producer(S, P, sh, stages, c0, c1);
+        else direct_prefetch(P, sh, c0, c1);
         return;
     }
     /* Items (chunk, segment) are taken in order from a shared counter, so a
@@ -1000,7 +1045,10 @@ __global__ void __launch_bounds__(GR_THREADS, 1) k_grep_scan(gfs_state* S, GrepD
             const uint32_t seg0 = (it % NC) * GR_SEG;
             if (seg0 < d.clen && !sh.abort) {
                 uint8_t* buf = stages + (size_t)warp * GR_DWIN;
-                if (load_window(S, P, sh, f, d.pos + seg0, buf)) {
+                bool ok = true;
+                if (P.maps[f]) load_mapped_window(P, f, d.pos + seg0, buf);
+                else ok = load_window(S, P, sh, f, d.pos + seg0, buf);
+                if (ok) {
                     CountSink sink{P, tbl, SMEM, f};
                     scan_segment<SMEM>(P, tbl, buf + GR_LB - seg0, d, it % NC, wscr, sh.kmask, sink);
                 }
@@ -1719,6 +1767,22 @@ static __global__ void k_open_files(const char* names, int n, int* fds, uint64_t
     }
 }
 
+/* counts matrix -> the caller's host memory, written by the SMs through the
+ * host page tables: 16-byte stores where the destination allows, then the
+ * 4-byte tail */
+static __global__ void __launch_bounds__(256) k_counts_out(const uint32_t* __restrict__ src, uint32_t* dst, size_t n) {
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (size_t)gridDim.x * blockDim.x;
+    size_t done = 0;
+    if (((uintptr_t)dst & 15u) == 0u) {
+        const size_t n16 = n / 4u;
+        const uint4* s4 = (const uint4*)src;
+        uint4* d4 = (uint4*)dst;
+        for (size_t i = tid; i < n16; i += nth) d4[i] = __ldg(s4 + i);
+        done = n16 * 4u;
+    }
+    for (size_t i = done + tid; i < n; i += nth) dst[i] = __ldg(src + i);
+}
+
 static __global__ void k_close_files(const int* fds, int n, int* rcs) {
     int f = blockIdx.x;
     if (f >= n) return;
@@ -2172,24 +2236,30 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     {
         /* per file: its host mapping's device address (direct scans read
          * it), chunk prefix sums, and the longest-first order of batched
-         * runs (LPT: the largest file bounds the run, so it starts first);
-         * staged in the pinned buffer after the slots, one copy each */
-        uint64_t* maps = (uint64_t*)(hb + align_up((size_t)n_files * 4, 64));
-        uint64_t* pf = maps + align_up((size_t)n_files, 8);
-        int* order = (int*)(pf + align_up((size_t)n_files + 1, 8));
+         * runs (LPT: the largest file bounds the run, so it starts first).
+         * Copied from pageable memory: the driver stages such a copy before
+         * the call returns, so the vectors may go at once and no round trip
+         * to the device is needed. */
+        std::vector<uint64_t> maps((size_t)n_files), pf((size_t)n_files + 1);
+        std::vector<int> order((size_t)n_files);
         for (int i = 0; i < n_files; i++) {
             unsigned long long a = 0, len = 0;
-            maps[i] = gfs__slot_map(ctx, (uint32_t)fds[i], &a, &len) > 0 && len >= g->sizes[(size_t)i] ? a : 0u;
+            maps[(size_t)i] = gfs__slot_map(ctx, (uint32_t)fds[i], &a, &len) > 0 && len >= g->sizes[(size_t)i] ? a : 0u;
         }
         pf[0] = 0;
-        for (int i = 0; i < n_files; i++) pf[i + 1] = pf[i] + (g->sizes[(size_t)i] + GR_CH - 1) / GR_CH;
-        d.total_chunks = pf[n_files];
-        for (int i = 0; i < n_files; i++) order[i] = i;
-        std::stable_sort(order, order + n_files, [&](int x, int y) { return g->sizes[(size_t)x] > g->sizes[(size_t)y]; });
-        cudaMemcpyAsync((void*)d.maps, maps, (size_t)n_files * 8, cudaMemcpyHostToDevice, s);
-        cudaMemcpyAsync((void*)d.chunk_prefix, pf, ((size_t)n_files + 1) * 8, cudaMemcpyHostToDevice, s);
-        cudaMemcpyAsync((void*)d.file_order, order, (size_t)n_files * 4, cudaMemcpyHostToDevice, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) { gfs_grep_close(g); return -GFS_EIO; }
+        for (int i = 0; i < n_files; i++) pf[(size_t)i + 1] = pf[(size_t)i] + (g->sizes[(size_t)i] + GR_CH - 1) / GR_CH;
+        d.total_chunks = pf[(size_t)n_files];
+        for (int i = 0; i < n_files; i++) order[(size_t)i] = i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int x, int y) { return g->sizes[(size_t)x] > g->sizes[(size_t)y]; });
+        if (cudaMemcpyAsync((void*)d.maps, maps.data(), (size_t)n_files * 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync((void*)d.chunk_prefix, pf.data(), ((size_t)n_files + 1) * 8, cudaMemcpyHostToDevice, s) !=
+                cudaSuccess ||
+            cudaMemcpyAsync((void*)d.file_order, order.data(), (size_t)n_files * 4, cudaMemcpyHostToDevice, s) !=
+                cudaSuccess) {
+            gfs_grep_close(g);
+            return -GFS_EIO;
+        }
     }
     /* shared memory: table (if it fits) + stages + token lists + scratch */
     g->sms = sms;
@@ -2206,7 +2276,14 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     return 0;
 }
 
-static int grep_run(gfs_grep* g, int n_ctas, float* kernel_ms, int direct) {
+static bool counts_out_ok(gfs_grep* g, size_t bytes);
+static void counts_out(gfs_grep* g, uint32_t* host_counts, size_t bytes, cudaStream_t s);
+
+/* One scan (+ the long-run fix-up).  host_counts: when the device may write
+ * the caller's memory (counts_out_ok), the counts are written there on the
+ * same stream, so the run and its counts cost one round trip; otherwise
+ * nullptr. */
+static int grep_run(gfs_grep* g, int n_ctas, float* kernel_ms, int direct, uint32_t* host_counts = nullptr) {
     if (!g) return -GFS_EINVAL;
     if (gfs__activate(g->ctx)) return -GFS_EIO;
     cudaStream_t s = (cudaStream_t)gfs_kernel_stream(g->ctx);
@@ -2240,16 +2317,38 @@ static int grep_run(gfs_grep* g, int n_ctas, float* kernel_ms, int direct) {
         cudaEventDestroy(a);
         cudaEventDestroy(b);
     }
+    if (host_counts) counts_out(g, host_counts, (size_t)g->n_words * g->n_files * 4, s);
+    /* the status words come back through the session's pinned buffer with
+     * the same synchronisation */
+    uint32_t* status = (uint32_t*)gfs__host_bounce(g->ctx, 64);
+    if (!status) return -GFS_ENOMEM;
+    status[0] = status[1] = 0;
+    cudaMemcpyAsync(status, d.status, 8, cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
+    if (le == cudaSuccess) le = cudaGetLastError();
     if (le != cudaSuccess || e != cudaSuccess) {
         fprintf(stderr, "gpufs_gb300: grep kernel failed: %s\n", cudaGetErrorString(le != cudaSuccess ? le : e));
         return -GFS_EIO;
     }
-    uint32_t status[2] = {0, 0};
-    cudaMemcpy(status, d.status, 8, cudaMemcpyDeviceToHost);
     g->last_status[0] = status[0];
     g->last_status[1] = status[1];
     return status[0] ? -((status[0] & GFS_ERRB_TIMEOUT) ? GFS_ETIMEDOUT : GFS_EIO) : 0;
+}
+
+/* Counts of up to 16 MiB go straight from the device into the caller's
+ * memory when the session's device may address pageable host memory: one
+ * kernel writing at link speed, no pinned staging and no host copy.  Larger
+ * matrices keep the pinned path (the caller's pages may not be resident,
+ * and faulting them in from the device is slower than a host copy). */
+static bool counts_out_ok(gfs_grep* g, size_t bytes) {
+    return bytes > 0 && bytes <= ((size_t)16 << 20) && gfs__pageable_access(g->ctx);
+}
+static void counts_out(gfs_grep* g, uint32_t* host_counts, size_t bytes, cudaStream_t s) {
+    const size_t n = bytes / 4u;
+    size_t blocks = (n / 4u + 255u) / 256u;
+    const size_t cap = (size_t)(g->sms > 0 ? g->sms : 1) * 4u;
+    blocks = blocks < 1u ? 1u : (blocks > cap ? cap : blocks);
+    k_counts_out<<<(unsigned)blocks, 256, 0, s>>>(g->dev.counts, host_counts, n);
 }
 
 int gfs_grep_run(gfs_grep* g, int n_ctas, float* kernel_ms) { return grep_run(g, n_ctas, kernel_ms, 0); }
@@ -2361,6 +2460,10 @@ int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts) {
     if (!g) return -GFS_EINVAL;
     cudaStream_t s = (cudaStream_t)gfs_kernel_stream(g->ctx);
     const size_t bytes = (size_t)g->n_words * g->n_files * 4;
+    if (counts_out_ok(g, bytes)) {
+        counts_out(g, host_counts, bytes, s);
+        return cudaStreamSynchronize(s) == cudaSuccess && cudaGetLastError() == cudaSuccess ? 0 : -GFS_EIO;
+    }
     /* through the session's pinned buffer: DMA at link speed, then a host
      * copy (a pageable copy is staged by the driver and much slower).  Up to
      * 1 GiB goes in one DMA and is copied out by several host threads (a
@@ -2662,8 +2765,12 @@ int gfs_grep_text(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     gfs_grep* g = nullptr;
     int rc = gfs_grep_open(ctx, dict_path, paths, n_files, &g);
     if (rc) return rc;
-    rc = gfs_grep_run_direct(g, n_ctas, nullptr); /* one pass: read straight from the files' mappings */
-    if (!rc) rc = gfs_grep_counts(g, host_counts);
+    /* one pass, read straight from the files' mappings; the counts come
+     * back with the run's own synchronisation where the device may write
+     * the caller's memory */
+    const bool merged = counts_out_ok(g, (size_t)g->n_words * g->n_files * 4);
+    rc = grep_run(g, n_ctas, nullptr, 1, merged ? host_counts : nullptr);
+    if (!rc && !merged) rc = gfs_grep_counts(g, host_counts);
     int c = gfs_grep_close(g);
     return rc ? rc : c;
 }

@@ -317,3 +317,24 @@ def test_table_seeds_and_sizes(built, shm_dir):
             got = g.grep_text(s, dpath, paths)
             assert np.array_equal(got, want), nd
         assert s.last_error() == 0
+
+
+@pytest.mark.parametrize("shift", [0, 4, 8, 12])
+def test_counts_into_any_host_buffer(sess, shm_dir, shift):
+    """The counts reach the caller's buffer whatever its alignment (the
+    device writes it with 16-byte stores where the address allows, else
+    4-byte ones), and the one-call grep_text's merged run + counts gives the
+    same matrix."""
+    paths, dpath = datagen.grep_corpus(shm_dir, n_files=3, total_bytes=2 * (1 << 20) + 4321, n_vocab=3000,
+                                       n_dict=777, seed=11)
+    with g.Grep(sess, dpath, paths) as gr:
+        gr.run(0, direct=True)
+        want = gr.counts()
+        n = want.size
+        raw = np.full(n * 4 + 64, 0xAB, dtype=np.uint8)
+        base = (-raw.ctypes.data) % 16 + shift  # 16-byte aligned plus shift
+        view = raw[base:base + n * 4].view(np.uint32)
+        assert sess.L.gfs_grep_counts(gr._h, view.ctypes.data) == 0
+        assert np.array_equal(view.reshape(want.shape), want)
+        assert np.all(raw[:base] == 0xAB) and np.all(raw[base + n * 4:] == 0xAB)  # nothing outside written
+    assert np.array_equal(g.grep_text(sess, dpath, paths), want)
