@@ -3,9 +3,10 @@
  * y = A x with A (rows x cols FP32, row-major) and x read through gmmap, y
  * written through gmmap of a write-once file.
  *
- * Each block owns a contiguous run of rows and keeps one matrix page mapped
- * at a time (the reference's get_row, :45-60, remaps only when the cursor
- * leaves the page); eight whole rows of a page are one pass in which every
+ * Blocks take groups of eight rows from a launch-wide counter and keep one
+ * matrix page mapped at a time (the reference's get_row, :45-60, remaps only
+ * when the cursor leaves the page; the reference gives each block a fixed
+ * run of rows); eight whole rows of a page are one pass in which every
  * thread keeps sixteen 16-byte loads in flight; rows are reduced in a fixed
  * order (warp shuffles, then one warp over the partials), so results are
  * deterministic -- the reference adds the per-thread partials with a
@@ -36,6 +37,16 @@ long long gfs__sum_results(long long* d, int n, cudaStream_t s);
 namespace {
 
 __device__ unsigned int g_init_lock; /* INIT_LOCK of the reference sample */
+__device__ unsigned long long g_bm_next; /* next group of eight rows to take (reset per launch) */
+
+/* a group of eight rows taken ahead, with its matrix page pinned */
+struct PageAhead {
+    unsigned long long g; /* group index (>= the group count: none left) */
+    int frame;            /* pinned frame, -1 if none */
+    int err;              /* map_pin's error */
+    int fresh;            /* the frame still has to be filled (fill) */
+    gfsd::MapFill fill;
+};
 
 /* block-wide sum of one float per thread, fixed order */
 __device__ float block_sum(float v, float* red) {
@@ -81,19 +92,21 @@ __device__ float dot_part(const float* a, const float* b, uint32_t n) {
 }
 
 /* Eight rows at once: a (16-byte aligned) holds rows of stride4 float4s,
- * b the vector.  Each thread takes two column steps per iteration: two
- * float4s of b and the eight rows' float4s beside each (sixteen 16-byte
- * loads in flight, about 90 registers, which the 512-thread launch bound
- * leaves room for); the eight sums are reduced together in a fixed order.
- * y[0..7] (shared) are valid after return. */
-__device__ __noinline__ void dot_rows8(const float* a, size_t stride4, const float* b, uint32_t n4, float* red, float* y) {
+ * b the vector.  The first nct threads of the block stream the rows (the
+ * others, if any, only join the reduction); each takes two column steps per
+ * iteration: two float4s of b and the eight rows' float4s beside each
+ * (sixteen 16-byte loads in flight, about 90 registers, which the 512-thread
+ * launch bound leaves room for); the eight sums are reduced together in a
+ * fixed order.  y[0..7] (shared) are valid after return. */
+__device__ __noinline__ void dot_rows8(const float* a, size_t stride4, const float* b, uint32_t n4, float* red, float* y,
+                                       uint32_t nct) {
     float s[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) s[k] = 0.f;
     const float4* a4 = (const float4*)a;
     const float4* b4 = (const float4*)b;
-    const uint32_t bd = blockDim.x;
-    uint32_t i = threadIdx.x;
+    const uint32_t bd = nct;
+    uint32_t i = threadIdx.x < nct ? threadIdx.x : n4;
     for (; i + bd < n4; i += 2u * bd) {
         const float4 q0 = __ldg(b4 + i), q1 = __ldg(b4 + i + bd);
         float4 p0[8], p1[8];
@@ -147,10 +160,24 @@ __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
     __shared__ float red[8 * 32];
     __shared__ float ys[8];
     __shared__ int s_fail;
+    __shared__ unsigned long long s_grp[2];
+    __shared__ PageAhead s_pa[2];
     const uint32_t page = g_gfs->page_size;
-    int zfd_m = gopen(f_m, O_GRDONLY);
-    int zfd_o = gopen(f_o, O_GWRONCE);
-    int zfd_v = gopen(f_v, O_GRDONLY);
+    /* the three opens go out together, from threads of different warps
+     * (one host round trip instead of three when the files need one); a
+     * block of fewer warps opens them in turn */
+    __shared__ int s_fd[3];
+    {
+        const char* names[3] = {f_m, f_o, f_v};
+        const int flags[3] = {O_GRDONLY, O_GWRONCE, O_GRDONLY};
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            if (threadIdx.x == (32u * (unsigned)k) % blockDim.x) s_fd[k] = single_thread_open(names[k], flags[k]);
+        __syncthreads();
+    }
+    int zfd_m = s_fd[0];
+    int zfd_o = s_fd[1];
+    int zfd_v = s_fd[2];
     if (zfd_m < 0 || zfd_o < 0 || zfd_v < 0) {
         if (threadIdx.x == 0) res[blockIdx.x] = zfd_m < 0 ? zfd_m : (zfd_o < 0 ? zfd_o : zfd_v);
         if (zfd_m >= 0) gclose(zfd_m);
@@ -159,20 +186,14 @@ __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
         return;
     }
     /* the first block truncates the output, the others wait for it
-     * (bigmatrix_mmap.cu:88-97, INIT_LOCK) */
+     * (bigmatrix_mmap.cu:88-97, INIT_LOCK) -- but only before their first
+     * store of y, so the truncation overlaps their first rows */
     if (threadIdx.x == 0) {
         s_fail = 0;
-        unsigned int prev = atomicCAS(&g_init_lock, 0u, 1u);
-        if (prev == 0u) {
+        if (atomicCAS(&g_init_lock, 0u, 1u) == 0u) {
             single_thread_ftruncate(zfd_o, 0);
             __threadfence();
             atomicExch(&g_init_lock, 2u);
-        } else {
-            unsigned long long deadline = gfs_globaltimer() + 30000000000ULL;
-            while (atomicAdd(&g_init_lock, 0u) != 2u) {
-                if (gfs_globaltimer() > deadline) { s_fail = -GFS_ETIMEDOUT; break; }
-                __nanosleep(1000);
-            }
         }
     }
     __syncthreads();
@@ -193,8 +214,6 @@ __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
             x = xs;
         }
     }
-    const uint64_t per = rows ? (rows + gridDim.x - 1) / gridDim.x : 0;
-    const uint64_t r0 = (uint64_t)blockIdx.x * per, r1 = r0 + per < rows ? r0 + per : rows;
     volatile uint8_t* mpage = (volatile uint8_t*)-1;
     uint64_t mbase = ~0ull;
     volatile uint8_t* opage = (volatile uint8_t*)-1;
@@ -202,8 +221,21 @@ __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
     /* map the output page holding y[r] (block-collective) and store y there
      * (thread 0; gmunmap of that page later is block-collective, so the
      * store is ordered before it without a barrier of its own) */
+    bool inited = false;
     auto put_y = [&](uint64_t r, float y) {
         const uint64_t oo = r * 4, ob = oo / page * page;
+        if (!inited) {
+            inited = true;
+            if (threadIdx.x == 0) {
+                const unsigned long long deadline = gfs_globaltimer() + 30000000000ULL;
+                while (atomicAdd(&g_init_lock, 0u) != 2u) {
+                    if (gfs_globaltimer() > deadline) { s_fail = -GFS_ETIMEDOUT; break; }
+                    __nanosleep(1000);
+                }
+            }
+            __syncthreads();
+            if (s_fail) { result = s_fail; return; }
+        }
         if (ob != obase) {
             if (opage != (volatile uint8_t*)-1) gmunmap(opage, 0);
             uint64_t olen = rows * 4 - ob < page ? rows * 4 - ob : page;
@@ -222,35 +254,9 @@ __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
         if (mpage == (volatile uint8_t*)-1) { result = -GFS_EIO; mbase = ~0ull; return; }
         mbase = pb;
     };
-    const bool vec4 = (cols & 3u) == 0u && (((uintptr_t)x) & 15u) == 0u;
-    const uint8_t* dm = (direct && !result) ? (const uint8_t*)gfs_direct_addr(zfd_m, 0, size_m * 4) : nullptr;
-    if (dm) {
-        /* the whole matrix in one mapping: eight-row passes anywhere */
-        for (uint64_t r = r0; r < r1 && !result;) {
-            if (vec4 && r + 8 <= r1) {
-                dot_rows8((const float*)(dm + r * cols * 4), cols / 4, x, (uint32_t)(cols / 4), red, ys);
-                for (int k = 0; k < 8 && !result; k++) put_y(r + (uint64_t)k, ys[k]);
-                r += 8;
-            } else {
-                float y = block_sum(dot_part((const float*)(dm + r * cols * 4), x, (uint32_t)cols), red);
-                put_y(r, y);
-                r++;
-            }
-        }
-    }
-    for (uint64_t r = dm ? r1 : r0; r < r1 && !result;) {
+    /* one row through the cache; it may span pages: walk its segments */
+    auto row_cached = [&](uint64_t r) {
         const uint64_t rbeg = r * cols * 4, rend = rbeg + cols * 4;
-        const uint64_t pb0 = rbeg / page * page;
-        if (vec4 && r + 8 <= r1 && rbeg + 8 * cols * 4 <= pb0 + page) {
-            /* eight whole rows inside one page */
-            map_m(pb0);
-            if (result) break;
-            dot_rows8((const float*)(mpage + (rbeg - pb0)), cols / 4, x, (uint32_t)(cols / 4), red, ys);
-            for (int k = 0; k < 8 && !result; k++) put_y(r + (uint64_t)k, ys[k]);
-            r += 8;
-            continue;
-        }
-        /* one row; it may span pages: walk its segments */
         float acc = 0.f;
         for (uint64_t pos = rbeg; pos < rend && !result;) {
             const uint64_t pb = pos / page * page;
@@ -260,17 +266,138 @@ __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
             acc += dot_part((const float*)(mpage + (pos - pb)), x + (pos - rbeg) / 4, (uint32_t)((seg_end - pos) / 4));
             pos = seg_end;
         }
-        if (result) break;
-        float y = block_sum(acc, red);
-        put_y(r, y);
-        r++;
+        if (result) return;
+        put_y(r, block_sum(acc, red));
+    };
+    const bool vec4 = (cols & 3u) == 0u && (((uintptr_t)x) & 15u) == 0u;
+    const uint8_t* dm = (direct && !result) ? (const uint8_t*)gfs_direct_addr(zfd_m, 0, size_m * 4) : nullptr;
+    /* Rows go in groups of eight, taken from a launch-wide counter: every
+     * block stays busy to the end whatever the row count and grid, and no
+     * block starts in the middle of a page.  A group inside one mapped page
+     * (or anywhere in the direct mapping) is one eight-row pass; any other
+     * goes row by row. */
+    const uint64_t groups = (rows + 7u) / 8u;
+    long long done = 0;
+    /* Lookahead form, for a cached matrix whose groups of eight rows each lie
+     * inside one page (16-byte aligned rows): the block's last warp takes the
+     * next group and pins its page (copying it in from the file's mapping if
+     * it missed) while the other warps stream the current one, so no pass
+     * waits on a page-index lookup.  The mapper also drops the pin of the
+     * group before, whose rows every warp has finished by then. */
+    const bool ahead = !dm && vec4 && cols && !result && blockDim.x >= 64u && (blockDim.x & 31u) == 0u &&
+                       (uint64_t)page % (8u * cols * 4u) == 0u;
+    if (ahead) {
+        const uint32_t mw = blockDim.x / 32u - 1u, warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+        auto take = [&](PageAhead* d) {
+            d->g = atomicAdd(&g_bm_next, 1ull);
+            d->err = 0;
+            d->fresh = 0;
+            d->frame = -1;
+            d->fill.len = 0;
+            if (d->g >= groups) return;
+            const uint64_t pb = d->g * 8u * cols * 4u / page * page;
+            bool fr = false;
+            const int f = gfsd::map_pin(g_gfs, zfd_m, pb, 0, &fr, 1, &d->fill);
+            if (f < 0) {
+                d->err = f;
+                return;
+            }
+            d->frame = f;
+            d->fresh = fr ? 1 : 0;
+        };
+        if (threadIdx.x == 0) take(&s_pa[0]);
+        __syncthreads();
+        /* mapper lane 0: held = the pinned frame of the group in hand, nxt =
+         * that of the group taken ahead (both dropped at the end) */
+        int held = -1, nxt = s_pa[0].frame;
+        for (uint32_t it = 0;; it++) {
+            PageAhead& cur = s_pa[it & 1u];
+            if (cur.err) {
+                result = cur.err;
+                break;
+            }
+            if (cur.g >= groups) break;
+            if (cur.fresh) gfsd::blk_fill_fresh(g_gfs, &cur.frame, cur.fill);
+            if (warp == mw && lane == 0) {
+                if (held >= 0) gfsd::unpin(g_gfs, (uint32_t)held);
+                held = cur.frame;
+                take(&s_pa[(it + 1u) & 1u]);
+                nxt = s_pa[(it + 1u) & 1u].frame;
+            }
+            const uint64_t r = cur.g * 8u, rn = rows - r < 8u ? rows - r : 8u;
+            const uint64_t rbeg = r * cols * 4, pb0 = rbeg / page * page;
+            const float* rowp = (const float*)(gfsd::frame_data(g_gfs, (uint32_t)cur.frame) + (rbeg - pb0));
+            if (rn == 8u) {
+                dot_rows8(rowp, cols / 4, x, (uint32_t)(cols / 4), red, ys, blockDim.x - 32u);
+                for (uint64_t k = 0; k < 8u && !result; k++) put_y(r + k, ys[k]);
+            } else {
+                for (uint64_t k = 0; k < rn && !result; k++) put_y(r + k, block_sum(dot_part(rowp + k * cols, x, (uint32_t)cols), red));
+            }
+            done += (long long)rn;
+            __syncthreads(); /* the next slot is filled; this group's rows are done */
+            if (result) break;
+        }
+        __syncthreads();
+        if (warp == mw && lane == 0) {
+            if (held >= 0) gfsd::unpin(g_gfs, (uint32_t)held);
+            /* a group taken ahead but never started (an error ended the
+             * loop after the take; at a normal end there is none).  Its pin
+             * is its own even when it shares the frame of the group in hand */
+            if (nxt >= 0) gfsd::unpin(g_gfs, (uint32_t)nxt);
+        }
+    }
+    for (uint32_t it = 0; !ahead && !result && cols; it++) {
+        if (threadIdx.x == 0) s_grp[it & 1u] = atomicAdd(&g_bm_next, 1ull);
+        __syncthreads();
+        const uint64_t gi = s_grp[it & 1u];
+        if (gi >= groups) break;
+        const uint64_t r = gi * 8u, rn = rows - r < 8u ? rows - r : 8u;
+        const uint64_t rbeg = r * cols * 4, pb0 = rbeg / page * page;
+        if (dm && vec4 && rn == 8u) {
+            dot_rows8((const float*)(dm + rbeg), cols / 4, x, (uint32_t)(cols / 4), red, ys, blockDim.x);
+        } else if (!dm && vec4 && rn == 8u && rbeg + 8 * cols * 4 <= pb0 + page) {
+            map_m(pb0);
+            if (result) break;
+            dot_rows8((const float*)(mpage + (rbeg - pb0)), cols / 4, x, (uint32_t)(cols / 4), red, ys, blockDim.x);
+        } else {
+            for (uint64_t k = 0; k < rn && !result; k++) {
+                if (dm) put_y(r + k, block_sum(dot_part((const float*)(dm + (r + k) * cols * 4), x, (uint32_t)cols), red));
+                else row_cached(r + k);
+            }
+            done += (long long)rn;
+            continue;
+        }
+        for (uint64_t k = 0; k < 8u && !result; k++) put_y(r + k, ys[k]);
+        done += 8;
     }
     if (mpage != (volatile uint8_t*)-1) gmunmap(mpage, 0);
     if (opage != (volatile uint8_t*)-1) gmunmap(opage, 0);
     if (xmap != (volatile void*)-1) gmunmap(xmap, 0);
-    int c0 = gclose(zfd_m), c1 = gclose(zfd_v), c2 = gclose(zfd_o);
+    /* Closes: the block writes back the output first if it is the last to
+     * close it (block-collective); then the output's host close and those of
+     * the two read-only files (nothing to write back) go out together from
+     * threads of different warps, so their host round trips overlap. */
+    __shared__ int s_cl[4];
+    if (threadIdx.x == 0) s_cl[3] = gfsd::file_close_begin(g_gfs, zfd_o);
+    __syncthreads();
+    const int yb = s_cl[3];
+    const int fl = yb > 0 ? gfsd::blk_flush(g_gfs, zfd_o) : 0;
+    {
+        const unsigned tm = 32u % blockDim.x, tv = 64u % blockDim.x;
+        if (threadIdx.x == 0) s_cl[2] = yb > 0 ? gfsd::file_close_finish(g_gfs, zfd_o) : yb;
+        if (threadIdx.x == tm) {
+            const int b = gfsd::file_close_begin(g_gfs, zfd_m);
+            s_cl[0] = b > 0 ? gfsd::file_close_finish(g_gfs, zfd_m) : b;
+        }
+        if (threadIdx.x == tv) {
+            const int b = gfsd::file_close_begin(g_gfs, zfd_v);
+            s_cl[1] = b > 0 ? gfsd::file_close_finish(g_gfs, zfd_v) : b;
+        }
+    }
+    __syncthreads();
+    const int c0 = s_cl[0], c1 = s_cl[1], c2 = fl < 0 ? fl : s_cl[2];
     if (threadIdx.x == 0)
-        res[blockIdx.x] = result ? result : (c0 < 0 ? c0 : (c1 < 0 ? c1 : (c2 < 0 ? c2 : (long long)(r1 > r0 ? r1 - r0 : 0))));
+        res[blockIdx.x] = result ? result : (c0 < 0 ? c0 : (c1 < 0 ? c1 : (c2 < 0 ? c2 : done)));
 }
 
 } // namespace
@@ -304,6 +431,8 @@ static int bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, c
     cudaMemsetAsync(res, 0, sizeof(long long) * (size_t)nblocks, s);
     unsigned int zero = 0;
     cudaMemcpyToSymbolAsync(g_init_lock, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, s);
+    const unsigned long long zero64 = 0;
+    cudaMemcpyToSymbolAsync(g_bm_next, &zero64, sizeof zero64, 0, cudaMemcpyHostToDevice, s);
     /* x scratch only when x does not fit a page */
     float* xs = nullptr;
     long long vbytes = 0;

@@ -420,17 +420,39 @@ __device__ __forceinline__ int mmap_mode(int oflags) {
 }
 
 /* Single-thread part of a mapping: pin the page holding `off`.  Returns the
- * frame or -error; *fresh when the caller must zero + publish it. */
-__device__ __forceinline__ int map_pin(gfs_state* S, int fd, uint64_t off, uint64_t size, bool* fresh, int ref) {
+ * frame or -error; *fresh when the caller must fill (or zero) and publish it.
+ * fill (optional): for a read-only file with a registered host mapping a
+ * missed page comes back fresh with fill->len > 0: the caller's threads copy
+ * the page's fill->len bytes from the mapping (fill->map, page fill->blk;
+ * no host request).  The caller holds no other unfilled page, so a page
+ * another caller is loading is simply waited for.  Without fill, or for
+ * other files, fill->len is 0 and a fresh page is zeroed. */
+struct MapFill {
+    uint64_t map, size, len;
+    uint32_t blk;
+};
+__device__ __forceinline__ int map_pin(gfs_state* S, int fd, uint64_t off, uint64_t size, bool* fresh, int ref,
+                                       MapFill* fill = nullptr) {
     *fresh = false;
+    if (fill) fill->len = 0;
     if (fd < 0 || (uint32_t)fd >= S->n_files || sstatus(ld_acq(&S->files[fd].st)) != GFS_SS_OPEN) return -GFS_EBADF;
     PinFile pf = pin_file(S, fd);
     const uint64_t page = (uint64_t)S->page_size;
     uint64_t boff = off & (page - 1);
     if (boff + size > page) { set_error(S, GFS_ERRB_ARG); return -GFS_EINVAL; }
     if (pf.oflags == O_GRDONLY && off >= pf.size) return -GFS_EINVAL;
-    int r = pin_page(S, pf, (uint32_t)(off >> S->log_page), mmap_mode(pf.oflags), fresh);
+    const uint32_t blk = (uint32_t)(off >> S->log_page);
+    const bool smfill = fill && pf.oflags == O_GRDONLY && pf.map_dev;
+    int r = pin_page(S, pf, blk, mmap_mode(pf.oflags) | (smfill ? GFS_PIN_SMFILL : 0), fresh);
+    if (r == -GFS_EAGAIN) r = pin_page(S, pf, blk, mmap_mode(pf.oflags), fresh);
     if (r < 0) return r;
+    if (*fresh && smfill) {
+        const uint64_t pst = (uint64_t)blk << S->log_page;
+        fill->map = pf.map_dev;
+        fill->size = pf.size;
+        fill->blk = blk;
+        fill->len = pf.size - pst < page ? pf.size - pst : page;
+    }
     if (ref > 1) atomicAdd(&S->frames[r].st, (uint32_t)(ref - 1));
     if (pf.oflags != O_GRDONLY) {
         atomicMax(&S->frames[r].content, (uint32_t)(boff + size));
@@ -439,20 +461,46 @@ __device__ __forceinline__ int map_pin(gfs_state* S, int fd, uint64_t off, uint6
     return r;
 }
 
+/* Block-collective: make a fresh frame returned by map_pin valid -- its
+ * bytes copied from the file's mapping (fill.len > 0) or zeros -- and
+ * publish it.  *frame is in shared memory. */
+__device__ __forceinline__ void blk_fill_fresh(gfs_state* S, int* frame, const MapFill& fill) {
+    const int tid = blk_tid(), nthr = blk_nthr();
+    const uint32_t r = (uint32_t)*frame;
+    uint8_t* d = frame_data(S, r);
+    const uint64_t len = fill.len, l16 = (len + 15u) & ~15ull;
+    if (len) blk_fill_round(S, frame, 1u, fill.blk, fill.map, fill.size);
+    /* the rest of the page (all of it without a fill) reads as zeros */
+    for (uint64_t k = len + (uint64_t)tid; k < l16; k += (uint64_t)nthr) d[k] = 0;
+    for (uint64_t k = l16 + 16u * (uint64_t)tid; k < S->page_size; k += 16u * (uint64_t)nthr)
+        *(uint4*)(d + k) = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    if (tid == 0) {
+        if (len) st_rlx(&S->frames[r].content, (uint32_t)len);
+        publish_valid(S, r);
+    }
+    __syncthreads();
+}
+
 __device__ __noinline__ void* blk_mmap(gfs_state* S, int fd, uint64_t off, uint64_t size) {
     __shared__ int s_r;
     __shared__ bool s_fresh;
+    __shared__ MapFill s_fill;
     const int tid = blk_tid(), nthr = blk_nthr();
     __syncthreads();
     if (tid == 0) {
         bool fr;
-        s_r = map_pin(S, fd, off, size, &fr, 1);
+        s_r = map_pin(S, fd, off, size, &fr, 1, &s_fill);
         s_fresh = fr;
     }
     __syncthreads();
     int r = s_r;
     if (r < 0) return (void*)-1; /* GMAP_FAILED */
-    if (s_fresh) {
+    if (s_fresh && s_fill.len) {
+        /* a missed page of a mapped file: the block copies it from the
+         * mapping */
+        blk_fill_fresh(S, &s_r, s_fill);
+    } else if (s_fresh) {
         const int warp = tid >> 5, lane = tid & 31, nwarps = (nthr + 31) >> 5;
         const int gsize = (warp == nwarps - 1) ? (nthr - 32 * warp) : 32;
         uint64_t chunk = ((uint64_t)S->page_size / (uint64_t)nwarps + 15u) & ~15ull;
@@ -544,8 +592,8 @@ __device__ __noinline__ int blk_flush(gfs_state* S, int fd) {
         }
         const unsigned work = __ballot_sync(wmask, fr >= 0);
         if (!work) break;
-        const int slot = fr >= 0 ? wstage_claim(S, (uint32_t)fr) : -1;
-        uint32_t content = fr >= 0 ? ld_rlx(&S->frames[fr].content) : 0u;
+        const uint32_t content = fr >= 0 ? ld_rlx(&S->frames[fr].content) : 0u;
+        const int slot = fr >= 0 ? wstage_claim(S, (uint32_t)fr, content) : -1;
         /* the warp copies each staged lane's frame into its slot */
         for (unsigned m = __ballot_sync(wmask, slot >= 0); m; m &= m - 1u) {
             const int l = __ffs(m) - 1;

@@ -68,17 +68,31 @@ __device__ volatile void* gmmap_warp(void* addr, size_t size, int prot, int flag
     const int leader = __ffs(mask) - 1;
     int r = 0;
     bool fresh = false;
-    if (lane == leader) r = map_pin(S, fd, (uint64_t)offset, size, &fresh, ref < 1 ? 1 : ref);
+    MapFill mf = {};
+    if (lane == leader) r = map_pin(S, fd, (uint64_t)offset, size, &fresh, ref < 1 ? 1 : ref, &mf);
     r = __shfl_sync(mask, r, leader);
     int fz = __shfl_sync(mask, (int)fresh, leader);
     if (r < 0) return (volatile void*)-1;
     if (fz) {
+        /* a missed page of a mapped file is copied from the mapping by the
+         * warp (no host request); any other fresh page is zeroed */
+        const uint64_t len = __shfl_sync(mask, mf.len, leader);
+        const uint64_t src = __shfl_sync(mask, mf.map + ((uint64_t)mf.blk << S->log_page), leader);
         int rank = __popc(mask & ((1u << lane) - 1u)), cnt = __popc(mask);
         uint8_t* d = frame_data(S, (uint32_t)r);
-        for (uint32_t k = (uint32_t)rank * 16u; k < S->page_size; k += (uint32_t)cnt * 16u)
+        const uint32_t n16 = (uint32_t)(len >> 4);
+        for (uint32_t k = (uint32_t)rank; k < n16; k += (uint32_t)cnt)
+            ((uint4*)d)[k] = ((const uint4*)(uintptr_t)src)[k];
+        const uint32_t l16 = ((uint32_t)len + 15u) & ~15u;
+        for (uint32_t k = n16 * 16u + (uint32_t)rank; k < l16; k += (uint32_t)cnt)
+            d[k] = k < (uint32_t)len ? ((const uint8_t*)(uintptr_t)src)[k] : (uint8_t)0;
+        for (uint32_t k = l16 + (uint32_t)rank * 16u; k < S->page_size; k += (uint32_t)cnt * 16u)
             *(uint4*)(d + k) = make_uint4(0, 0, 0, 0);
         __syncwarp(mask);
-        if (lane == leader) publish_valid(S, (uint32_t)r);
+        if (lane == leader) {
+            if (len) st_rlx(&S->frames[r].content, (uint32_t)len);
+            publish_valid(S, (uint32_t)r);
+        }
         __syncwarp(mask);
     }
     return (volatile void*)(frame_data(S, (uint32_t)r) + ((uint64_t)offset & (S->page_size - 1u)));

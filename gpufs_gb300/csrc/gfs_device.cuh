@@ -612,15 +612,17 @@ __device__ __forceinline__ void publish_valid(gfs_state* S, uint32_t fr) {
     atomicAdd(&S->frames[fr].st, (GFS_FS_VALID - GFS_FS_LOADING) << GFS_F_SHIFT);
 }
 
-/* Largest page the SMs stage for write-back themselves (a warp copies a
- * page into a write-stage slot); larger pages are copied by the host. */
-#define GFS_WSTAGE_MAX_PAGE (256u << 10)
+/* Most valid bytes of a frame the SMs stage for write-back themselves (one
+ * warp copies them into a write-stage slot); fuller frames are copied by the
+ * host's copy engine, which moves a large page faster than one warp. */
+#define GFS_WSTAGE_MAX_BYTES (256u << 10)
 
-/* A free write-stage slot, or -1 when none is free (the caller then has the
+/* A free write-stage slot for a frame of `content` valid bytes, or -1 when
+ * the frame is too full to stage or no slot is free (the caller then has the
  * host copy the frame).  The bitmap's words are scanned once from a word
  * chosen by `hint`, so concurrent claimers start apart. */
-__device__ __forceinline__ int wstage_claim(gfs_state* S, uint32_t hint) {
-    if (S->page_size > GFS_WSTAGE_MAX_PAGE || !S->wstage || !S->wstage_slots) return -1;
+__device__ __forceinline__ int wstage_claim(gfs_state* S, uint32_t hint, uint32_t content) {
+    if (content > GFS_WSTAGE_MAX_BYTES || !S->wstage || !S->wstage_slots) return -1;
     const uint32_t nw = (S->wstage_slots + 31u) >> 5;
     for (uint32_t t = 0; t < nw; t++) {
         const uint32_t wi = (hint + t) % nw;

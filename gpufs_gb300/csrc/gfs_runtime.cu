@@ -1054,11 +1054,12 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
         s.wstage = nullptr;
         s.wstage_bits = nullptr;
         s.wstage_slots = 0;
-        if (page <= (256u << 10)) {
-            /* write-back staging for pages the SMs stage themselves: 64 MiB
-             * of host memory, at most 1024 pages */
+        {
+            /* write-back staging for frames the SMs stage themselves (at
+             * most 256 KiB of valid bytes each): 64 MiB of host memory in
+             * page-sized slots, 32 to 1024 of them */
             uint64_t slots = (64ull << 20) / page;
-            slots = slots > 1024 ? 1024 : slots;
+            slots = slots > 1024 ? 1024 : (slots < 32 ? 32 : slots);
             c->wstage_bytes = (size_t)slots * page;
             CK(cudaHostAlloc((void**)&c->wstage_h, c->wstage_bytes, cudaHostAllocMapped | cudaHostAllocPortable));
             CK(cudaHostGetDevicePointer((void**)&s.wstage, c->wstage_h, 0));

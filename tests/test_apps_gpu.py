@@ -12,16 +12,24 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("rows,cols,log_page", [(512, 4096, 16), (300, 65536, 21), (97, 1000, 12), (64, 70000, 16)])
-def test_bigmatrix_matches_fp64(built, shm_dir, rows, cols, log_page):
+# (300, 65536, 21), (200, 1024, 16) and (2048, 2048, 16) take the lookahead
+# form (every group of eight rows inside one page; two groups per page in the
+# second; the third through a pool smaller than the matrix); the others go
+# row by row where rows cross pages
+@pytest.mark.parametrize("rows,cols,log_page,pool_mb", [(512, 4096, 16, 256), (300, 65536, 21, 256), (97, 1000, 12, 256),
+                                                        (64, 70000, 16, 256), (200, 1024, 16, 256),
+                                                        (2048, 2048, 16, 8)])
+def test_bigmatrix_matches_fp64(built, shm_dir, rows, cols, log_page, pool_mb):
     vp, mp, op = (os.path.join(shm_dir, n) for n in ("v.f32", "m.f32", "o.f32"))
     datagen.normal_f32(vp, cols, seed=3)
     datagen.normal_f32(mp, rows * cols, seed=4)
     with open(op, "wb") as f:
         f.write(b"\xff" * 1000)  # stale bytes: the sample truncates its output first
-    with g.Session(log_page=log_page, pool_bytes=256 << 20, timeout_s=20) as s:
+    with g.Session(log_page=log_page, pool_bytes=pool_mb << 20, timeout_s=20) as s:
         s.bigmatrix(vp, mp, op, nblocks=37, nthreads=256)
         assert s.last_error() == 0, s.error_report()
+        if pool_mb * (1 << 20) < rows * cols * 4:
+            assert s.stats()["evictions"] > 0
     A = np.fromfile(mp, dtype=np.float32).reshape(rows, cols)
     x = np.fromfile(vp, dtype=np.float32)
     y = np.fromfile(op, dtype=np.float32)

@@ -253,10 +253,10 @@ def test_stalled_host_times_out(built, shm_dir):
 def test_reads_use_registered_file_mapping(built, shm_dir):
     """Read-only opens get a registered mapping of the host file: gread's
     misses are filled by the reading block itself, with SM loads from the
-    mapping (no request to the host at all), and gmmap's single-thread misses
-    are copy-engine DMA from it (no pread); a rewritten file (new size/ctime)
-    is mapped afresh; with the mapping off every miss goes through pread
-    into staging."""
+    mapping (no request to the host at all), and so are gmmap's misses, by
+    the mapping block or warp; a rewritten file (new size/ctime) is mapped
+    afresh; with the mapping off every miss goes through pread into
+    staging."""
     p = os.path.join(shm_dir, "mapped.bin")
     want = _mk(p, 3 * (1 << 20) + 5, seed=20)
     with g.Session(log_page=16, pool_bytes=64 << 20, timeout_s=20) as s:
@@ -265,13 +265,15 @@ def test_reads_use_registered_file_mapping(built, shm_dir):
         st = s.stats()
         assert st["misses"] == (want.size + 65535) // 65536
         assert st["read_rpcs"] == 0 and st["host_reads"] == 0
-        # gmmap pins one page at a time by one thread: the host copies it
-        # from the mapping (kept across closes: still no pread)
-        s.drop_cache()
-        s.reset_stats()
-        assert np.array_equal(s.mmap_read(p, 0, want.size, nblocks=4), want)
-        st = s.stats()
-        assert st["host_reads"] > 0 and st["host_map_reads"] == st["host_reads"]
+        # gmmap (block-collective, then warp-collective): the mapping
+        # block or warp copies each missed page from the file's mapping
+        for warp_api in (False, True):
+            s.drop_cache()
+            s.reset_stats()
+            assert np.array_equal(s.mmap_read(p, 0, want.size, nblocks=4, warp_api=warp_api), want)
+            st = s.stats()
+            assert st["misses"] == (want.size + 65535) // 65536
+            assert st["read_rpcs"] == 0 and st["host_reads"] == 0
         time.sleep(0.01)
         want2 = _mk(p, 2 * (1 << 20) + 77, seed=21)
         assert np.array_equal(s.pread(p, 0, want2.size, nblocks=3), want2)
