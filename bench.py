@@ -947,6 +947,7 @@ def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
     t_open = time.perf_counter() - t0
     # saturation: a burst of requests all due at once
     burst = _served_trace(sizes, 30000, n_out, rng)
+    resident_warps = sv.warps_per_sm(32)  # asked 32; the device may hold fewer at once
     sv.run(burst[:2000], inflight_pages=budget, warps_per_sm=32)  # warm-up
     res = sv.run(burst, inflight_pages=budget, warps_per_sm=32)
     # saturation: the whole burst (long enough that its last large requests
@@ -1051,7 +1052,7 @@ def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
                                    "Zipf(0.9), lengths log-uniform 4 KiB-16 MiB, 80%% read+XXH64 / 15%% grep / 5%% "
                                    "write, 24 GiB buffer cache, memory-gated admission, open-loop Poisson arrivals at "
                                    "10-90%% of saturation" % (len(paths), total / 2 ** 30),
-                       "page_bytes": 1 << page_log, "warps_per_sm": 32, "admission_pages": budget,
+                       "page_bytes": 1 << page_log, "warps_per_sm": resident_warps, "admission_pages": budget,
                        "value_at": "90%% of saturation load, p99 %.0f us" % top["p99_us"]},
             "roofline": {"bound": "link", "achieved": top["gbs"], "peak": link[0] if link else None, "unit": "GB/s",
                          "frac": top["gbs"] / link[0] if link else None, "peak_source": "measured pinned H2D",

@@ -94,6 +94,7 @@ _SIGS = {
                               ctypes.POINTER(_c_p)]),
     "gfs_serve_run": (_int, [_c_p, _c_p, _int, _c_p, _u64, _int]),
     "gfs_serve_close": (_int, [_c_p]),
+    "gfs_serve_warps_per_sm": (_int, [_c_p, _int]),
     "gfs_grep_bench": (_int, [_c_p, _int, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "gfs_drop_cache": (_i64, [_c_p]),
     "gfs_retained_pages": (_i64, [_c_p]),
@@ -452,6 +453,11 @@ class Server:
                                       res.ctypes.data if reqs.size else None, int(inflight_pages), warps_per_sm),
                "gfs_serve_run")
         return res
+
+    def warps_per_sm(self, asked=32):
+        """Serving warps per SM a run asked for `asked` uses (whole blocks of
+        8, capped at what the device holds at once)."""
+        return _check(self.s.L.gfs_serve_warps_per_sm(self._h, asked), "gfs_serve_warps_per_sm")
 
     def close(self):
         if self._h:

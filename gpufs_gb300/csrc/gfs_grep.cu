@@ -1189,6 +1189,25 @@ struct SvComp { /* completion, indexed by request id: done is written last */
     int status;
     uint32_t done;
 };
+/* A large grep request is split into parts that any serving warp may take
+ * (a part is a run of the request's 512-byte segments); the request's
+ * accumulator collects the parts' counts and the part that finishes last
+ * publishes the completion. */
+struct SvAcc {
+    unsigned long long count;
+    uint32_t left; /* parts not finished */
+    int status;    /* the first part's error */
+};
+struct SvPart { /* a slot of the part queue (sequence protocol as the ring) */
+    uint32_t seq;
+    uint32_t id, file, unused;
+    uint64_t off, end;       /* the request's range */
+    uint64_t seg_lo, seg_hi; /* this part's segments: [seg_lo, seg_hi) in steps of 512 */
+};
+#define SV_QCAP 16384u          /* part queue slots (power of two) */
+#define SV_SPLIT (1ull << 20)   /* greps longer than this are split ... */
+#define SV_PART (256ull << 10)  /* ... into parts of about this many bytes ... */
+#define SV_MAXP 64u             /* ... and at most this many */
 struct ServeDev {
     GrepDev G;              /* the dictionary (table in global memory) */
     SvReq* ring;            /* device view of the mapped ring */
@@ -1200,6 +1219,10 @@ struct ServeDev {
     const int* out_fds;     /* output files (write-once) */
     int n_files, n_out;
     const uint32_t* stop;   /* mapped: set by the host when every request is done */
+    SvAcc* acc;             /* per request id (device memory, zeroed per run) */
+    SvPart* parts;          /* SV_QCAP slots */
+    uint32_t* q_head;       /* next part to take */
+    uint32_t* q_tail;       /* next part position to reserve */
 };
 #define SV_WARPS 8
 #define SV_STAGE (GR_LB + GR_SEG + GR_LA + 16)
@@ -1320,13 +1343,14 @@ __device__ int sv_read_xxh(gfs_state* S, const ServeDev& D, int fd, uint64_t off
 
 /* dictionary words among the tokens of [off, end), the range read as a
  * text of its own (bytes outside it are not letters), by one warp */
-__device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, uint64_t end, uint8_t* st,
-                       uint8_t* wscr, const uint4* km, unsigned long long* result) {
+__device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, uint64_t end, uint64_t seg_lo,
+                       uint64_t seg_hi, uint8_t* st, uint8_t* wscr, const uint4* km, unsigned long long* result) {
     const int lane = threadIdx.x & 31;
     const uint32_t lp = S->log_page, pmask = S->page_size - 1u;
     PageWindow win;
     win.pf = pin_file(S, fd);
-    win.last = end > off ? (uint32_t)((end - 1) >> lp) : 0u;
+    win.last = seg_hi > seg_lo ? (uint32_t)(((seg_hi + GR_SEG + GR_LA < end ? seg_hi + GR_SEG + GR_LA : end) - 1) >> lp)
+                               : 0u;
     Tbl t;
     t.tags = D.G.tags;
     t.disp = D.G.disp;
@@ -1334,9 +1358,12 @@ __device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, ui
     TotalSink sink;
     int err = 0;
     /* segments start 16-byte aligned in the file (the staged units are then
-     * aligned); bytes before off or from end on are staged as zeros, which
-     * are not letters, so the range reads as a text of its own */
-    for (uint64_t seg = off & ~15ull; seg < end; seg += GR_SEG) {
+     * aligned), at off & ~15 plus multiples of 512; this call scans those in
+     * [seg_lo, seg_hi).  Bytes before off or from end on are staged as
+     * zeros, which are not letters, so the range reads as a text of its own
+     * and a token is counted by the segment it starts in, whichever part
+     * that segment falls in. */
+    for (uint64_t seg = seg_lo; seg < seg_hi && seg < end; seg += GR_SEG) {
         /* stage [seg - 16, seg + 512 + 64) with bytes outside [off, end) zero */
         const uint64_t lo = seg >= off + GR_LB ? seg - GR_LB : off;
         const uint64_t hi = seg + GR_SEG + GR_LA < end ? seg + GR_SEG + GR_LA : end;
@@ -1433,11 +1460,148 @@ __device__ int sv_write(gfs_state* S, int fd, uint64_t off, uint64_t len, uint32
     return 0;
 }
 
+/* publish a request's completion (lane 0) */
+__device__ __forceinline__ void sv_complete(const ServeDev& D, uint32_t id, unsigned long long res, int status) {
+    SvComp* c = &D.comp[id];
+    asm volatile("st.relaxed.sys.global.u64 [%0], %1;" ::"l"(&c->result), "l"(res) : "memory");
+    asm volatile("st.relaxed.sys.global.u32 [%0], %1;" ::"l"(&c->status), "r"((uint32_t)status) : "memory");
+    st_rel_sys(&c->done, 1u);
+}
+
+/* lane 0: one part of a split request is done; the part that finishes last
+ * publishes the request's completion with the summed count */
+__device__ void sv_part_done(const ServeDev& D, uint32_t id, unsigned long long n, int status) {
+    SvAcc* a = &D.acc[id];
+    if (status) atomicCAS(&a->status, 0, status);
+    atomicAdd(&a->count, n);
+    __threadfence();
+    if (atomicSub(&a->left, 1u) == 1u) {
+        __threadfence();
+        const unsigned long long total = atomicAdd(&a->count, 0ull);
+        const int st = atomicAdd(&a->status, 0);
+        sv_complete(D, id, st ? 0ull : total, st);
+    }
+}
+
+/* lane 0: take a queued part if there is one (true: *pt holds it) */
+__device__ bool sv_take_part(const ServeDev& D, const gfs_state* S, SvPart* pt) {
+    for (;;) {
+        const uint32_t h = ld_rlx(D.q_head);
+        if ((int32_t)(ld_rlx(D.q_tail) - h) <= 0) return false;
+        if (atomicCAS(D.q_head, h, h + 1u) != h) continue;
+        SvPart* q = &D.parts[h & (SV_QCAP - 1u)];
+        /* the producer reserved the position before writing it: wait the
+         * few instructions until it is there (bounded all the same) */
+        Waiter w(S->timeout_ns);
+        while (ld_acq(&q->seq) != h + 1u)
+            if (!w.tick(256)) return false;
+        *pt = *q;
+        __threadfence();
+        st_rel(&q->seq, h + SV_QCAP);
+        return true;
+    }
+}
+
+/* lane 0: reserve n consecutive part positions if the queue has room for
+ * them (else false: the request is served whole) */
+__device__ bool sv_reserve_parts(const ServeDev& D, uint32_t n, uint32_t* pos) {
+    for (;;) {
+        const uint32_t t = ld_rlx(D.q_tail);
+        if (t + n - ld_rlx(D.q_head) > SV_QCAP) return false;
+        if (atomicCAS(D.q_tail, t, t + n) == t) {
+            *pos = t;
+            return true;
+        }
+    }
+}
+
+/* One queued part of a split grep (the whole warp; pt valid in lane 0). */
+__device__ __noinline__ void sv_serve_part(gfs_state* S, const ServeDev& D, const SvPart& pt, uint8_t* st,
+                                           uint8_t* wscr, const uint4* kmask) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t id = __shfl_sync(0xFFFFFFFFu, pt.id, 0), file = __shfl_sync(0xFFFFFFFFu, pt.file, 0);
+    const uint64_t o = __shfl_sync(0xFFFFFFFFu, pt.off, 0), e = __shfl_sync(0xFFFFFFFFu, pt.end, 0);
+    const uint64_t lo = __shfl_sync(0xFFFFFFFFu, pt.seg_lo, 0), hi = __shfl_sync(0xFFFFFFFFu, pt.seg_hi, 0);
+    unsigned long long n = 0;
+    const int stt = sv_grep(S, D, D.fds[file], o, e, lo, hi, st, wscr, kmask, &n);
+    if (lane == 0) sv_part_done(D, id, n, stt);
+    __syncwarp();
+}
+
+/* A grep request (the whole warp): served whole, or -- longer than SV_SPLIT
+ * -- split into parts, all but the first queued for any warp to take.
+ * Returns true when split (the completion then comes from the part that
+ * finishes last); false with *res and *status set otherwise. */
+__device__ __noinline__ bool sv_grep_request(gfs_state* S, const ServeDev& D, uint32_t file, uint32_t id, uint64_t o,
+                                             uint64_t e, uint8_t* st, uint8_t* wscr, const uint4* kmask,
+                                             unsigned long long* res, int* status) {
+    const int lane = threadIdx.x & 31;
+    bool split = false;
+    const uint64_t s0 = o & ~15ull, nseg = (e - s0 + GR_SEG - 1) / GR_SEG;
+    uint32_t np = 1;
+    if (e - o > SV_SPLIT) {
+        const uint64_t want = (e - o + SV_PART - 1) / SV_PART;
+        np = (uint32_t)(want < SV_MAXP ? want : SV_MAXP);
+    }
+    uint32_t pos = 0;
+    if (np > 1) {
+        /* the accumulator first, then the queued parts 1..np-1 */
+        bool ok = false;
+        if (lane == 0) {
+            atomicExch(&D.acc[id].count, 0ull);
+            atomicExch(&D.acc[id].status, 0);
+            atomicExch(&D.acc[id].left, np);
+            __threadfence();
+            ok = sv_reserve_parts(D, np - 1u, &pos);
+        }
+        ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
+        pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
+        if (!ok) np = 1;
+    }
+    if (np > 1) {
+        split = true;
+        for (uint32_t k = 1u + (uint32_t)lane; k < np; k += 32u) {
+            SvPart* q = &D.parts[(pos + k - 1u) & (SV_QCAP - 1u)];
+            /* the slot is free once its last taker has copied it out (it
+             * took the position before the reservation, which left room
+             * for these): a few instructions */
+            Waiter w(S->timeout_ns);
+            bool freed = true;
+            while (ld_acq(&q->seq) != pos + k - 1u)
+                if (!w.tick(256)) { freed = false; break; }
+            if (!freed) {
+                /* never seen: the part is counted as failed */
+                sv_part_done(D, id, 0ull, -GFS_ETIMEDOUT);
+                continue;
+            }
+            q->id = id;
+            q->file = file;
+            q->off = o;
+            q->end = e;
+            q->seg_lo = s0 + GR_SEG * (nseg * k / np);
+            q->seg_hi = s0 + GR_SEG * (nseg * (k + 1u) / np);
+            __threadfence();
+            st_rel(&q->seq, pos + k);
+        }
+        __syncwarp();
+        unsigned long long n0 = 0;
+        const int st0 = sv_grep(S, D, D.fds[file], o, e, s0, s0 + GR_SEG * (nseg / np), st, wscr, kmask, &n0);
+        if (lane == 0) sv_part_done(D, id, n0, st0);
+        __syncwarp();
+    } else {
+        *status = sv_grep(S, D, D.fds[file], o, e, s0, e, st, wscr, kmask, res);
+    }
+    return split;
+}
+
 } // namespace
 
 /* Served loop: each warp takes the next ticket, waits (bounded by the
  * session timeout, or until the host sets stop) for that request, frees
- * its ring slot, serves it and publishes the completion. */
+ * its ring slot, serves it and publishes the completion.  A grep longer
+ * than SV_SPLIT is split: its warp queues all but the first part, serves
+ * the first, and the rest are taken by warps between requests (a warp
+ * waiting for its next request serves queued parts meanwhile). */
 __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev D) {
     __shared__ __align__(16) uint8_t stage[SV_WARPS][SV_STAGE];
     __shared__ __align__(16) uint8_t rawb[SV_WARPS][33 * 16 + 16]; /* read requests' aligned units */
@@ -1460,25 +1624,35 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev 
         SvReq* slot = &D.ring[t & D.ring_mask];
         uint32_t have = 0;
         uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
-        if (lane == 0) {
-            const uint64_t t0 = gtimer();
-            uint32_t ns = 64, k = 0;
-            for (;;) {
-                if (ld_acq_sys(&slot->seq) == t + 1u) { have = 1; break; }
-                if (ld_rlx_sys(D.stop)) break;
-                if ((++k & 63u) == 0u && gtimer() - t0 > S->timeout_ns) break; /* idle too long: leave */
-                __nanosleep(ns);
-                if (ns < 2048) ns <<= 1;
+        for (;;) {
+            /* lane 0 waits for the ticket's request; a queued part found
+             * meanwhile is served by the warp (have = 2), then the wait
+             * goes on (the idle limit counts from the last work done) */
+            SvPart pt;
+            if (lane == 0) {
+                have = 0;
+                const uint64_t t0 = gtimer();
+                uint32_t ns = 64, k = 0;
+                for (;;) {
+                    if (ld_acq_sys(&slot->seq) == t + 1u) { have = 1; break; }
+                    if (sv_take_part(D, S, &pt)) { have = 2; break; }
+                    if (ld_rlx_sys(D.stop)) break;
+                    if ((++k & 63u) == 0u && gtimer() - t0 > S->timeout_ns) break; /* idle too long: leave */
+                    __nanosleep(ns);
+                    if (ns < 2048) ns <<= 1;
+                }
+                if (have == 1) {
+                    asm volatile("ld.relaxed.sys.global.v4.u32 {%0,%1,%2,%3}, [%4];"
+                                 : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w) : "l"(slot) : "memory");
+                    asm volatile("ld.relaxed.sys.global.v4.u32 {%0,%1,%2,%3}, [%4];"
+                                 : "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w) : "l"((const uint8_t*)slot + 16) : "memory");
+                    st_rel_sys(&slot->seq, t + D.ring_mask + 1u); /* the slot is free for the host again */
+                }
             }
-            if (have) {
-                asm volatile("ld.relaxed.sys.global.v4.u32 {%0,%1,%2,%3}, [%4];"
-                             : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w) : "l"(slot) : "memory");
-                asm volatile("ld.relaxed.sys.global.v4.u32 {%0,%1,%2,%3}, [%4];"
-                             : "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w) : "l"((const uint8_t*)slot + 16) : "memory");
-                st_rel_sys(&slot->seq, t + D.ring_mask + 1u); /* the slot is free for the host again */
-            }
+            have = __shfl_sync(0xFFFFFFFFu, have, 0);
+            if (have != 2) break;
+            sv_serve_part(S, D, pt, stage[warp], wscr[warp], kmask);
         }
-        have = __shfl_sync(0xFFFFFFFFu, have, 0);
         if (!have) return;
         const uint32_t op = __shfl_sync(0xFFFFFFFFu, a.y, 0), file = __shfl_sync(0xFFFFFFFFu, a.z, 0),
                        id = __shfl_sync(0xFFFFFFFFu, a.w, 0);
@@ -1486,6 +1660,7 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev 
         const uint64_t len = ((uint64_t)__shfl_sync(0xFFFFFFFFu, b.w, 0) << 32) | __shfl_sync(0xFFFFFFFFu, b.z, 0);
         unsigned long long res = 0;
         int status = 0;
+        bool split = false;
         if (op == GFS_SV_WRITE && (off & 15u)) {
             status = -GFS_EINVAL; /* written ranges start 16-byte aligned (vector stores) */
         } else if (op == GFS_SV_WRITE) {
@@ -1493,17 +1668,15 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev 
         } else if ((int)file < D.n_files && (op == GFS_SV_READ || op == GFS_SV_GREP)) {
             const uint64_t size = D.sizes[file];
             const uint64_t o = off < size ? off : size, e = len < size - o ? o + len : size;
-            if (op == GFS_SV_READ) status = sv_read_xxh(S, D, D.fds[file], o, e, stage[warp], rawb[warp], &res);
-            else status = sv_grep(S, D, D.fds[file], o, e, stage[warp], wscr[warp], kmask, &res);
+            if (op == GFS_SV_READ) {
+                status = sv_read_xxh(S, D, D.fds[file], o, e, stage[warp], rawb[warp], &res);
+            } else {
+                split = sv_grep_request(S, D, file, id, o, e, stage[warp], wscr[warp], kmask, &res, &status);
+            }
         } else {
             status = -GFS_EINVAL;
         }
-        if (lane == 0) {
-            SvComp* c = &D.comp[id];
-            asm volatile("st.relaxed.sys.global.u64 [%0], %1;" ::"l"(&c->result), "l"(res) : "memory");
-            asm volatile("st.relaxed.sys.global.u32 [%0], %1;" ::"l"(&c->status), "r"((uint32_t)status) : "memory");
-            st_rel_sys(&c->done, 1u);
-        }
+        if (lane == 0 && !split) sv_complete(D, id, res, status);
         __syncwarp();
     }
 }
@@ -2550,6 +2723,7 @@ struct gfs_server {
     uint64_t* sizes = nullptr;
     int* out_fds = nullptr;
     uint32_t* head = nullptr;
+    SvPart* parts = nullptr;  /* part queue of split greps */
     SvReq* ring_h = nullptr;  /* mapped */
     SvReq* ring_d = nullptr;
     uint32_t ring_n = 0;
@@ -2558,6 +2732,13 @@ struct gfs_server {
     int sms = 0;
     std::vector<uint64_t> host_sizes;
 };
+
+/* part queue of a run: slot i free for position i, head = tail = 0 */
+static __global__ void k_sv_reset(SvPart* parts, uint32_t* qht) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < SV_QCAP) parts[i].seq = i;
+    if (i < 2u) qht[i] = 0u;
+}
 
 static uint64_t now_ns() {
     struct timespec ts;
@@ -2586,13 +2767,15 @@ int gfs_serve_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths
     const size_t n_all = (size_t)n_files + (size_t)n_out;
     size_t o_fds = 0, o_sz = align_up(o_fds + (size_t)n_files * 4, 256), o_ofd = align_up(o_sz + (size_t)n_files * 8, 256),
            o_osz = align_up(o_ofd + (size_t)n_out * 4 + 4, 256), o_head = align_up(o_osz + (size_t)n_out * 8 + 8, 256),
-           o_names = align_up(o_head + 64, 256), total = align_up(o_names + n_all * GFS_NAME_MAX, 256);
+           o_parts = align_up(o_head + 64, 256), o_names = align_up(o_parts + (size_t)SV_QCAP * sizeof(SvPart), 256),
+           total = align_up(o_names + n_all * GFS_NAME_MAX, 256);
     if (cudaMalloc(&sv->dmem, total) != cudaSuccess) { gfs_serve_close(sv); return -GFS_ENOMEM; }
     cudaMemset(sv->dmem, 0, total);
     sv->fds = (int*)(sv->dmem + o_fds);
     sv->sizes = (uint64_t*)(sv->dmem + o_sz);
     sv->out_fds = (int*)(sv->dmem + o_ofd);
-    sv->head = (uint32_t*)(sv->dmem + o_head);
+    sv->head = (uint32_t*)(sv->dmem + o_head); /* ticket counter, then the part queue's head and tail */
+    sv->parts = (SvPart*)(sv->dmem + o_parts);
     {
         std::vector<char> names(n_all * GFS_NAME_MAX, 0);
         for (int i = 0; i < n_files; i++) memcpy(&names[(size_t)i * GFS_NAME_MAX], paths[i], strlen(paths[i]));
@@ -2633,6 +2816,22 @@ int gfs_serve_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths
  * once the pages of the requests in flight leave room for it under
  * inflight_pages (memory-gated admission); latencies are completion minus
  * arrival, host clock.  warps_per_sm: serving warps per SM (multiple of 8). */
+/* as many blocks as are resident at once: a queued block of this persistent
+ * kernel would only start when others leave */
+int gfs_serve_warps_per_sm(gfs_server* sv, int warps_per_sm) {
+    if (!sv) return -GFS_EINVAL;
+    if (gfs__activate(sv->ctx)) return -GFS_EIO;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_serve, SV_WARPS * 32, 0) != cudaSuccess) {
+        cudaGetLastError();
+        per_sm = 0; /* unknown: no cap */
+    }
+    int bps = warps_per_sm / SV_WARPS;
+    if (bps < 1) bps = 1;
+    if (per_sm > 0 && bps > per_sm) bps = per_sm;
+    return bps * SV_WARPS;
+}
+
 int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_res* res, uint64_t inflight_pages,
                   int warps_per_sm) {
     if (!sv || n < 0 || (n && (!reqs || !res))) return -GFS_EINVAL;
@@ -2648,6 +2847,11 @@ int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_re
     for (uint32_t i = 0; i < sv->ring_n; i++) __atomic_store_n(&sv->ring_h[i].seq, i, __ATOMIC_RELAXED);
     __atomic_store_n(sv->stop_h, 0u, __ATOMIC_RELEASE);
     cudaMemsetAsync(sv->head, 0, 4, s);
+    /* split greps: an accumulator per request id, the part queue reset */
+    SvAcc* acc = (SvAcc*)gfs__dev_alloc(sv->ctx, (size_t)(n ? n : 1) * sizeof(SvAcc), s);
+    if (!acc) { cudaFreeHost(comp_h); return -GFS_ENOMEM; }
+    cudaMemsetAsync(acc, 0, (size_t)(n ? n : 1) * sizeof(SvAcc), s);
+    k_sv_reset<<<(SV_QCAP + 255u) / 256u, 256, 0, s>>>(sv->parts, sv->head + 1);
     ServeDev D{};
     D.G = sv->dict->dev;
     D.ring = sv->ring_d;
@@ -2660,10 +2864,18 @@ int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_re
     D.n_files = sv->n_files;
     D.n_out = sv->n_out;
     D.stop = sv->stop_d;
+    D.acc = acc;
+    D.parts = sv->parts;
+    D.q_head = sv->head + 1;
+    D.q_tail = sv->head + 2;
     const uint32_t page = gfs_page_size(sv->ctx);
-    const int blocks = sv->sms * (warps_per_sm / SV_WARPS);
+    const int blocks = sv->sms * (gfs_serve_warps_per_sm(sv, warps_per_sm) / SV_WARPS);
     k_serve<<<blocks, SV_WARPS * 32, 0, s>>>((gfs_state*)gfs_device_state(sv->ctx), D);
-    if (cudaGetLastError() != cudaSuccess) { cudaFreeHost(comp_h); return -GFS_EIO; }
+    if (cudaGetLastError() != cudaSuccess) {
+        gfs__dev_free(sv->ctx, acc, s);
+        cudaFreeHost(comp_h);
+        return -GFS_EIO;
+    }
     std::vector<uint32_t> cost((size_t)n);
     for (int k = 0; k < n; k++) cost[(size_t)k] = (uint32_t)((reqs[k].length + page - 1) / page) + 1u;
     std::atomic<uint64_t> inflight{0};
@@ -2728,6 +2940,7 @@ int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_re
     __atomic_store_n(sv->stop_h, 1u, __ATOMIC_RELEASE);
     cudaError_t e = cudaStreamSynchronize(s);
     poller.join();
+    gfs__dev_free(sv->ctx, acc, s);
     cudaFreeHost(comp_h);
     if (e != cudaSuccess) return -GFS_EIO;
     return rc;

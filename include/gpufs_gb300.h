@@ -251,9 +251,14 @@ typedef struct gfs_server gfs_server;
 int gfs_serve_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths, int n_files,
                    const char* const* out_paths, int n_out, gfs_server** out);
 /* one open-loop run over requests sorted by arrival; inflight_pages bounds the
- * pages of admitted, unfinished requests (memory-gated admission) */
+ * pages of admitted, unfinished requests (memory-gated admission);
+ * warps_per_sm: serving warps per SM asked for, rounded down to whole blocks
+ * of 8 and capped at what the device holds at once (gfs_serve_warps_per_sm).
+ * Greps longer than 1 MiB are split into parts that idle serving warps take. */
 int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_res* res, uint64_t inflight_pages,
                   int warps_per_sm);
+/* the serving warps per SM a run asked for `warps_per_sm` uses */
+int gfs_serve_warps_per_sm(gfs_server* sv, int warps_per_sm);
 /* closes every file (dirty output pages are written back) */
 int gfs_serve_close(gfs_server* sv);
 

@@ -123,3 +123,39 @@ def test_served_any_offset(built, shm_dir):
             res = sv.run(reqs)
     assert res[63]["status"] == -errno.EINVAL
     _check(res[:63], reqs[:63], paths, raw_dict, first_idx)
+
+
+@pytest.mark.parametrize("pool_mb", [64, 8])
+def test_served_split_greps(built, shm_dir, pool_mb):
+    """Greps longer than 1 MiB are split into parts that other warps take
+    (a token is counted by the part its first letter falls in); many at once,
+    at any offset, up to the end of the file, with and without eviction,
+    mixed with reads: every count equals the oracle's."""
+    paths, dpath, outs, rng = _setup(shm_dir, seed=70)
+    raw_dict, first_idx = _dict_words(dpath)
+    sizes = [os.path.getsize(p) for p in paths]
+    reqs = np.zeros(48, dtype=g.SERVE_REQ)
+    for k in range(48):
+        f = [5, 6, 7][k % 3]
+        off = int(rng.integers(0, sizes[f] // 3))
+        length = int(rng.integers((1 << 20) + 1, 5 << 20))
+        if k % 8 == 7:
+            length = sizes[f]  # runs to the end of the file
+        reqs[k] = (g.SV_GREP if k % 4 else g.SV_READ, f, off, length, 0)
+    with g.Session(log_page=16, pool_bytes=pool_mb << 20, max_files=64, timeout_s=30) as s:
+        with g.Server(s, dpath, paths, outs) as sv:
+            res = sv.run(reqs, inflight_pages=(pool_mb << 20) // (2 << 16))
+        assert s.last_error() == 0
+    _check(res, reqs, paths, raw_dict, first_idx)
+
+
+def test_serving_warps_are_resident(built, shm_dir):
+    """A run uses whole blocks of 8 serving warps per SM, no more than the
+    device holds at once (a persistent block that is not resident would
+    serve nothing until others leave)."""
+    paths, dpath, outs, _ = _setup(shm_dir, seed=90)
+    with g.Session(log_page=16, pool_bytes=32 << 20, max_files=64, timeout_s=30) as s:
+        with g.Server(s, dpath, paths, outs) as sv:
+            got = [sv.warps_per_sm(w) for w in (1, 8, 16, 24, 32, 64)]
+    assert all(w % 8 == 0 and 8 <= w <= max(8, asked) for w, asked in zip(got, (1, 8, 16, 24, 32, 64)))
+    assert got == sorted(got) and got[1] == 8 and got[-1] < 64
