@@ -41,6 +41,7 @@
 #include <unistd.h>
 #include <sched.h>
 #include <time.h>
+#include <sys/mman.h>
 #include <sys/stat.h>
 
 #include <algorithm>
@@ -2449,6 +2450,11 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     return 0;
 }
 
+#ifdef MADV_POPULATE_WRITE
+#define GFS_MADV_POPULATE_WRITE MADV_POPULATE_WRITE
+#else
+#define GFS_MADV_POPULATE_WRITE 23 /* Linux 5.14 */
+#endif
 static bool counts_out_ok(gfs_grep* g, size_t bytes);
 static void counts_out(gfs_grep* g, uint32_t* host_counts, size_t bytes, cudaStream_t s);
 
@@ -2517,6 +2523,16 @@ static bool counts_out_ok(gfs_grep* g, size_t bytes) {
     return bytes > 0 && bytes <= ((size_t)16 << 20) && gfs__pageable_access(g->ctx);
 }
 static void counts_out(gfs_grep* g, uint32_t* host_counts, size_t bytes, cudaStream_t s) {
+    /* Fault the caller's pages in first, as a host write would, without
+     * touching their bytes: a fresh buffer's first write from the device
+     * otherwise takes a page fault per page through the host's page tables
+     * (measured 0.65 ms for 2.56 MB, against 0.02 ms once the pages exist).
+     * Kernels without this call still work, only slower. */
+    {
+        const uintptr_t pg = (uintptr_t)sysconf(_SC_PAGESIZE);
+        const uintptr_t a = (uintptr_t)host_counts & ~(pg - 1u), e = ((uintptr_t)host_counts + bytes + pg - 1u) & ~(pg - 1u);
+        madvise((void*)a, e - a, GFS_MADV_POPULATE_WRITE);
+    }
     const size_t n = bytes / 4u;
     size_t blocks = (n / 4u + 255u) / 256u;
     const size_t cap = (size_t)(g->sms > 0 ? g->sms : 1) * 4u;
