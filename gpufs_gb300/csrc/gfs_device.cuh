@@ -258,8 +258,11 @@ __device__ __forceinline__ bool host_stalled(gfs_state* S) {
  * non-negative result (bytes moved, or 0) or -errno / -GFS_ETIMEDOUT. */
 __device__ __noinline__ int rpc_call(gfs_state* S, const Req& r, uint32_t* done) {
     if (host_stalled(S)) return -GFS_ETIMEDOUT;
+    /* the completion word is cleared before the request is published: the
+     * release store of the sequence word below orders both this store and
+     * the request's fields before it at system scope, so no separate fence
+     * is needed (each costs a round trip to host memory) */
     st_rlx_sys(done, 0u);
-    __threadfence_system();
     Waiter w(S->timeout_ns);
     /* the lanes of a warp that call together (a lane-per-page miss burst)
      * take consecutive ring tickets with one atomic by their leader */
@@ -295,7 +298,6 @@ __device__ __noinline__ int rpc_call(gfs_state* S, const Req& r, uint32_t* done)
             ((volatile uint32_t*)vs->name)[i / 4] = v;
         }
     }
-    __threadfence_system();
     st_rel_sys(&slot->seq, t + 1u);
     count(S, &S->stats.rpc_submitted);
     uint32_t c;
