@@ -1224,6 +1224,8 @@ struct ServeDev {
     SvPart* parts;          /* SV_QCAP slots */
     uint32_t* q_head;       /* next part to take */
     uint32_t* q_tail;       /* next part position to reserve */
+    uint32_t tbl_smem;      /* bytes of slot tags + displacements staged in each block's
+                               dynamic shared memory (0: read from global memory) */
 };
 #define SV_WARPS 8
 #define SV_STAGE (GR_LB + GR_SEG + GR_LA + 16)
@@ -1352,9 +1354,12 @@ __device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, ui
     win.pf = pin_file(S, fd);
     win.last = seg_hi > seg_lo ? (uint32_t)(((seg_hi + GR_SEG + GR_LA < end ? seg_hi + GR_SEG + GR_LA : end) - 1) >> lp)
                                : 0u;
+    /* the table's tags and displacements from the block's shared copy when
+     * there is one (generic loads serve either place) */
+    extern __shared__ __align__(128) uint8_t sv_dsm[];
     Tbl t;
-    t.tags = D.G.tags;
-    t.disp = D.G.disp;
+    t.tags = D.tbl_smem ? (const uint16_t*)sv_dsm : D.G.tags;
+    t.disp = D.tbl_smem ? (const uint16_t*)(sv_dsm + grep_tag_smem(D.G.m)) : D.G.disp;
     t.cnt = nullptr;
     TotalSink sink;
     int err = 0;
@@ -1401,7 +1406,7 @@ __device__ int sv_grep(gfs_state* S, const ServeDev& D, int fd, uint64_t off, ui
         d.fseq = 0;
         d.clen = end - seg < GR_SEG ? (uint32_t)(end - seg) : (uint32_t)GR_SEG;
         d.avail = end - seg < GR_SEG + GR_LA ? (uint32_t)(end - seg) : (uint32_t)(GR_SEG + GR_LA);
-        scan_segment<false>(D.G, t, st + GR_LB, d, 0u, wscr, km, sink);
+        scan_segment<true>(D.G, t, st + GR_LB, d, 0u, wscr, km, sink);
         __syncwarp();
     }
     win.release(S);
@@ -1608,6 +1613,7 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev 
     __shared__ __align__(16) uint8_t rawb[SV_WARPS][33 * 16 + 16]; /* read requests' aligned units */
     __shared__ __align__(16) uint8_t wscr[SV_WARPS][GR_WSCR];
     __shared__ uint4 kmask[17];
+    extern __shared__ __align__(128) uint8_t sv_dsm[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x <= 16u) {
         uint32_t mw[4];
@@ -1616,6 +1622,16 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev 
             mw[i] = b >= 32 ? 0xFFFFFFFFu : (b <= 0 ? 0u : (1u << b) - 1u);
         }
         kmask[threadIdx.x] = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+    }
+    /* the dictionary's slot tags and displacements into shared memory (the
+     * plan's global copies are zero padded to these sizes): the grep path's
+     * two table loads per token then cost a shared-memory access */
+    if (D.tbl_smem) {
+        const uint32_t tb = grep_tag_smem(D.G.m), db = grep_disp_smem(D.G.r);
+        for (uint32_t i = threadIdx.x; i < tb / 16u; i += blockDim.x)
+            ((uint4*)sv_dsm)[i] = __ldg((const uint4*)D.G.tags + i);
+        for (uint32_t i = threadIdx.x; i < db / 16u; i += blockDim.x)
+            ((uint4*)(sv_dsm + tb))[i] = __ldg((const uint4*)D.G.disp + i);
     }
     __syncthreads();
     for (;;) {
@@ -2834,11 +2850,30 @@ int gfs_serve_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths
  * arrival, host clock.  warps_per_sm: serving warps per SM (multiple of 8). */
 /* as many blocks as are resident at once: a queued block of this persistent
  * kernel would only start when others leave */
+/* shared memory a served block stages the dictionary's tags and
+ * displacements in (0 when they do not fit: the grep path then reads them
+ * from global memory); the kernel attribute is raised to match */
+static uint32_t serve_tbl_smem(gfs_server* sv) {
+    const GrepDev& G = sv->dict->dev;
+    const uint32_t bytes = grep_tag_smem(G.m) + grep_disp_smem(G.r);
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, k_serve) != cudaSuccess) return 0;
+    if ((size_t)bytes + a.sharedSizeBytes > (size_t)optin) return 0;
+    if (cudaFuncSetAttribute(k_serve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return bytes;
+}
+
 int gfs_serve_warps_per_sm(gfs_server* sv, int warps_per_sm) {
     if (!sv) return -GFS_EINVAL;
     if (gfs__activate(sv->ctx)) return -GFS_EIO;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_serve, SV_WARPS * 32, 0) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_serve, SV_WARPS * 32, serve_tbl_smem(sv)) != cudaSuccess) {
         cudaGetLastError();
         per_sm = 0; /* unknown: no cap */
     }
@@ -2884,9 +2919,10 @@ int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_re
     D.parts = sv->parts;
     D.q_head = sv->head + 1;
     D.q_tail = sv->head + 2;
+    D.tbl_smem = serve_tbl_smem(sv);
     const uint32_t page = gfs_page_size(sv->ctx);
     const int blocks = sv->sms * (gfs_serve_warps_per_sm(sv, warps_per_sm) / SV_WARPS);
-    k_serve<<<blocks, SV_WARPS * 32, 0, s>>>((gfs_state*)gfs_device_state(sv->ctx), D);
+    k_serve<<<blocks, SV_WARPS * 32, D.tbl_smem, s>>>((gfs_state*)gfs_device_state(sv->ctx), D);
     if (cudaGetLastError() != cudaSuccess) {
         gfs__dev_free(sv->ctx, acc, s);
         cudaFreeHost(comp_h);
