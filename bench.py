@@ -933,6 +933,16 @@ def _served_bytes(reqs, sizes):
     return tot
 
 
+def _hist_quantiles(hist, qs):
+    """Quantiles (us) of a log2 histogram (bucket b: [2**b, 2**(b+1)) ns),
+    each taken as the upper edge of the bucket it falls in."""
+    import numpy as np
+    c = np.cumsum(hist.astype(np.float64))
+    if c[-1] <= 0:
+        return None
+    return {"p%g" % q: float(2.0 ** (int(np.searchsorted(c, q / 100.0 * c[-1])) + 1) / 1e3) for q in qs}
+
+
 def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
     import resource
     import numpy as np
@@ -988,7 +998,8 @@ def _run_served(args, rank, ws, local, td, d, nt, workers, link, extra, clk):
         loads.append({"offered_frac": frac, "offered_rps": rate, "achieved_rps": n_req / dur,
                       "gbs": _served_bytes(reqs, sizes) / dur / 1e9,
                       "p50_us": float(np.percentile(lat, 50)), "p99_us": float(np.percentile(lat, 99)),
-                      "p999_us": float(np.percentile(lat, 99.9)), "errors": int((r["status"] != 0).sum())})
+                      "p999_us": float(np.percentile(lat, 99.9)), "errors": int((r["status"] != 0).sum()),
+                      "device_service_us": _hist_quantiles(sv.service_hist(), (50, 99, 99.9))})
         checks.append((reqs, r))
     # the plain per-call path: the same kind of requests, one call (one launch) each
     single = _served_trace(sizes, 300, n_out, rng)

@@ -95,6 +95,7 @@ _SIGS = {
     "gfs_serve_run": (_int, [_c_p, _c_p, _int, _c_p, _u64, _int]),
     "gfs_serve_close": (_int, [_c_p]),
     "gfs_serve_warps_per_sm": (_int, [_c_p, _int]),
+    "gfs_serve_service_hist": (_int, [_c_p, _c_p, _int]),
     "gfs_grep_bench": (_int, [_c_p, _int, _int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "gfs_drop_cache": (_i64, [_c_p]),
     "gfs_retained_pages": (_i64, [_c_p]),
@@ -453,6 +454,13 @@ class Server:
                                       res.ctypes.data if reqs.size else None, int(inflight_pages), warps_per_sm),
                "gfs_serve_run")
         return res
+
+    def service_hist(self):
+        """The last run's device-side histogram of service times: element b
+        counts requests served in [2**b, 2**(b+1)) ns."""
+        out = np.zeros(64, dtype=np.uint64)
+        _check(self.s.L.gfs_serve_service_hist(self._h, out.ctypes.data, out.size), "gfs_serve_service_hist")
+        return out
 
     def warps_per_sm(self, asked=32):
         """Serving warps per SM a run asked for `asked` uses (whole blocks of

@@ -1196,9 +1196,11 @@ struct SvComp { /* completion, indexed by request id: done is written last */
  * publishes the completion. */
 struct SvAcc {
     unsigned long long count;
-    uint32_t left; /* parts not finished */
-    int status;    /* the first part's error */
+    uint32_t left;         /* parts not finished */
+    int status;            /* the first part's error */
+    unsigned long long t0; /* %globaltimer when a warp took the request */
 };
+#define SV_HIST 64 /* service-time histogram: bucket b counts times in [2^b, 2^(b+1)) ns */
 struct SvPart { /* a slot of the part queue (sequence protocol as the ring) */
     uint32_t seq;
     uint32_t id, file, unused;
@@ -1226,6 +1228,7 @@ struct ServeDev {
     uint32_t* q_tail;       /* next part position to reserve */
     uint32_t tbl_smem;      /* bytes of slot tags + displacements staged in each block's
                                dynamic shared memory (0: read from global memory) */
+    unsigned long long* hist; /* SV_HIST buckets of device service time (device memory) */
 };
 #define SV_WARPS 8
 #define SV_STAGE (GR_LB + GR_SEG + GR_LA + 16)
@@ -1467,7 +1470,12 @@ __device__ int sv_write(gfs_state* S, int fd, uint64_t off, uint64_t len, uint32
 }
 
 /* publish a request's completion (lane 0) */
+/* publish a request's completion (lane 0), after counting its device
+ * service time -- from the take of its ticket's request to now -- in the
+ * run's histogram */
 __device__ __forceinline__ void sv_complete(const ServeDev& D, uint32_t id, unsigned long long res, int status) {
+    const unsigned long long dt = gtimer() - D.acc[id].t0;
+    atomicAdd(&D.hist[63 - __clzll((long long)(dt | 1ull))], 1ull);
     SvComp* c = &D.comp[id];
     asm volatile("st.relaxed.sys.global.u64 [%0], %1;" ::"l"(&c->result), "l"(res) : "memory");
     asm volatile("st.relaxed.sys.global.u32 [%0], %1;" ::"l"(&c->status), "r"((uint32_t)status) : "memory");
@@ -1673,6 +1681,7 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_serve(gfs_state* S, ServeDev 
         if (!have) return;
         const uint32_t op = __shfl_sync(0xFFFFFFFFu, a.y, 0), file = __shfl_sync(0xFFFFFFFFu, a.z, 0),
                        id = __shfl_sync(0xFFFFFFFFu, a.w, 0);
+        if (lane == 0) D.acc[id].t0 = gtimer(); /* ordered before any part of it is queued */
         const uint64_t off = ((uint64_t)__shfl_sync(0xFFFFFFFFu, b.y, 0) << 32) | __shfl_sync(0xFFFFFFFFu, b.x, 0);
         const uint64_t len = ((uint64_t)__shfl_sync(0xFFFFFFFFu, b.w, 0) << 32) | __shfl_sync(0xFFFFFFFFu, b.z, 0);
         unsigned long long res = 0;
@@ -2756,6 +2765,7 @@ struct gfs_server {
     int* out_fds = nullptr;
     uint32_t* head = nullptr;
     SvPart* parts = nullptr;  /* part queue of split greps */
+    unsigned long long last_hist[SV_HIST] = {}; /* the last run's service-time histogram */
     SvReq* ring_h = nullptr;  /* mapped */
     SvReq* ring_d = nullptr;
     uint32_t ring_n = 0;
@@ -2898,10 +2908,13 @@ int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_re
     for (uint32_t i = 0; i < sv->ring_n; i++) __atomic_store_n(&sv->ring_h[i].seq, i, __ATOMIC_RELAXED);
     __atomic_store_n(sv->stop_h, 0u, __ATOMIC_RELEASE);
     cudaMemsetAsync(sv->head, 0, 4, s);
-    /* split greps: an accumulator per request id, the part queue reset */
-    SvAcc* acc = (SvAcc*)gfs__dev_alloc(sv->ctx, (size_t)(n ? n : 1) * sizeof(SvAcc), s);
+    /* an accumulator per request id (split greps, service start times), the
+     * part queue reset, the service-time histogram after the accumulators */
+    const size_t acc_bytes = ((size_t)(n ? n : 1) * sizeof(SvAcc) + 255u) & ~(size_t)255u;
+    SvAcc* acc = (SvAcc*)gfs__dev_alloc(sv->ctx, acc_bytes + SV_HIST * 8, s);
     if (!acc) { cudaFreeHost(comp_h); return -GFS_ENOMEM; }
-    cudaMemsetAsync(acc, 0, (size_t)(n ? n : 1) * sizeof(SvAcc), s);
+    unsigned long long* hist = (unsigned long long*)((uint8_t*)acc + acc_bytes);
+    cudaMemsetAsync(acc, 0, acc_bytes + SV_HIST * 8, s);
     k_sv_reset<<<(SV_QCAP + 255u) / 256u, 256, 0, s>>>(sv->parts, sv->head + 1);
     ServeDev D{};
     D.G = sv->dict->dev;
@@ -2920,6 +2933,7 @@ int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_re
     D.q_head = sv->head + 1;
     D.q_tail = sv->head + 2;
     D.tbl_smem = serve_tbl_smem(sv);
+    D.hist = hist;
     const uint32_t page = gfs_page_size(sv->ctx);
     const int blocks = sv->sms * (gfs_serve_warps_per_sm(sv, warps_per_sm) / SV_WARPS);
     k_serve<<<blocks, SV_WARPS * 32, D.tbl_smem, s>>>((gfs_state*)gfs_device_state(sv->ctx), D);
@@ -2992,10 +3006,18 @@ int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_re
     __atomic_store_n(sv->stop_h, 1u, __ATOMIC_RELEASE);
     cudaError_t e = cudaStreamSynchronize(s);
     poller.join();
+    if (e == cudaSuccess) e = cudaMemcpy(sv->last_hist, hist, sizeof sv->last_hist, cudaMemcpyDeviceToHost);
     gfs__dev_free(sv->ctx, acc, s);
     cudaFreeHost(comp_h);
     if (e != cudaSuccess) return -GFS_EIO;
     return rc;
+}
+
+int gfs_serve_service_hist(gfs_server* sv, unsigned long long* out, int n) {
+    if (!sv || n < 0 || (n && !out)) return -GFS_EINVAL;
+    const int k = n < SV_HIST ? n : SV_HIST;
+    for (int i = 0; i < k; i++) out[i] = sv->last_hist[i];
+    return SV_HIST;
 }
 
 int gfs_serve_close(gfs_server* sv) {

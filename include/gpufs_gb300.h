@@ -259,6 +259,11 @@ int gfs_serve_run(gfs_server* sv, const gfs_serve_req* reqs, int n, gfs_serve_re
                   int warps_per_sm);
 /* the serving warps per SM a run asked for `warps_per_sm` uses */
 int gfs_serve_warps_per_sm(gfs_server* sv, int warps_per_sm);
+/* the last run's histogram of device service times, counted on the device:
+ * out[b] = requests served in [2^b, 2^(b+1)) ns, from the take of the
+ * request to its completion (the host-side latency adds queueing, admission
+ * and the ring); copies min(n, 64) buckets, returns 64 */
+int gfs_serve_service_hist(gfs_server* sv, unsigned long long* out, int n);
 /* closes every file (dirty output pages are written back) */
 int gfs_serve_close(gfs_server* sv);
 

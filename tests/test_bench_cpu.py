@@ -136,3 +136,15 @@ def test_clock_reasons_name_thermal_and_hw_slowdowns():
     c.f.write("0, 1500, 2070, 900, 0x48, Active, Not Active, Active, Not Active\n")
     c.p = _DoneProc()
     assert c.stop()["reasons"] == ["hw_slowdown", "sw_thermal_slowdown"]
+
+
+def test_hist_quantiles_take_bucket_upper_edges():
+    h = np.zeros(64, dtype=np.uint64)
+    h[10] = 50   # [1024, 2048) ns
+    h[20] = 49   # [~1.05 ms, ~2.1 ms)
+    h[30] = 1
+    q = bench._hist_quantiles(h, (50, 99, 99.9))
+    assert q["p50"] == 2048 / 1e3
+    assert q["p99"] == 2 ** 21 / 1e3
+    assert q["p99.9"] == 2 ** 31 / 1e3
+    assert bench._hist_quantiles(np.zeros(64, dtype=np.uint64), (50,)) is None

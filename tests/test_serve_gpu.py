@@ -159,3 +159,22 @@ def test_serving_warps_are_resident(built, shm_dir):
             got = [sv.warps_per_sm(w) for w in (1, 8, 16, 24, 32, 64)]
     assert all(w % 8 == 0 and 8 <= w <= max(8, asked) for w, asked in zip(got, (1, 8, 16, 24, 32, 64)))
     assert got == sorted(got) and got[1] == 8 and got[-1] < 64
+
+
+def test_device_service_histogram(built, shm_dir):
+    """The served kernel counts every request's device service time (from
+    the take of its request to its completion) in a log2 histogram: one
+    count per request, none below 256 ns or above 2**40 ns, and the device
+    time of the slowest bucket no longer than the host-measured latency of
+    the slowest request."""
+    paths, dpath, outs, rng = _setup(shm_dir, seed=95)
+    reqs = _requests(paths, outs, rng, 120, 0)
+    with g.Session(log_page=16, pool_bytes=64 << 20, max_files=64, timeout_s=30) as s:
+        with g.Server(s, dpath, paths, outs) as sv:
+            res = sv.run(reqs)
+            hist = sv.service_hist()
+    assert hist.sum() == reqs.size
+    nz = np.nonzero(hist)[0]
+    assert nz.min() >= 8 and nz.max() <= 40
+    host_max_ns = int((res["complete_ns"].astype(np.int64) - reqs["arrival_ns"].astype(np.int64)).max())
+    assert 2 ** int(nz.max()) <= host_max_ns
