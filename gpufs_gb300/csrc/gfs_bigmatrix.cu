@@ -36,8 +36,7 @@ long long gfs__sum_results(long long* d, int n, cudaStream_t s);
 
 namespace {
 
-__device__ unsigned int g_init_lock; /* INIT_LOCK of the reference sample */
-__device__ unsigned long long g_bm_next; /* next group of eight rows to take (reset per launch) */
+
 
 /* a group of eight rows taken ahead, with its matrix page pinned */
 struct PageAhead {
@@ -156,7 +155,8 @@ __device__ __noinline__ void dot_rows8(const float* a, size_t stride4, const flo
  * has one (one pass over a cold matrix: no cache pages, SM loads over the
  * host link) */
 __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
-    k_bigmatrix(const char* f_v, const char* f_m, const char* f_o, float* x_scratch, long long* res, int direct) {
+    k_bigmatrix(const char* f_v, const char* f_m, const char* f_o, float* x_scratch, long long* res, int direct,
+                unsigned int* init_lock, unsigned long long* next_group) {
     __shared__ float red[8 * 32];
     __shared__ float ys[8];
     __shared__ int s_fail;
@@ -190,10 +190,10 @@ __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
      * store of y, so the truncation overlaps their first rows */
     if (threadIdx.x == 0) {
         s_fail = 0;
-        if (atomicCAS(&g_init_lock, 0u, 1u) == 0u) {
+        if (atomicCAS(init_lock, 0u, 1u) == 0u) {
             single_thread_ftruncate(zfd_o, 0);
             __threadfence();
-            atomicExch(&g_init_lock, 2u);
+            atomicExch(init_lock, 2u);
         }
     }
     __syncthreads();
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
             inited = true;
             if (threadIdx.x == 0) {
                 const unsigned long long deadline = gfs_globaltimer() + 30000000000ULL;
-                while (atomicAdd(&g_init_lock, 0u) != 2u) {
+                while (atomicAdd(init_lock, 0u) != 2u) {
                     if (gfs_globaltimer() > deadline) { s_fail = -GFS_ETIMEDOUT; break; }
                     __nanosleep(1000);
                 }
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
     if (ahead) {
         const uint32_t mw = blockDim.x / 32u - 1u, warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
         auto take = [&](PageAhead* d) {
-            d->g = atomicAdd(&g_bm_next, 1ull);
+            d->g = atomicAdd(next_group, 1ull);
             d->err = 0;
             d->fresh = 0;
             d->frame = -1;
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(GFS_BIGMATRIX_THREADS, 1)
         }
     }
     for (uint32_t it = 0; !ahead && !result && cols; it++) {
-        if (threadIdx.x == 0) s_grp[it & 1u] = atomicAdd(&g_bm_next, 1ull);
+        if (threadIdx.x == 0) s_grp[it & 1u] = atomicAdd(next_group, 1ull);
         __syncthreads();
         const uint64_t gi = s_grp[it & 1u];
         if (gi >= groups) break;
@@ -427,12 +427,14 @@ static int bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, c
     char* d = (char*)gfs__scratch(ctx, 256 + sizeof(long long) * (size_t)nblocks);
     if (!d) return -GFS_ENOMEM;
     long long* res = (long long*)(d + 256);
+    /* names at 0..191; the launch's control words (the sample's INIT_LOCK
+     * and the next row group to take) at 192 and 200, zeroed per launch so
+     * that launches of other sessions never share them; results from 256 */
+    static_assert(3 * GFS_NAME_MAX <= 192, "names fit before the control words");
     cudaMemcpyAsync(d, names, sizeof names, cudaMemcpyHostToDevice, s);
-    cudaMemsetAsync(res, 0, sizeof(long long) * (size_t)nblocks, s);
-    unsigned int zero = 0;
-    cudaMemcpyToSymbolAsync(g_init_lock, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, s);
-    const unsigned long long zero64 = 0;
-    cudaMemcpyToSymbolAsync(g_bm_next, &zero64, sizeof zero64, 0, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(d + 192, 0, 64 + sizeof(long long) * (size_t)nblocks, s);
+    unsigned int* init_lock = (unsigned int*)(d + 192);
+    unsigned long long* next_group = (unsigned long long*)(d + 200);
     /* x scratch only when x does not fit a page */
     float* xs = nullptr;
     long long vbytes = 0;
@@ -448,7 +450,8 @@ static int bigmatrix(gfs_ctx* ctx, const char* vec_path, const char* mat_path, c
         cudaEventCreate(&b);
         cudaEventRecord(a, s);
     }
-    k_bigmatrix<<<nblocks, nthreads, 0, s>>>(d, d + GFS_NAME_MAX, d + 2 * GFS_NAME_MAX, xs, res, direct);
+    k_bigmatrix<<<nblocks, nthreads, 0, s>>>(d, d + GFS_NAME_MAX, d + 2 * GFS_NAME_MAX, xs, res, direct, init_lock,
+                                             next_group);
     cudaError_t le = cudaGetLastError();
     if (kernel_ms) {
         cudaEventRecord(b, s);
