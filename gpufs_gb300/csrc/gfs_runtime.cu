@@ -47,6 +47,7 @@
 #include <atomic>
 #include <memory>
 #include <mutex>
+#include <random>
 #include <unordered_map>
 #include <thread>
 #include <vector>
@@ -793,21 +794,53 @@ struct RetainedCache {
     std::unordered_multimap<uint64_t, FileMap*> maps;
     size_t mapped_bytes = 0;
     uint64_t map_clock = 0;
+    /* a token in device memory of its own, written when the cache is kept:
+     * after a cudaDeviceReset the kept allocations are gone (and a new
+     * allocation may take their addresses), so the cache is only touched if
+     * every kept pointer is still device memory of this device and the
+     * token reads back unchanged */
+    uint64_t* token_d = nullptr;
+    uint64_t token = 0;
 };
 static std::mutex g_retained_mu;
 static RetainedCache* g_retained = nullptr; /* under g_retained_mu */
 
+/* the kept allocations still belong to this process's context on r's
+ * device (the caller has made that device current) */
+static bool retained_alive(const RetainedCache* r) {
+    const void* ptrs[] = {r->pool, r->frames, r->index, r->bucket_lock, r->files, r->dirty_bits, r->token_d};
+    for (const void* p : ptrs) {
+        cudaPointerAttributes a;
+        if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeDevice ||
+            a.device != r->device) {
+            cudaGetLastError();
+            return false;
+        }
+    }
+    uint64_t t = 0;
+    if (cudaMemcpy(&t, r->token_d, sizeof t, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return t == r->token;
+}
+
+/* Free a kept cache; one whose allocations did not survive (a device
+ * reset in between) is dropped without freeing what is no longer ours. */
 static void retained_free(RetainedCache* r) {
     if (!r) return;
     int cur = -1;
     if (cudaGetDevice(&cur) != cudaSuccess) cur = -1;
     cudaSetDevice(r->device);
-    cudaFree(r->pool);
-    cudaFree(r->frames);
-    cudaFree(r->index);
-    cudaFree(r->bucket_lock);
-    cudaFree(r->files);
-    cudaFree(r->dirty_bits);
+    if (retained_alive(r)) {
+        cudaFree(r->pool);
+        cudaFree(r->frames);
+        cudaFree(r->index);
+        cudaFree(r->bucket_lock);
+        cudaFree(r->files);
+        cudaFree(r->dirty_bits);
+        cudaFree(r->token_d);
+    }
     for (auto& e : r->maps) map_release(e.second);
     if (cur >= 0) cudaSetDevice(cur);
     cudaGetLastError();
@@ -871,6 +904,17 @@ static void retain_cache(gfs_ctx* c) {
     r->files = s.files;
     r->dirty_bits = s.dirty_bits;
     r->pages = h[1];
+    r->token = ((uint64_t)std::random_device{}() << 32) ^ (uint64_t)std::random_device{}() ^
+               (uint64_t)(uintptr_t)r ^ 0x9E3779B97F4A7C15ull;
+    if (cudaMalloc(&r->token_d, sizeof r->token) != cudaSuccess ||
+        cudaMemcpy(r->token_d, &r->token, sizeof r->token, cudaMemcpyHostToDevice) != cudaSuccess) {
+        /* no token, no keeping: nothing has left the session yet, which
+         * frees its cache as usual */
+        cudaGetLastError();
+        if (r->token_d) cudaFree(r->token_d);
+        delete r;
+        return;
+    }
     {
         std::lock_guard<std::mutex> lk(c->map_mu);
         for (auto& e : c->maps) {
@@ -1006,10 +1050,12 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
             if (RetainedCache* r = g_retained) {
                 g_retained = nullptr;
                 if ((cfg.flags & GFS_CFG_RETAIN_CACHE) && r->device == cfg.device && r->log_page == s.log_page &&
-                    r->n_frames == s.n_frames && r->n_buckets == s.n_buckets && r->n_files == s.n_files)
+                    r->n_frames == s.n_frames && r->n_buckets == s.n_buckets && r->n_files == s.n_files &&
+                    retained_alive(r)) {
                     adopt = r;
-                else
+                } else {
                     retained_free(r);
+                }
             }
         }
         if (adopt) {
@@ -1023,6 +1069,7 @@ int gfs_create(const gfs_config* cfg_in, gfs_ctx** out) {
             c->maps.swap(adopt->maps);
             c->mapped_bytes = adopt->mapped_bytes;
             c->map_clock = adopt->map_clock;
+            cudaFree(adopt->token_d);
             delete adopt;
         } else {
             CK(cudaMalloc(&s.pool, nf * page));

@@ -101,9 +101,10 @@ long long gfs_drop_cache(gfs_ctx* ctx);
 long long gfs_retained_pages(gfs_ctx* ctx);
 /* free a retained cache that no session has taken over (gfs_create without
  * GFS_CFG_RETAIN_CACHE, or with another geometry, frees it too); returns 1
- * if one was freed, 0 if none was kept.  A retained cache lives in the
- * process's CUDA context: call this before cudaDeviceReset(), which would
- * free the cache's memory under it. */
+ * if one was kept.  A retained cache lives in the process's CUDA context; a
+ * cudaDeviceReset() frees its memory, after which no session takes it over
+ * (its pointers and a token in device memory are checked first) and this
+ * call drops it without freeing anything. */
 int gfs_release_retained(void);
 /* pinned host<->device cudaMemcpyAsync bandwidth, best of `reps` (GB/s) */
 int gfs_measure_link(uint64_t bytes, int reps, float* h2d_gbs, float* d2h_gbs);

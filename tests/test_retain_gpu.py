@@ -100,3 +100,47 @@ def test_grep_corpus_stays_resident_across_sessions(shm_dir):
     want = oracle.grep_counts(open(dpath, "rb").read(), [open(q, "rb").read() for q in paths], mode="fast")
     assert np.array_equal(first, want)
     assert np.array_equal(second, want)
+
+
+_RESET_SCRIPT = r"""
+import ctypes, os, sys
+sys.path.insert(0, %r)
+import numpy as np
+import gpufs_gb300 as g
+p = %r
+a = np.random.default_rng(7).integers(0, 256, (1 << 20) + 33, dtype=np.uint8)
+a.tofile(p)
+geom = dict(log_page=16, pool_bytes=64 << 20, max_files=64, timeout_s=20)
+rt = ctypes.CDLL("libcudart.so.13")
+with g.Session(retain_cache=True, **geom) as s:
+    assert np.array_equal(s.pread(p), a)
+assert rt.cudaDeviceReset() == 0
+# the kept cache did not survive the reset: a new session starts empty, and
+# reads the file again
+with g.Session(retain_cache=True, **geom) as s:
+    assert s.retained_pages == 0, s.retained_pages
+    assert np.array_equal(s.pread(p), a)
+    assert s.last_error() == 0
+# a cache kept and then orphaned by a reset is dropped (not freed) on release
+with g.Session(retain_cache=True, **geom) as s:
+    assert np.array_equal(s.pread(p), a)
+assert rt.cudaDeviceReset() == 0
+assert g.release_retained_cache() == 1
+with g.Session(**geom) as s:
+    assert np.array_equal(s.pread(p), a)
+print("reset-guard-ok")
+"""
+
+
+def test_kept_cache_does_not_survive_a_device_reset(shm_dir):
+    """A cudaDeviceReset between sessions frees a kept cache's memory under
+    it: the next retaining session must not take it over (its pointers are
+    checked, and a token in device memory read back, before any use), and
+    releasing such a cache frees nothing that is no longer ours.  Runs in a
+    child process, since the reset ends every CUDA object of the process."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = _RESET_SCRIPT % (root, os.path.join(shm_dir, "reset.bin"))
+    out = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0 and "reset-guard-ok" in out.stdout, out.stdout[-2000:] + out.stderr[-2000:]
