@@ -3,14 +3,17 @@
  * y = A x with A (rows x cols FP32, row-major) and x read through gmmap, y
  * written through gmmap of a write-once file.
  *
- * Blocks take groups of eight rows from a launch-wide counter and keep one
- * matrix page mapped at a time (the reference's get_row, :45-60, remaps only
- * when the cursor leaves the page; the reference gives each block a fixed
- * run of rows); eight whole rows of a page are one pass in which every
- * thread keeps sixteen 16-byte loads in flight; rows are reduced in a fixed
- * order (warp shuffles, then one warp over the partials), so results are
- * deterministic -- the reference adds the per-thread partials with a
- * shared-memory float atomicAdd (:35), whose order varies run to run.
+ * Blocks take groups of eight rows from a counter of the launch (the
+ * reference gives each block a fixed run of rows) and map the matrix page
+ * under the group (the reference's get_row, :45-60, remaps only when the
+ * cursor leaves the page).  Where every group lies in one page, the block's
+ * last warp pins the next group's page while the others stream the current
+ * one, so a block holds at most two matrix pages; otherwise one page is
+ * mapped at a time.  Eight whole rows of a page are one pass in which every
+ * streaming thread keeps sixteen 16-byte loads in flight; rows are reduced
+ * in a fixed order (warp shuffles, then one warp over the partials), so
+ * results are deterministic -- the reference adds the per-thread partials
+ * with a shared-memory float atomicAdd (:35), whose order varies run to run.
  *
  * This translation unit is compiled without the 64-register cap of the
  * device-API units: the kernel is bounded at 512 threads a block, which
