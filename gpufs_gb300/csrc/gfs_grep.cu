@@ -7,22 +7,28 @@
  * dictionary word and rescans every 16 KiB corpus chunk for it -- O(words x
  * corpus bytes).  Here the corpus is read once:
  *
- *   - one persistent 1024-thread CTA per SM owns a contiguous run of 16 KiB
- *     chunks of the concatenated corpus; warp 0 pins the run's pages in the
- *     buffer cache 32 at a time (one lane per page, host reads in parallel
- *     on a miss) and thread 0 streams chunks from the page frames into a
- *     4-stage shared-memory ring with 1D TMA bulk copies (cp.async.bulk,
- *     mbarrier completion, bounded waits);
- *   - each warp classifies a 512-byte segment with SWAR byte arithmetic
- *     (16 bytes per lane), finds token starts/ends from the alpha bitmasks
- *     and a shuffle across lanes, and compacts the tokens into a per-warp
- *     list so every lane works on one token;
- *   - a token is hashed from its zero-padded bytes and looked up in a
- *     bucketised cuckoo table (2 choices x 4 slots, 12-bit tags) held in
- *     shared memory; a tag hit is verified against the 32-byte record (L2),
- *     and the slot's 20-bit counter in shared memory is incremented;
+ *   - one persistent 1024-thread CTA per SM owns a contiguous run of
+ *     15,872-byte chunks of the concatenated corpus; warp 31 pins the run's
+ *     pages in windows (one lane per page, misses in parallel) and streams
+ *     chunks from the page frames into a 3-stage shared-memory ring with 1D
+ *     TMA bulk copies (cp.async.bulk, mbarrier completion, bounded waits),
+ *     asking L2 for the chunks ahead;
+ *   - warps 0..30 take (chunk, 512-byte segment) items in order; a segment
+ *     is classified with SWAR byte arithmetic (16 bytes per lane), its token
+ *     starts compacted into a per-warp list, and each lane then looks up two
+ *     tokens per round;
+ *   - a token's key (its zero-padded bytes) is hashed and looked up in a
+ *     hash-and-displace table in shared memory (gfs_grep_common.h): one
+ *     displacement and one 16-bit tag per token; a tag hit is verified
+ *     against the 32-byte record and adds to the slot's 32-bit counter;
  *   - counters are flushed to counts[word][file] with global atomics when
- *     the CTA moves to another file (or a counter reaches 2^19).
+ *     the CTA's consumers move to another file.
+ *
+ * The same kernel, instantiated otherwise, is the one-pass direct scan (each
+ * warp loads its segment's window straight from the file's registered host
+ * mapping) and the batched scan (CTAs take whole files, a hasher warp adds
+ * each file's XXH64).  The served loop (k_serve) runs the segment scanner on
+ * requested ranges.  The table is built on the device at open (k_tb_*).
  *
  * Exactness: a token counts for record w iff it equals w (match_string
  * semantics; empty records never match, duplicate records all count).  The
