@@ -13,10 +13,13 @@
  *   blk_close  <- gclose       fs_calls.cu:35-105
  *
  * GB300 changes: up to 32 pages of one request are faulted in parallel, one
- * lane per page (warp-cooperative lookup), so a block keeps up to 32 host
- * reads in flight; then all warps copy, each warp a page segment with
- * 16-byte cache-global vectors.  Reads clamp at end of file and return the
- * byte count (the reference returns `size` whatever it read).
+ * lane per page; missed pages of a file with a registered host mapping are
+ * filled by the whole block from the mapping (SM loads over the host link,
+ * no request to the host), others by the host in parallel; then all threads
+ * copy with 16-byte vectors.  gmmap fills a missed page the same way.
+ * Dirty pages are staged for write-back by the closing block's warps.
+ * Reads clamp at end of file and return the byte count (the reference
+ * returns `size` whatever it read).
  */
 #ifndef GFS_BLOCK_CUH
 #define GFS_BLOCK_CUH

@@ -17,12 +17,18 @@
  *     is a single 64-bit word written while the frame is unpinnable);
  *   - misses allocate with a clock (second-chance) sweep that evicts clean
  *     frames and writes dirty ones back through the host when it must;
+ *   - a miss of a file with a registered host mapping can come back fresh
+ *     (GFS_PIN_SMFILL) for the caller's own threads to fill from the
+ *     mapping, with no request to the host; dirty frames of at most 256 KiB
+ *     are staged by the SMs into mapped host slots for write-back;
  *   - every wait is bounded by %globaltimer and returns -GFS_ETIMEDOUT with
  *     a sticky error bit instead of spinning forever (the reference's
- *     WAIT_ON_MEM, util.cu.h:28, never gives up);
- *   - requests to the host are 128-byte slots of an MPMC ring in mapped
- *     pinned host memory; completions come back as a word in device memory
- *     written in stream order after the data has landed.
+ *     WAIT_ON_MEM, util.cu.h:28, never gives up); once the bit is set,
+ *     waits on the host fail at once;
+ *   - requests to the host are 136-byte slots of an MPMC ring in mapped
+ *     pinned host memory, published by one release store of the slot's
+ *     sequence word; completions come back as a word in mapped host memory
+ *     that the host worker writes after the data has landed.
  */
 #ifndef GFS_DEVICE_CUH
 #define GFS_DEVICE_CUH

@@ -11,17 +11,21 @@
  * hand-off per batch, an extra device staging copy per page, and a D2H copy
  * plus stream synchronisation per written page.  Here:
  *   - `host_workers` threads consume one MPMC request ring (mapped pinned
- *     memory, 128-byte slots, sequence-numbered) for the whole lifetime of
+ *     memory, 136-byte slots, sequence-numbered) for the whole lifetime of
  *     the session, so kernels may run at any time, not only inside the
  *     handler call;
- *   - reads go pread -> pinned staging -> cudaMemcpyAsync straight into the
- *     page frame on the worker's own stream (no device staging copy); the
- *     worker itself writes the request's completion word, in mapped host
- *     memory, once the copy's event has fired -- nothing in the completion
- *     path is executed by the GPU, so a kernel that occupies every SM while
- *     it waits cannot hold up its own completions;
+ *   - read-only files are mmap'ed and registered before kernels open them;
+ *     most misses of such files are then filled by the SMs themselves, and
+ *     those that reach the host are one cudaMemcpyAsync from the mapping
+ *     into the page frame; other reads go pread -> pinned staging ->
+ *     cudaMemcpyAsync into the frame (no device staging copy); the worker
+ *     itself writes the request's completion word, in mapped host memory,
+ *     once the copy's event has fired -- nothing in the completion path is
+ *     executed by the GPU, so a kernel that occupies every SM while it
+ *     waits cannot hold up its own completions;
  *   - open replies are written into mapped host memory, no copy at all;
- *   - writes go D2H -> (OR-merge for write-once files) -> pwrite;
+ *   - writes come either staged by the SMs in mapped write-stage slots or
+ *     as a D2H copy, then (OR-merge for write-once files) -> pwrite;
  *   - staging slots are recycled in issue order as their events complete;
  *   - every kernel is loaded at session creation: a lazily loaded kernel
  *     launched while a file-system kernel runs stalls driver calls.
