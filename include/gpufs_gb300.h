@@ -72,9 +72,11 @@ void gfs_default_config(gfs_config* cfg);
  * Files opened read-only are mapped and registered with CUDA on their first
  * open (kept across closes while unchanged: same inode, size and ctime, and
  * released at destroy or when over half the host memory is mapped), so a
- * page miss is one copy-engine DMA from the host page cache into the frame;
- * other files, and any file whose mapping fails, go through pread into
- * pinned staging as the reference does (host_loop.h:431-557). */
+ * page miss is filled by the missing block's own loads from the host page
+ * cache, or by one copy-engine DMA from it into the frame; other files, and
+ * any file whose mapping fails, go through pread into pinned staging as the
+ * reference does (host_loop.h:431-557).  Dirty pages of at most 256 KiB are
+ * staged by the GPU into mapped host slots for write-back. */
 int gfs_create(const gfs_config* cfg, gfs_ctx** out);
 /* replaces GPUGlobals::~GPUGlobals (libgpufs/fs_initializer.cu.h:180-198) */
 int gfs_destroy(gfs_ctx* ctx);
@@ -203,9 +205,9 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
 /* n_ctas <= 0: one per SM.  *kernel_ms (optional): device time of the scan. */
 int gfs_grep_run(gfs_grep* g, int n_ctas, float* kernel_ms);
 /* The same scan, read once: chunks of files that have a registered host
- * mapping are loaded by the GPU straight from it (cp.async over the
- * host link), bypassing the buffer cache, as O_DIRECT does; other files go
- * through the cache.  No reference counterpart (the sample reads through
+ * mapping are loaded by the GPU straight from it (16-byte SM loads over
+ * the host link), bypassing the buffer cache, as O_DIRECT does; other files
+ * go through the cache.  No reference counterpart (the sample reads through
  * the cache). */
 int gfs_grep_run_direct(gfs_grep* g, int n_ctas, float* kernel_ms);
 int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts);
@@ -229,7 +231,8 @@ int gfs_grep_batch(gfs_grep* g, int n_ctas, unsigned long long* host_xxh, float*
  * A persistent kernel whose warps take (file, offset, length, op) requests
  * from a ring in mapped host memory and serve them through the buffer
  * cache; served files are opened once and stay open on the device.
- * Offsets must be 16-byte aligned (else -GFS_EINVAL for that request). */
+ * Read and grep ranges start at any byte; write ranges must start 16-byte
+ * aligned (else -GFS_EINVAL for that request). */
 #define GFS_SV_READ 1  /* read the range of a served file; result: its XXH64 (seed 0) */
 #define GFS_SV_GREP 2  /* result: tokens of the range (read as a text of its own) that are dictionary words */
 #define GFS_SV_WRITE 3 /* write the request's byte pattern over the range of an output file; result: bytes */
