@@ -108,6 +108,9 @@ struct GrepDev {
     /* direct scan: files with a registered host mapping are read from it by
      * the SMs, bypassing the buffer cache */
     const uint64_t* maps;         /* per file: device address of its host mapping, 0 if none */
+    /* per file: where the bytes that the reference's chunk walk reads a
+     * second time start (the file size when there are none; k_grep_tail) */
+    const uint64_t* tail_start;
 };
 
 /* Shared-memory bytes of the table's parts (each a multiple of 128); the
@@ -1169,6 +1172,45 @@ __global__ void k_grep_fixup(gfs_state* S, GrepDev P) {
     pc.release();
 }
 
+/* One block per file; thread 0 counts the tokens of [tail_start, size) once
+ * more.  The reference's walk moves its cursor by 16384 after its last
+ * window too (grep_text_gpu.cu:318), so when that window is longer than
+ * 16384 bytes the loop goes round again and reads the bytes past the cursor
+ * (at most 31) as a window of their own: their alpha runs, cut at the
+ * window's start, are counted a second time.  The host finds tail_start by
+ * the same walk. */
+static __global__ void k_grep_tail(gfs_state* S, GrepDev P) {
+    const int f = blockIdx.x;
+    if (threadIdx.x != 0 || f >= P.n_files) return;
+    const uint64_t size = P.sizes[f];
+    uint64_t q = P.tail_start[f];
+    if (q >= size) return;
+    PageCursor pc;
+    pc.S = S;
+    pc.pf = pin_file(S, P.fds[f]);
+    while (q < size) {
+        const int c = pc.byte(q);
+        if (c < 0) {
+            atomicOr(P.status, GFS_ERRB_IO);
+            break;
+        }
+        if (!is_alpha((uint32_t)c)) {
+            q++;
+            continue;
+        }
+        uint64_t e = q + 1u;
+        int ce = 0;
+        while (e < size && (ce = pc.byte(e)) >= 0 && is_alpha((uint32_t)ce)) e++;
+        if (ce < 0) {
+            atomicOr(P.status, GFS_ERRB_IO);
+            break;
+        }
+        count_piece(P, pc, q, e, f);
+        q = e;
+    }
+    pc.release();
+}
+
 template __global__ void k_grep_scan<true, false, false>(gfs_state*, GrepDev);
 template __global__ void k_grep_scan<false, false, false>(gfs_state*, GrepDev);
 template __global__ void k_grep_scan<true, true, false>(gfs_state*, GrepDev);
@@ -2137,6 +2179,15 @@ struct gfs_grep {
     /* batched run: captured once per grid size, replayed */
     cudaGraphExec_t batch_graph = nullptr;
     int batch_ctas = 0;
+    /* the bytes the reference's chunk walk reads twice (k_grep_tail): host
+     * threads started at open walk the files; the first run joins them and
+     * copies the per-file starts to the device */
+    std::vector<int> hfds;              /* device file slot of each file */
+    std::vector<uint64_t> tail;         /* per file: start, its size if none, ~0 if unreadable */
+    std::vector<std::thread> tail_threads;
+    std::atomic<int> tail_next{0};      /* next file to walk */
+    bool tail_joined = true;
+    int tail_files = 0, tail_err = 0;   /* files with such bytes; -errno */
 };
 
 /* Pages per window so that all CTAs' pinned windows (two each) fit in half
@@ -2160,7 +2211,7 @@ static uint64_t host_us() {
  * zero padded to their shared-memory sizes (the scan copies them whole). */
 struct PlanLayout {
     size_t o_tbl, o_disp, o_recs, o_sw, o_nd, o_names, o_cnt, o_fds, o_sz, o_pf, o_fl, o_st, o_fo, o_fn, o_xxh,
-        o_maps, total;
+        o_maps, o_tail, total;
 };
 static PlanLayout plan_layout(uint32_t m, uint32_t r, int n_words, int n_files) {
     PlanLayout L;
@@ -2180,9 +2231,119 @@ static PlanLayout plan_layout(uint32_t m, uint32_t r, int n_words, int n_files) 
     L.o_fn = align_up(L.o_fo + (size_t)n_files * 4, 256);
     L.o_xxh = align_up(L.o_fn + 64, 256);
     L.o_maps = align_up(L.o_xxh + (size_t)n_files * 8, 256);
-    L.total = align_up(L.o_maps + (size_t)n_files * 8, 256);
+    L.o_tail = align_up(L.o_maps + (size_t)n_files * 8, 256);
+    L.total = align_up(L.o_tail + (size_t)n_files * 8, 256);
     return L;
 }
+
+/* ---------------- the bytes the reference's walk reads twice ---------------- */
+static inline bool host_alpha(uint8_t c) { return (uint32_t)(c | 32u) - 97u < 26u || c == 95u; }
+
+/* The reference's chunk walk over one file (grep_text_gpu.cu:298-318):
+ * windows of 16384 + 32 bytes; a window short of the end moves the cursor
+ * 16384 bytes plus the letters that begin its 32-byte halo (find_overlap,
+ * :89-101), the last window 16384 bytes as well, so when the last window is
+ * longer than 16384 bytes the loop goes round once more and reads the bytes
+ * past the cursor again.  Returns where those bytes start, `size` when there
+ * are none, or UINT64_MAX when a halo could not be read.  halo(off, h) reads
+ * the 32 bytes at off (always inside the file); ahead(off, n) may prefetch
+ * bytes that a later step reads. */
+template <class Halo, class Ahead>
+static uint64_t walk_tail_start(uint64_t size, Halo&& halo, Ahead&& ahead) {
+    const uint64_t W = 16384u, H = 32u;
+    uint64_t c = 0;
+    while (size - c >= W + H) {
+        /* the cursor four windows on is in [c + 4W, c + 4(W + H)], so its
+         * halo is in [c + 5W, c + 5W + 5H) */
+        ahead(c + 5u * W, 5u * H);
+        uint8_t h[32];
+        if (!halo(c + W, h)) return UINT64_MAX;
+        uint64_t ov = 0;
+        while (ov < H && host_alpha(h[ov])) ov++;
+        c += W + ov;
+    }
+    return size - c > W ? c + W : size;
+}
+
+/* the walk over bytes in host memory (a file's mapping) */
+static uint64_t tail_start_mem(const uint8_t* b, uint64_t size) {
+    return walk_tail_start(
+        size,
+        [&](uint64_t off, uint8_t* h) {
+            memcpy(h, b + off, 32);
+            return true;
+        },
+        [&](uint64_t off, uint64_t n) {
+            const uint64_t e = off + n < size ? off + n : size;
+            for (uint64_t a = off & ~(uint64_t)63; a < e; a += 64) __builtin_prefetch(b + a);
+        });
+}
+
+/* the walk over an open file slot: its host mapping, else pread */
+static uint64_t tail_start_slot(gfs_ctx* ctx, uint32_t slot, uint64_t size) {
+    const uint8_t* base = nullptr;
+    unsigned long long len = 0;
+    if (gfs__slot_map_host(ctx, slot, &base, &len) > 0 && base && len >= size) return tail_start_mem(base, size);
+    return walk_tail_start(
+        size, [&](uint64_t off, uint8_t* h) { return gfs__slot_pread(ctx, slot, h, 32, off) == 32; },
+        [](uint64_t, uint64_t) {});
+}
+
+static void tail_walk_files(gfs_grep* g) {
+    for (int f; (f = g->tail_next.fetch_add(1)) < g->n_files;)
+        g->tail[(size_t)f] = tail_start_slot(g->ctx, (uint32_t)g->hfds[(size_t)f], g->sizes[(size_t)f]);
+}
+
+/* Starts the walk of every file on host threads (called once the files are
+ * open on the device and their slots known). */
+static void tail_walk_start(gfs_grep* g) {
+    g->tail.assign((size_t)g->n_files, 0);
+    g->tail_next.store(0);
+    g->tail_joined = false;
+    unsigned nt = std::thread::hardware_concurrency() / 2u;
+    nt = nt < 1u ? 1u : (nt > 8u ? 8u : nt);
+    if (nt > (unsigned)g->n_files) nt = (unsigned)g->n_files;
+    try {
+        for (unsigned i = 0; i < nt; i++) g->tail_threads.emplace_back(tail_walk_files, g);
+    } catch (...) {
+        /* no thread: tail_finish walks what is left itself */
+    }
+}
+
+/* Finishes the walk (the calling thread takes the files still unclaimed),
+ * joins it and, once, copies the per-file starts to the device on stream s.
+ * Returns the number of files with bytes read twice, or -errno. */
+static int tail_finish(gfs_grep* g, cudaStream_t s) {
+    if (!g->tail_joined) {
+        tail_walk_files(g);
+        for (auto& t : g->tail_threads) t.join();
+        g->tail_threads.clear();
+        g->tail_joined = true;
+        int n = 0;
+        for (int i = 0; i < g->n_files && !g->tail_err; i++) {
+            const uint64_t t = g->tail[(size_t)i];
+            if (t == UINT64_MAX) g->tail_err = -GFS_EIO;
+            else if (t < g->sizes[(size_t)i]) n++;
+        }
+        g->tail_files = n;
+        if (!g->tail_err && n &&
+            cudaMemcpyAsync((void*)g->dev.tail_start, g->tail.data(), (size_t)g->n_files * 8, cudaMemcpyHostToDevice,
+                            s) != cudaSuccess)
+            g->tail_err = -GFS_EIO;
+    }
+    return g->tail_err ? g->tail_err : g->tail_files;
+}
+
+/* Stops the walk without finishing it (the plan is closing). */
+static void tail_abandon(gfs_grep* g) {
+    if (g->tail_joined) return;
+    g->tail_next.store(g->n_files);
+    for (auto& t : g->tail_threads) t.join();
+    g->tail_threads.clear();
+    g->tail_joined = true;
+}
+
+extern "C" uint64_t gfs__grep_tail_start(const uint8_t* bytes, uint64_t size) { return tail_start_mem(bytes, size); }
 
 /* Device build of the dictionary table (the dictionary's n_words records
  * are in pinned host memory at hdict; flag is 8 spare pinned bytes).  On
@@ -2344,7 +2505,8 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     const PlanLayout L = plan_layout(m, r, n_words, n_files);
     const size_t o_tbl = L.o_tbl, o_disp = L.o_disp, o_recs = L.o_recs, o_sw = L.o_sw, o_nd = L.o_nd,
                  o_names = L.o_names, o_cnt = L.o_cnt, o_fds = L.o_fds, o_sz = L.o_sz, o_pf = L.o_pf, o_fl = L.o_fl,
-                 o_st = L.o_st, o_fo = L.o_fo, o_fn = L.o_fn, o_xxh = L.o_xxh, o_maps = L.o_maps, total = L.total;
+                 o_st = L.o_st, o_fo = L.o_fo, o_fn = L.o_fn, o_xxh = L.o_xxh, o_maps = L.o_maps, o_tail = L.o_tail,
+                 total = L.total;
     g->dmem = gfs__dev_alloc(ctx, total, s);
     if (!g->dmem || !(hb = (uint8_t*)gfs__host_bounce(ctx, tmp ? names_bytes : o_cnt))) {
         gfs__dev_free(ctx, tmp, s);
@@ -2421,6 +2583,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     d.file_next = (uint32_t*)(b + o_fn);
     d.xxh = (unsigned long long*)(b + o_xxh);
     d.maps = (const uint64_t*)(b + o_maps);
+    d.tail_start = (const uint64_t*)(b + o_tail);
     const uint64_t t_open = host_us();
     k_open_files<<<n_files, 128, 0, s>>>((const char*)(b + o_names), n_files, (int*)d.fds, (uint64_t*)d.sizes);
     /* slots and sizes back through the pinned buffer (the image copy before
@@ -2432,6 +2595,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     if (cudaStreamSynchronize(s) != cudaSuccess) { gfs_grep_close(g); return -GFS_EIO; }
     g->open_us = (long long)(host_us() - t_open);
     g->sizes.assign(szs, szs + n_files);
+    g->hfds.assign(fds, fds + n_files);
     for (int i = 0; i < n_files; i++)
         if (fds[i] < 0) {
             int e = fds[i];
@@ -2477,6 +2641,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     cudaFuncSetAttribute(k_grep_scan<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
     cudaFuncSetAttribute(k_grep_scan<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
     cudaFuncSetAttribute(k_grep_scan<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
+    tail_walk_start(g);
     *out = g;
     return 0;
 }
@@ -2519,7 +2684,10 @@ static int grep_run(gfs_grep* g, int n_ctas, float* kernel_ms, int direct, uint3
         else k_grep_scan<false, false, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
     }
     cudaError_t le = cudaGetLastError();
-    k_grep_fixup<<<g->n_files, 32, 0, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
+    k_grep_fixup<<<g->n_files, 32, 0, s>>>(S, d);
+    /* the host finishes the walk while the scan runs */
+    const int n_tail = tail_finish(g, s);
+    if (n_tail > 0) k_grep_tail<<<g->n_files, 32, 0, s>>>(S, d);
     if (kernel_ms) {
         cudaEventRecord(b, s);
         cudaEventSynchronize(b);
@@ -2542,7 +2710,8 @@ static int grep_run(gfs_grep* g, int n_ctas, float* kernel_ms, int direct, uint3
     }
     g->last_status[0] = status[0];
     g->last_status[1] = status[1];
-    return status[0] ? -((status[0] & GFS_ERRB_TIMEOUT) ? GFS_ETIMEDOUT : GFS_EIO) : 0;
+    if (status[0]) return -((status[0] & GFS_ERRB_TIMEOUT) ? GFS_ETIMEDOUT : GFS_EIO);
+    return n_tail < 0 ? n_tail : 0;
 }
 
 /* Counts of up to 16 MiB go straight from the device into the caller's
@@ -2585,6 +2754,8 @@ int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* s
     GrepDev& d = g->dev;
     if (n_ctas <= 0) n_ctas = g->sms;
     gfs_state* S = (gfs_state*)gfs_device_state(g->ctx);
+    const int n_tail = tail_finish(g, s);
+    if (n_tail < 0) return n_tail;
     std::vector<cudaEvent_t> ev((size_t)steps * 2 + 2);
     for (auto& e : ev) cudaEventCreate(&e);
     cudaMemsetAsync(d.status, 0, 8, s);
@@ -2598,6 +2769,7 @@ int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* s
         else k_grep_scan<false, false, false><<<n_ctas, GR_THREADS, g->smem_bytes, s>>>(S, d);
         cudaEventRecord(ev[3 + 2 * (size_t)i], s);
         k_grep_fixup<<<g->n_files, 32, 0, s>>>(S, d);
+        if (n_tail > 0) k_grep_tail<<<g->n_files, 32, 0, s>>>(S, d);
     }
     cudaEventRecord(ev[1], s);
     cudaError_t e = cudaEventSynchronize(ev[1]);
@@ -2659,6 +2831,8 @@ int gfs_grep_batch(gfs_grep* g, int n_ctas, unsigned long long* host_xxh, float*
     cudaEventCreate(&b);
     cudaEventRecord(a, s);
     cudaError_t le = cudaGraphLaunch(g->batch_graph, s);
+    const int n_tail = tail_finish(g, s); /* on the host while the batch runs */
+    if (n_tail > 0) k_grep_tail<<<g->n_files, 32, 0, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
     cudaEventRecord(b, s);
     cudaError_t e = cudaStreamSynchronize(s); /* kernels first, then copies back */
     if (kernel_ms) cudaEventElapsedTime(kernel_ms, a, b);
@@ -2673,7 +2847,8 @@ int gfs_grep_batch(gfs_grep* g, int n_ctas, unsigned long long* host_xxh, float*
     g->last_status[0] = status[0];
     g->last_status[1] = status[1];
     if (host_xxh) cudaMemcpy(host_xxh, d.xxh, (size_t)g->n_files * 8, cudaMemcpyDeviceToHost);
-    return status[0] ? -((status[0] & GFS_ERRB_TIMEOUT) ? GFS_ETIMEDOUT : GFS_EIO) : 0;
+    if (status[0]) return -((status[0] & GFS_ERRB_TIMEOUT) ? GFS_ETIMEDOUT : GFS_EIO);
+    return n_tail < 0 ? n_tail : 0;
 }
 
 int gfs_grep_counts(gfs_grep* g, uint32_t* host_counts) {
@@ -2739,6 +2914,7 @@ void* gfs_grep_device_counts(gfs_grep* g) { return g ? (void*)g->dev.counts : nu
 
 int gfs_grep_close(gfs_grep* g) {
     if (!g) return 0;
+    tail_abandon(g);
     int rc = 0;
     if (g->dmem && g->dev.fds) {
         gfs__activate(g->ctx);

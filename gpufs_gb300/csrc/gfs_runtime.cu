@@ -1332,6 +1332,29 @@ int gfs__slot_map(gfs_ctx* c, uint32_t slot, unsigned long long* dev_addr, unsig
     return 1;
 }
 
+int gfs__slot_map_host(gfs_ctx* c, uint32_t slot, const uint8_t** base, unsigned long long* len) {
+    *base = nullptr;
+    *len = 0;
+    if (!c || !c->slots || slot >= c->hs.n_files) return -GFS_EINVAL;
+    HostSlot& h = c->slots[slot];
+    std::lock_guard<std::mutex> lk(h.mu);
+    FileMap* m = h.open ? h.map.load(std::memory_order_acquire) : nullptr;
+    if (!m) return 0;
+    *base = m->base;
+    *len = m->len;
+    return 1;
+}
+
+long long gfs__slot_pread(gfs_ctx* c, uint32_t slot, void* buf, size_t n, uint64_t off) {
+    if (!c || !c->slots || slot >= c->hs.n_files) return -GFS_EINVAL;
+    const int fd = slot_acquire_fd(c, slot);
+    if (fd < 0) return fd;
+    const ssize_t r = pread_full(fd, (uint8_t*)buf, n, (off_t)off);
+    const int e = errno;
+    slot_release_fd(c, slot);
+    return r < 0 ? -(long long)e : (long long)r;
+}
+
 void* gfs__host_bounce(gfs_ctx* c, size_t bytes) {
     if (bytes > c->h_bounce_cap) {
         if (c->h_bounce) cudaFreeHost(c->h_bounce);

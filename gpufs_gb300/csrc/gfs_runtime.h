@@ -23,6 +23,15 @@ void gfs__dev_free(gfs_ctx* c, void* p, cudaStream_t s);
 /* the registered host mapping of an open file slot, as a device address and
  * its length (0 when the slot has none); valid while the slot stays open */
 int gfs__slot_map(gfs_ctx* c, uint32_t slot, unsigned long long* dev_addr, unsigned long long* len);
+/* the same mapping's host address (1), or 0 when the slot has none */
+int gfs__slot_map_host(gfs_ctx* c, uint32_t slot, const uint8_t** base, unsigned long long* len);
+/* pread through an open slot's host fd (reopened by name if it was closed
+ * past the open-file limit); bytes read or -errno */
+long long gfs__slot_pread(gfs_ctx* c, uint32_t slot, void* buf, size_t n, uint64_t off);
+/* where the bytes that the reference's grep chunk walk reads twice start in
+ * a file held in memory (its size when there are none): the host walk the
+ * grep plans run over each file, callable on its own */
+uint64_t gfs__grep_tail_start(const uint8_t* bytes, uint64_t size);
 int gfs__activate(gfs_ctx* c);
 /* register a file's host mapping from the calling thread before a kernel
  * opens it read-only (the open then makes no CUDA call on a host worker) */

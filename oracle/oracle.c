@@ -17,8 +17,10 @@
  *   - orc_grep_file_faithful restates the reference's per-file chunk loop
  *     (grep_text_gpu.cu:89-101 `find_overlap`, :298-329) around match_string.
  *   - orc_grep_counts_fast is the single-pass restatement (tokenise once, hash
- *     lookup); it is checked against orc_grep_file_faithful on random and
- *     adversarial inputs.
+ *     lookup, plus the walk's cut points and the tail it reads twice:
+ *     orc_grep_split_points, orc_grep_tail_start); it is checked against
+ *     orc_grep_file_faithful on random, adversarial and property-generated
+ *     inputs.
  *   - orc_gemv_f64 is the FP64 host GEMV the bigmatrix sample is checked against
  *     (samples/bigmatrix_mmap/bigmatrix_mmap.cu:24-41 computes the FP32 dot).
  */
@@ -200,6 +202,20 @@ size_t orc_grep_split_points(const uint8_t* file, size_t size, uint64_t* out, si
     return n;
 }
 
+/* Start of the bytes the reference's chunk walk reads twice, or `size` when
+ * there are none.  The walk moves its cursor by 16384 after its last window
+ * too (grep_text_gpu.cu:318: `_cursor += CORPUS_PREFETCH_SIZE` whatever
+ * last_iter says), so when that window is longer than 16384 bytes the cursor
+ * is still inside the file and the loop reads the bytes past it once more, as
+ * a window of their own (at most 31 bytes, NUL-terminated like any last
+ * window).  Their tokens are counted a second time. */
+size_t orc_grep_tail_start(const uint8_t* file, size_t size) {
+    size_t cursor = 0;
+    while (size - cursor >= (size_t)(REF_CHUNK + REF_HALO))
+        cursor += REF_CHUNK + (size_t)orc_find_overlap(file + cursor + REF_CHUNK);
+    return size - cursor > (size_t)REF_CHUNK ? cursor + REF_CHUNK : size;
+}
+
 /* ------------------------------------------------------------------------- */
 /* Single-pass restatement: tokenise once, look each token up.                */
 /* ------------------------------------------------------------------------- */
@@ -307,6 +323,18 @@ static void orc_count_file(const orc_dict* d, const uint8_t* f, size_t n, uint32
         }
     }
     free(splits);
+    /* the bytes the walk reads a second time: their tokens (alpha runs cut
+     * at the window's start) count again */
+    for (i = orc_grep_tail_start(f, n); i < n;) {
+        if (!orc_alpha(f[i])) { i++; continue; }
+        size_t s = i;
+        while (i < n && orc_alpha(f[i])) i++;
+        int w = orc_dict_find(d, f + s, (int)(i - s));
+        while (w >= 0) {
+            counts[(size_t)w * n_files + col] += 1;
+            w = d->next_dup[w];
+        }
+    }
 }
 
 typedef struct {

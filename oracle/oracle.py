@@ -57,6 +57,8 @@ def L():
         lib.orc_grep_file_faithful_word.argtypes = [ctypes.c_char_p, vp, ctypes.c_size_t]
         lib.orc_grep_split_points.restype = ctypes.c_size_t
         lib.orc_grep_split_points.argtypes = [vp, ctypes.c_size_t, vp, ctypes.c_size_t]
+        lib.orc_grep_tail_start.restype = ctypes.c_size_t
+        lib.orc_grep_tail_start.argtypes = [vp, ctypes.c_size_t]
         for fn in ("orc_grep_counts_faithful",):
             getattr(lib, fn).argtypes = [vp, i, vp, vp, i, vp]
         for fn in ("orc_grep_counts_fast", "orc_grep_counts_refalgo"):
@@ -141,6 +143,13 @@ def split_points(data):
     out = np.zeros(max(1, n), dtype=np.uint64)
     L().orc_grep_split_points(a.ctypes.data, a.size, out.ctypes.data, n)
     return out[:n]
+
+
+def tail_start(data):
+    """Offset of the bytes the reference's chunk walk reads a second time
+    (len(data) when there are none)."""
+    a = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8))
+    return int(L().orc_grep_tail_start(a.ctypes.data if a.size else None, a.size))
 
 
 def gemv_f64(A, x, nthreads=None):

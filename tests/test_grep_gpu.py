@@ -338,3 +338,65 @@ def test_counts_into_any_host_buffer(sess, shm_dir, shift):
         assert np.array_equal(view.reshape(want.shape), want)
         assert np.all(raw[:base] == 0xAB) and np.all(raw[base + n * 4:] == 0xAB)  # nothing outside written
     assert np.array_equal(g.grep_text(sess, dpath, paths), want)
+
+
+def _walk_cursors(b):
+    """Cursors of the reference's chunk walk over b (windows of 16384 + 32
+    bytes; a window short of the end moves on by 16384 plus the letters that
+    begin its halo)."""
+    alpha = set(range(65, 91)) | set(range(97, 123)) | {95}
+    c, out = 0, [0]
+    while len(b) - c >= 16416:
+        ov = 0
+        while ov < 32 and b[c + 16384 + ov] in alpha:
+            ov += 1
+        c += 16384 + ov
+        out.append(c)
+    return out
+
+
+def test_bytes_the_reference_reads_twice(sess, shm_dir):
+    """When the reference's last window is longer than 16384 bytes its walk
+    goes round once more and counts the tokens past 16384 a second time
+    (grep_text_gpu.cu:298-318).  Files cut so, small (read with pread) and
+    large (read through their mappings, after windows whose halos began with
+    letters), give the oracle's counts in every form: cached, direct,
+    batched and one call."""
+    voc = datagen.vocab(300, seed=71, minlen=2, maxlen=5)
+    dpath = os.path.join(shm_dir, "dict.gpu")
+    datagen.dictionary(dpath, voc, 300, seed=72)
+    raw = open(dpath, "rb").read()
+    words = [raw[i:i + 32].rstrip(b"\0") for i in range(0, len(raw), 32)]
+    words = [w for w in words if w and b"\0" not in w]
+    big = os.path.join(shm_dir, "z.txt")
+    datagen.zipf_files([big], [600000], voc, s=1.1, seed=73)
+    z = open(big, "rb").read()
+    cs = _walk_cursors(z)
+    texts = [b" " * 16384 + words[0] + b" " + words[1],                    # one window of 16384 + a few
+             b"x" * 16380 + words[2] + b"." + words[0]]                      # a word cut by the second read
+    for k in (5, 17, len(cs) - 3):                                            # mapped files (> 64 KiB)
+        for d in range(31, 0, -1):
+            t = z[:cs[k] + 16384 + d]
+            if oracle.tail_start(t) < len(t) and any(w in t[cs[k] + 16384:] for w in words):
+                texts.append(t)
+                break
+    texts.append(z)
+    paths = []
+    for i, t in enumerate(texts):
+        p = os.path.join(shm_dir, "t%d.txt" % i)
+        _write(p, t)
+        paths.append(p)
+    assert sum(oracle.tail_start(t) < len(t) for t in texts) >= 4
+    want = oracle.grep_counts(raw, texts, mode="fast")
+    for i, t in enumerate(texts):
+        if len(t) < 100000:
+            assert np.array_equal(want[:, i], oracle.grep_counts(raw, [t], mode="faithful")[:, 0]), i
+    with g.Grep(sess, dpath, paths) as gr:
+        gr.run(direct=True)
+        assert np.array_equal(gr.counts(), want)
+        gr.run()
+        assert np.array_equal(gr.counts(), want)
+        gr.batch()
+        assert np.array_equal(gr.counts(), want)
+    assert np.array_equal(g.grep_text(sess, dpath, paths), want)
+    assert sess.last_error() == 0
