@@ -2179,14 +2179,13 @@ struct gfs_grep {
     /* batched run: captured once per grid size, replayed */
     cudaGraphExec_t batch_graph = nullptr;
     int batch_ctas = 0;
-    /* the bytes the reference's chunk walk reads twice (k_grep_tail): host
-     * threads started at open walk the files; the first run joins them and
-     * copies the per-file starts to the device */
+    /* the bytes the reference's chunk walk reads twice (k_grep_tail): the
+     * first run walks the files on host threads while its scan runs */
     std::vector<int> hfds;              /* device file slot of each file */
-    std::vector<uint64_t> tail;         /* per file: start, its size if none, ~0 if unreadable */
-    std::vector<std::thread> tail_threads;
+    uint64_t* tail = nullptr;           /* per file: start, its size if none, ~0 if unreadable;
+                                           mapped pinned memory, read by k_grep_tail */
     std::atomic<int> tail_next{0};      /* next file to walk */
-    bool tail_joined = true;
+    bool tail_done = false;
     int tail_files = 0, tail_err = 0;   /* files with such bytes; -errno */
 };
 
@@ -2211,7 +2210,7 @@ static uint64_t host_us() {
  * zero padded to their shared-memory sizes (the scan copies them whole). */
 struct PlanLayout {
     size_t o_tbl, o_disp, o_recs, o_sw, o_nd, o_names, o_cnt, o_fds, o_sz, o_pf, o_fl, o_st, o_fo, o_fn, o_xxh,
-        o_maps, o_tail, total;
+        o_maps, total;
 };
 static PlanLayout plan_layout(uint32_t m, uint32_t r, int n_words, int n_files) {
     PlanLayout L;
@@ -2231,8 +2230,7 @@ static PlanLayout plan_layout(uint32_t m, uint32_t r, int n_words, int n_files) 
     L.o_fn = align_up(L.o_fo + (size_t)n_files * 4, 256);
     L.o_xxh = align_up(L.o_fn + 64, 256);
     L.o_maps = align_up(L.o_xxh + (size_t)n_files * 8, 256);
-    L.o_tail = align_up(L.o_maps + (size_t)n_files * 8, 256);
-    L.total = align_up(L.o_tail + (size_t)n_files * 8, 256);
+    L.total = align_up(L.o_maps + (size_t)n_files * 8, 256);
     return L;
 }
 
@@ -2294,31 +2292,27 @@ static void tail_walk_files(gfs_grep* g) {
         g->tail[(size_t)f] = tail_start_slot(g->ctx, (uint32_t)g->hfds[(size_t)f], g->sizes[(size_t)f]);
 }
 
-/* Starts the walk of every file on host threads (called once the files are
- * open on the device and their slots known). */
-static void tail_walk_start(gfs_grep* g) {
-    g->tail.assign((size_t)g->n_files, 0);
-    g->tail_next.store(0);
-    g->tail_joined = false;
-    unsigned nt = std::thread::hardware_concurrency() / 2u;
-    nt = nt < 1u ? 1u : (nt > 8u ? 8u : nt);
-    if (nt > (unsigned)g->n_files) nt = (unsigned)g->n_files;
-    try {
-        for (unsigned i = 0; i < nt; i++) g->tail_threads.emplace_back(tail_walk_files, g);
-    } catch (...) {
-        /* no thread: tail_finish walks what is left itself */
-    }
-}
-
-/* Finishes the walk (the calling thread takes the files still unclaimed),
- * joins it and, once, copies the per-file starts to the device on stream s.
- * Returns the number of files with bytes read twice, or -errno. */
-static int tail_finish(gfs_grep* g, cudaStream_t s) {
-    if (!g->tail_joined) {
+/* Walks every file once, on up to 8 host threads and the calling one, the
+ * first time a run asks (after it has launched its scan, so the walk
+ * overlaps the scan).  Returns the number of files with bytes read twice,
+ * or -errno.  It makes no CUDA call: it runs while the plan's kernels may be
+ * waiting on the host workers, and a call that waits on the stream could
+ * hold them up. */
+static int tail_finish(gfs_grep* g) {
+    if (!g->tail_done) {
+        g->tail_next.store(0);
+        std::vector<std::thread> th;
+        unsigned nt = std::thread::hardware_concurrency() / 2u;
+        nt = nt > 8u ? 8u : nt;
+        if (nt + 1u > (unsigned)g->n_files) nt = g->n_files > 1 ? (unsigned)g->n_files - 1u : 0u;
+        try {
+            for (unsigned i = 0; i < nt; i++) th.emplace_back(tail_walk_files, g);
+        } catch (...) {
+            /* fewer threads: this one walks what is left */
+        }
         tail_walk_files(g);
-        for (auto& t : g->tail_threads) t.join();
-        g->tail_threads.clear();
-        g->tail_joined = true;
+        for (auto& t : th) t.join();
+        g->tail_done = true;
         int n = 0;
         for (int i = 0; i < g->n_files && !g->tail_err; i++) {
             const uint64_t t = g->tail[(size_t)i];
@@ -2326,21 +2320,8 @@ static int tail_finish(gfs_grep* g, cudaStream_t s) {
             else if (t < g->sizes[(size_t)i]) n++;
         }
         g->tail_files = n;
-        if (!g->tail_err && n &&
-            cudaMemcpyAsync((void*)g->dev.tail_start, g->tail.data(), (size_t)g->n_files * 8, cudaMemcpyHostToDevice,
-                            s) != cudaSuccess)
-            g->tail_err = -GFS_EIO;
     }
     return g->tail_err ? g->tail_err : g->tail_files;
-}
-
-/* Stops the walk without finishing it (the plan is closing). */
-static void tail_abandon(gfs_grep* g) {
-    if (g->tail_joined) return;
-    g->tail_next.store(g->n_files);
-    for (auto& t : g->tail_threads) t.join();
-    g->tail_threads.clear();
-    g->tail_joined = true;
 }
 
 extern "C" uint64_t gfs__grep_tail_start(const uint8_t* bytes, uint64_t size) { return tail_start_mem(bytes, size); }
@@ -2440,6 +2421,8 @@ void gfs__preload_grep() {
     cudaFuncGetAttributes(&a, k_grep_scan<false, false, true>);
     cudaFuncGetAttributes(&a, k_serve);
     cudaFuncGetAttributes(&a, k_grep_fixup);
+    cudaFuncGetAttributes(&a, k_grep_tail);
+    cudaFuncGetAttributes(&a, k_counts_out);
     cudaFuncGetAttributes(&a, k_open_files);
     cudaFuncGetAttributes(&a, k_close_files);
 }
@@ -2505,8 +2488,7 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     const PlanLayout L = plan_layout(m, r, n_words, n_files);
     const size_t o_tbl = L.o_tbl, o_disp = L.o_disp, o_recs = L.o_recs, o_sw = L.o_sw, o_nd = L.o_nd,
                  o_names = L.o_names, o_cnt = L.o_cnt, o_fds = L.o_fds, o_sz = L.o_sz, o_pf = L.o_pf, o_fl = L.o_fl,
-                 o_st = L.o_st, o_fo = L.o_fo, o_fn = L.o_fn, o_xxh = L.o_xxh, o_maps = L.o_maps, o_tail = L.o_tail,
-                 total = L.total;
+                 o_st = L.o_st, o_fo = L.o_fo, o_fn = L.o_fn, o_xxh = L.o_xxh, o_maps = L.o_maps, total = L.total;
     g->dmem = gfs__dev_alloc(ctx, total, s);
     if (!g->dmem || !(hb = (uint8_t*)gfs__host_bounce(ctx, tmp ? names_bytes : o_cnt))) {
         gfs__dev_free(ctx, tmp, s);
@@ -2583,7 +2565,6 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     d.file_next = (uint32_t*)(b + o_fn);
     d.xxh = (unsigned long long*)(b + o_xxh);
     d.maps = (const uint64_t*)(b + o_maps);
-    d.tail_start = (const uint64_t*)(b + o_tail);
     const uint64_t t_open = host_us();
     k_open_files<<<n_files, 128, 0, s>>>((const char*)(b + o_names), n_files, (int*)d.fds, (uint64_t*)d.sizes);
     /* slots and sizes back through the pinned buffer (the image copy before
@@ -2641,7 +2622,21 @@ int gfs_grep_open(gfs_ctx* ctx, const char* dict_path, const char* const* paths,
     cudaFuncSetAttribute(k_grep_scan<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
     cudaFuncSetAttribute(k_grep_scan<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)with_tbl);
     cudaFuncSetAttribute(k_grep_scan<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fixed);
-    tail_walk_start(g);
+    {
+        /* the walk's per-file starts, where k_grep_tail reads them */
+        void* th = nullptr;
+        void* td = nullptr;
+        if (cudaHostAlloc(&th, (size_t)n_files * 8, cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer(&td, th, 0) != cudaSuccess) {
+            cudaGetLastError();
+            if (th) cudaFreeHost(th);
+            gfs_grep_close(g);
+            return -GFS_ENOMEM;
+        }
+        g->tail = (uint64_t*)th;
+        g->dev.tail_start = (const uint64_t*)td;
+        for (int i = 0; i < n_files; i++) g->tail[i] = g->sizes[(size_t)i];
+    }
     *out = g;
     return 0;
 }
@@ -2686,7 +2681,7 @@ static int grep_run(gfs_grep* g, int n_ctas, float* kernel_ms, int direct, uint3
     cudaError_t le = cudaGetLastError();
     k_grep_fixup<<<g->n_files, 32, 0, s>>>(S, d);
     /* the host finishes the walk while the scan runs */
-    const int n_tail = tail_finish(g, s);
+    const int n_tail = tail_finish(g);
     if (n_tail > 0) k_grep_tail<<<g->n_files, 32, 0, s>>>(S, d);
     if (kernel_ms) {
         cudaEventRecord(b, s);
@@ -2754,7 +2749,7 @@ int gfs_grep_bench(gfs_grep* g, int n_ctas, int steps, float* total_ms, float* s
     GrepDev& d = g->dev;
     if (n_ctas <= 0) n_ctas = g->sms;
     gfs_state* S = (gfs_state*)gfs_device_state(g->ctx);
-    const int n_tail = tail_finish(g, s);
+    const int n_tail = tail_finish(g);
     if (n_tail < 0) return n_tail;
     std::vector<cudaEvent_t> ev((size_t)steps * 2 + 2);
     for (auto& e : ev) cudaEventCreate(&e);
@@ -2831,7 +2826,7 @@ int gfs_grep_batch(gfs_grep* g, int n_ctas, unsigned long long* host_xxh, float*
     cudaEventCreate(&b);
     cudaEventRecord(a, s);
     cudaError_t le = cudaGraphLaunch(g->batch_graph, s);
-    const int n_tail = tail_finish(g, s); /* on the host while the batch runs */
+    const int n_tail = tail_finish(g); /* on the host while the batch runs */
     if (n_tail > 0) k_grep_tail<<<g->n_files, 32, 0, s>>>((gfs_state*)gfs_device_state(g->ctx), d);
     cudaEventRecord(b, s);
     cudaError_t e = cudaStreamSynchronize(s); /* kernels first, then copies back */
@@ -2914,7 +2909,6 @@ void* gfs_grep_device_counts(gfs_grep* g) { return g ? (void*)g->dev.counts : nu
 
 int gfs_grep_close(gfs_grep* g) {
     if (!g) return 0;
-    tail_abandon(g);
     int rc = 0;
     if (g->dmem && g->dev.fds) {
         gfs__activate(g->ctx);
@@ -2932,6 +2926,7 @@ int gfs_grep_close(gfs_grep* g) {
     }
     if (g->batch_graph) cudaGraphExecDestroy(g->batch_graph);
     gfs__dev_free(g->ctx, g->dmem, (cudaStream_t)gfs_kernel_stream(g->ctx));
+    if (g->tail) cudaFreeHost(g->tail);
     delete g;
     return rc;
 }
