@@ -32,10 +32,15 @@
  *
  * Exactness: a token counts for record w iff it equals w (match_string
  * semantics; empty records never match, duplicate records all count).  The
- * reference's chunk walk additionally cuts an alpha run when the 32 bytes
- * after a 16384-byte window are all letters (grep_text_gpu.cu:302-318); runs
- * of >= 33 letters are flagged per file and k_grep_fixup restates that walk
- * for flagged files only, so counts equal the reference on any input.
+ * reference's chunk walk (grep_text_gpu.cu:298-318) has two more effects,
+ * both reproduced, so counts equal the reference on any input:
+ *   - it cuts an alpha run when the 32 bytes after a 16384-byte window are
+ *     all letters; runs of >= 33 letters are flagged per file and
+ *     k_grep_fixup restates the walk for flagged files only;
+ *   - a last window longer than 16384 bytes is followed by one more window
+ *     of the 1..31 bytes past 16384, whose tokens count again; host threads
+ *     find those bytes by the same walk while the first scan runs
+ *     (walk_tail_start) and k_grep_tail counts them.
  */
 #include <cuda_runtime.h>
 #include <cooperative_groups.h>
