@@ -196,7 +196,10 @@ int gfs_xxh64_files_noalloc(gfs_ctx* ctx, const char* const* paths, int n, unsig
 /* ---- grep_text (samples/grep_text/grep_text_gpu.cu:193-387) ----
  * Whole-word occurrence counts of every record of a dictionary file (32-byte
  * NUL-padded records, the reference's dict.gpu format) in every corpus file,
- * read through the buffer cache.  counts[w * n_files + f] (uint32).
+ * read through the buffer cache.  counts[w * n_files + f] (uint32), equal to
+ * the reference's on any input, including the effects of its 16 KiB window
+ * walk: letter runs cut at windows whose halo is all letters, and the last
+ * 1..31 bytes counted twice when the last window is longer than 16384.
  * gfs_grep_open reads the dictionary, builds its hash table, uploads it and
  * opens the corpus files on the device; gfs_grep_run scans (files stay open
  * and cached between runs); gfs_grep_close closes them. */
