@@ -2297,9 +2297,10 @@ static void tail_walk_files(gfs_grep* g) {
         g->tail[(size_t)f] = tail_start_slot(g->ctx, (uint32_t)g->hfds[(size_t)f], g->sizes[(size_t)f]);
 }
 
-/* Walks every file once, on up to 8 host threads and the calling one, the
- * first time a run asks (after it has launched its scan, so the walk
- * overlaps the scan).  Returns the number of files with bytes read twice,
+/* Walks every file once, on up to 4 host threads and the calling one (a
+ * quarter of the cores at most: the host workers serving the scan's page
+ * fills keep the rest), the first time a run asks, after it has launched
+ * its scan, so the walk overlaps the scan.  Returns the number of files with bytes read twice,
  * or -errno.  It makes no CUDA call: it runs while the plan's kernels may be
  * waiting on the host workers, and a call that waits on the stream could
  * hold them up. */
@@ -2307,8 +2308,8 @@ static int tail_finish(gfs_grep* g) {
     if (!g->tail_done) {
         g->tail_next.store(0);
         std::vector<std::thread> th;
-        unsigned nt = std::thread::hardware_concurrency() / 2u;
-        nt = nt > 8u ? 8u : nt;
+        unsigned nt = std::thread::hardware_concurrency() / 4u;
+        nt = nt > 4u ? 4u : nt;
         if (nt + 1u > (unsigned)g->n_files) nt = g->n_files > 1 ? (unsigned)g->n_files - 1u : 0u;
         try {
             for (unsigned i = 0; i < nt; i++) th.emplace_back(tail_walk_files, g);
