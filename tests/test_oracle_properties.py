@@ -24,6 +24,8 @@ words = st.lists(
         st.binary(min_size=0, max_size=0),                                      # empty record
         st.lists(st.sampled_from(WORD_BYTES), min_size=1, max_size=6).map(bytes),
         st.lists(st.sampled_from(WORD_BYTES), min_size=28, max_size=32).map(bytes),
+        # records with bytes that are not letters: no token can equal them
+        st.lists(st.sampled_from(WORD_BYTES + list(b"9' -") + [0x80, 0xFF]), min_size=1, max_size=8).map(bytes),
         st.tuples(st.lists(st.sampled_from(WORD_BYTES), min_size=1, max_size=5).map(bytes),
                   st.binary(min_size=1, max_size=8)).map(lambda t: (t[0] + b"\0" + t[1])[:32]),
     ),
